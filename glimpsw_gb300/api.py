@@ -1,0 +1,374 @@
+"""Python mirror of GLimpSW's renderer API over the C ABI of libswr_gb300.so (ctypes).
+
+Names follow the reference: ``Rasterizer`` (src/SwRast/Rasterizer.h:202-340), ``Framebuffer`` /
+``create_framebuffer`` (Rasterizer.h:10-78), ``Texture2D`` / ``create_texture2d`` (Texture.h:314-636),
+``ShadingContext`` (Shading.h:12-50) with ``cull_meshlets``, ``resolve`` and ``VisBufferShader``,
+and ``downsample_depth`` (Texture.h:243). Errors raise ``SwrError`` carrying the status code and
+``swr_last_error()``. The CUDA library is required: importing this module on a machine without
+it raises instead of falling back to anything else.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libswr_gb300.so")
+
+SWR_OK, SWR_EINVAL, SWR_ECAPACITY, SWR_ETIMEOUT, SWR_ECUDA, SWR_ENOMEM = range(6)
+STATUS_NAMES = {0: "SWR_OK", 1: "SWR_EINVAL", 2: "SWR_ECAPACITY", 3: "SWR_ETIMEOUT", 4: "SWR_ECUDA", 5: "SWR_ENOMEM"}
+FORMAT_RGBA8U, FORMAT_R11G11B10F, FORMAT_R32F = 0, 1, 2
+VisBufferShader = 0
+MAX_RENDER_SIZE = 2896
+
+
+class SwrError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{STATUS_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class SwrMaterial(C.Structure):
+    _fields_ = [("texture", C.c_void_p), ("is_double_sided", C.c_uint8), ("alpha_cutoff", C.c_uint8)]
+
+
+class SwrLight(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("position", C.c_float * 3), ("direction", C.c_float * 3),
+                ("color", C.c_float * 3), ("intensity", C.c_float), ("radius", C.c_float),
+                ("spot_inner_angle", C.c_float), ("spot_outer_angle", C.c_float), ("inv_radius_sq", C.c_float),
+                ("spot_scale", C.c_float), ("spot_offset", C.c_float)]
+
+
+class SwrShadingContext(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("meshlet_offset", C.c_uint32), ("cull_bitmap", C.c_void_p),
+                ("world_to_clip", C.c_float * 16), ("object_to_clip", C.c_float * 16),
+                ("object_to_world", C.c_float * 9), ("skybox", C.c_void_p), ("view_pos", C.c_float * 3),
+                ("exposure", C.c_float), ("lights", C.c_void_p), ("num_lights", C.c_uint32)]
+
+
+_lib = None
+
+# name -> argtypes (all return swr_status unless listed in _RESTYPES)
+_SIGS = {
+    "swr_last_error": [],
+    "swr_set_stream": [C.c_void_p],
+    "swr_get_stream": [],
+    "swr_synchronize": [],
+    "swr_launch_count": [],
+    "swr_profile_enable": [C.c_int],
+    "swr_profile_collect": [C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p],
+    "swr_rasterizer_create": [C.c_uint32, C.c_void_p],
+    "swr_rasterizer_destroy": [C.c_void_p],
+    "swr_rasterizer_set_flags": [C.c_void_p, C.c_int, C.c_int, C.c_int],
+    "swr_rasterizer_get_counters": [C.c_void_p, C.c_void_p],
+    "swr_rasterizer_reset_counters": [C.c_void_p],
+    "swr_draw_meshlets": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p],
+    "swr_framebuffer_create": [C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p],
+    "swr_framebuffer_destroy": [C.c_void_p],
+    "swr_framebuffer_clear": [C.c_void_p, C.c_uint32, C.c_float],
+    "swr_framebuffer_clear_layer": [C.c_void_p, C.c_uint32, C.c_uint32],
+    "swr_framebuffer_get_pixels": [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32],
+    "swr_framebuffer_get_pixels_device": [C.c_void_p, C.c_uint32, C.c_void_p],
+    "swr_framebuffer_layer_data": [C.c_void_p, C.c_uint32, C.c_void_p],
+    "swr_framebuffer_invalidate": [C.c_void_p],
+    "swr_framebuffer_size": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+    "swr_scene_create": [C.c_void_p],
+    "swr_scene_destroy": [C.c_void_p],
+    "swr_scene_upload_meshlets": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32],
+    "swr_scene_set_materials": [C.c_void_p, C.c_void_p, C.c_uint32],
+    "swr_scene_meshlet_count": [C.c_void_p, C.c_void_p],
+    "swr_texture_create": [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p],
+    "swr_texture_destroy": [C.c_void_p],
+    "swr_texture_set_pixels": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32],
+    "swr_texture_generate_mips": [C.c_void_p],
+    "swr_texture_info": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+    "swr_texture_get_data": [C.c_void_p, C.c_void_p, C.c_size_t],
+    "swr_texture_set_data": [C.c_void_p, C.c_void_p, C.c_size_t],
+    "swr_cull_meshlets": [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                          C.c_void_p, C.c_float, C.c_float, C.c_void_p, C.c_void_p],
+    "swr_downsample_depth": [C.c_void_p, C.c_void_p],
+    "swr_resolve": [C.c_void_p, C.c_void_p, C.c_void_p],
+}
+_RESTYPES = {"swr_last_error": C.c_char_p, "swr_get_stream": C.c_void_p, "swr_launch_count": C.c_uint64}
+
+
+def load_library(path: str = LIB_PATH):
+    """Loads libswr_gb300.so (building it with nvcc first if it is missing). Raises if the CUDA
+    library cannot be built or loaded: there is no other implementation to fall back to."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        from . import build as _build
+        _build.build()
+    lib = C.CDLL(path)
+    for name, args in _SIGS.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = _RESTYPES.get(name, C.c_int)
+    _lib = lib
+    return lib
+
+
+def _check(code: int):
+    if code != SWR_OK:
+        raise SwrError(code, _lib.swr_last_error().decode())
+
+
+def _ptr(a) -> int:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):  # torch tensor (device memory)
+        return a.data_ptr()
+    return int(a)
+
+
+def _f16(m) -> C.Array:
+    a = np.ascontiguousarray(m, dtype=np.float32).reshape(16)
+    return (C.c_float * 16)(*a.tolist())
+
+
+def set_stream(stream) -> None:
+    """Enqueue subsequent work on a CUDA stream (an int handle or a torch.cuda.Stream)."""
+    h = getattr(stream, "cuda_stream", stream)
+    _check(load_library().swr_set_stream(h))
+
+
+def synchronize() -> None:
+    _check(load_library().swr_synchronize())
+
+
+def launch_count() -> int:
+    """Kernels this library has launched so far (all threads)."""
+    return int(load_library().swr_launch_count())
+
+
+def profile_enable(on: bool = True) -> None:
+    _check(load_library().swr_profile_enable(int(on)))
+
+
+def profile_collect(max_records: int = 4096) -> list[tuple[str, float]]:
+    """(kernel name, ms) of every launch recorded since the last collect (synchronises)."""
+    names = (C.c_char_p * max_records)()
+    ms = (C.c_float * max_records)()
+    n = C.c_uint32()
+    _check(load_library().swr_profile_collect(max_records, names, ms, C.byref(n)))
+    return [(names[i].decode(), float(ms[i])) for i in range(min(n.value, max_records))]
+
+
+class Framebuffer:
+    def __init__(self, width: int, height: int, num_layers: int = 2):
+        L = load_library()
+        h = C.c_void_p()
+        _check(L.swr_framebuffer_create(width, height, num_layers, C.byref(h)))
+        self.h = h
+        self.width, self.height, self.num_layers = width, height, num_layers
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.swr_framebuffer_destroy(self.h)
+            self.h = None
+
+    def clear(self, color: int, depth: float) -> None:
+        _check(_lib.swr_framebuffer_clear(self.h, C.c_uint32(color), C.c_float(depth)))
+
+    def clear_layer(self, layer: int, value: int) -> None:
+        _check(_lib.swr_framebuffer_clear_layer(self.h, layer, C.c_uint32(value)))
+
+    def get_pixels(self, layer: int, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty((self.height, self.width), dtype=np.uint32)
+        _check(_lib.swr_framebuffer_get_pixels(self.h, layer, out.ctypes.data, out.shape[1]))
+        return out
+
+    def get_pixels_device(self, layer: int, dest_device) -> None:
+        _check(_lib.swr_framebuffer_get_pixels_device(self.h, layer, _ptr(dest_device)))
+
+    def layer_data(self, layer: int) -> int:
+        p = C.c_void_p()
+        _check(_lib.swr_framebuffer_layer_data(self.h, layer, C.byref(p)))
+        return p.value
+
+    def invalidate(self) -> None:
+        _check(_lib.swr_framebuffer_invalidate(self.h))
+
+
+def create_framebuffer(width: int, height: int, num_layers: int = 2) -> Framebuffer:
+    return Framebuffer(width, height, num_layers)
+
+
+class Texture2D:
+    def __init__(self, fmt: int, width: int, height: int, max_levels: int = 1, num_layers: int = 1):
+        L = load_library()
+        h = C.c_void_p()
+        _check(L.swr_texture_create(fmt, width, height, max_levels, num_layers, C.byref(h)))
+        self.h = h
+        self.fmt, self.width, self.height, self.num_layers = fmt, width, height, num_layers
+        levels, stride = C.c_uint32(), C.c_uint32()
+        offs = (C.c_uint32 * 16)()
+        _check(L.swr_texture_info(self.h, C.byref(levels), C.byref(stride), offs))
+        self.mip_levels, self.layer_stride, self.mip_offsets = levels.value, stride.value, list(offs)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.swr_texture_destroy(self.h)
+            self.h = None
+
+    @property
+    def words(self) -> int:
+        return self.layer_stride * self.num_layers + 64
+
+    def set_pixels(self, pixels: np.ndarray, layer: int = 0) -> None:
+        pixels = np.ascontiguousarray(pixels, dtype=np.uint32)
+        _check(_lib.swr_texture_set_pixels(self.h, pixels.ctypes.data, pixels.shape[1], layer))
+
+    def generate_mips(self) -> None:
+        _check(_lib.swr_texture_generate_mips(self.h))
+
+    def get_data(self) -> np.ndarray:
+        out = np.empty(self.words, dtype=np.uint32)
+        _check(_lib.swr_texture_get_data(self.h, out.ctypes.data, out.size))
+        return out
+
+    def set_data(self, data: np.ndarray) -> None:
+        data = np.ascontiguousarray(data, dtype=np.uint32)
+        _check(_lib.swr_texture_set_data(self.h, data.ctypes.data, data.size))
+
+
+def create_texture2d(fmt: int, width: int, height: int, max_levels: int = 1, num_layers: int = 1) -> Texture2D:
+    return Texture2D(fmt, width, height, max_levels, num_layers)
+
+
+class Scene:
+    """Device-resident Meshlet and Material pools (Scene.h:117-128)."""
+
+    def __init__(self):
+        L = load_library()
+        h = C.c_void_p()
+        _check(L.swr_scene_create(C.byref(h)))
+        self.h = h
+        self.textures = []
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.swr_scene_destroy(self.h)
+            self.h = None
+
+    def upload_meshlets(self, meshlets: np.ndarray, first: int = 0) -> None:
+        assert meshlets.dtype.itemsize == 1728 and meshlets.flags.c_contiguous
+        _check(_lib.swr_scene_upload_meshlets(self.h, meshlets.ctypes.data, first, len(meshlets)))
+
+    def set_materials(self, materials: np.ndarray, textures: list | None = None) -> None:
+        self.textures = list(textures or [])
+        arr = (SwrMaterial * max(1, len(materials)))()
+        for i, m in enumerate(materials):
+            t = int(m["texture"])
+            arr[i].texture = self.textures[t].h.value if self.textures and t < len(self.textures) else None
+            arr[i].is_double_sided = int(m["is_double_sided"])
+            arr[i].alpha_cutoff = int(m["alpha_cutoff"])
+        _check(_lib.swr_scene_set_materials(self.h, arr, len(materials)))
+
+
+class ShadingContext:
+    """ShadingContext (Shading.h:12-50) bound to a device Scene."""
+
+    VisBufferShader = VisBufferShader
+
+    def __init__(self, scene: Scene, object_to_clip, world_to_clip=None, object_to_world=None,
+                 meshlet_offset: int = 0, cull_bitmap=None, skybox: Texture2D | None = None, view_pos=(0, 0, 0),
+                 exposure: float = 1.0, lights: list | None = None):
+        s = SwrShadingContext()
+        s.scene = scene.h.value
+        s.meshlet_offset = meshlet_offset
+        s.cull_bitmap = _ptr(cull_bitmap)
+        s.object_to_clip = _f16(object_to_clip)
+        s.world_to_clip = _f16(world_to_clip if world_to_clip is not None else object_to_clip)
+        ow = np.ascontiguousarray(object_to_world if object_to_world is not None else np.eye(3), dtype=np.float32)
+        s.object_to_world = (C.c_float * 9)(*ow.reshape(9).tolist())
+        s.skybox = skybox.h.value if skybox is not None else None
+        s.view_pos = (C.c_float * 3)(*[float(v) for v in view_pos])
+        s.exposure = exposure
+        self._lights = (SwrLight * max(1, len(lights or [])))(*(lights or []))
+        s.lights = C.cast(self._lights, C.c_void_p) if lights else None
+        s.num_lights = len(lights or [])
+        self.s = s
+        self.scene = scene
+        self._keep = (cull_bitmap, skybox)
+
+    def resolve(self, rast: "Rasterizer", fb: Framebuffer) -> None:
+        _check(_lib.swr_resolve(rast.h, fb.h, C.byref(self.s)))
+
+
+def cull_meshlets(scene: Scene, first: int, count: int, bitmap_device, proj, view, model, prev_view,
+                  frame_w: float, frame_h: float, depth_map: Texture2D | None = None, want_count: bool = False):
+    """ShadingContext::CullMeshlets (Shading.cpp:775-869) into a device bitmap (uint16 per 16)."""
+    cnt = C.c_uint32(0)
+    _check(_lib.swr_cull_meshlets(scene.h, first, count, _ptr(bitmap_device), _f16(proj), _f16(view), _f16(model),
+                                  _f16(prev_view), float(frame_w), float(frame_h),
+                                  depth_map.h if depth_map is not None else None,
+                                  C.byref(cnt) if want_count else None))
+    return cnt.value if want_count else None
+
+
+def downsample_depth(fb: Framebuffer, dest: Texture2D) -> None:
+    _check(_lib.swr_downsample_depth(fb.h, dest.h))
+
+
+class Rasterizer:
+    def __init__(self, num_threads: int = 0):
+        L = load_library()
+        h = C.c_void_p()
+        _check(L.swr_rasterizer_create(num_threads, C.byref(h)))
+        self.h = h
+        self._flags = [True, True, True]
+        self._apply()
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.swr_rasterizer_destroy(self.h)
+            self.h = None
+
+    def _apply(self):
+        _check(_lib.swr_rasterizer_set_flags(self.h, *[int(f) for f in self._flags]))
+
+    @property
+    def EnableBinning(self):
+        return self._flags[0]
+
+    @EnableBinning.setter
+    def EnableBinning(self, v):
+        self._flags[0] = bool(v)
+        self._apply()
+
+    @property
+    def EnableClipping(self):
+        return self._flags[1]
+
+    @EnableClipping.setter
+    def EnableClipping(self, v):
+        self._flags[1] = bool(v)
+        self._apply()
+
+    @property
+    def EnableGuardband(self):
+        return self._flags[2]
+
+    @EnableGuardband.setter
+    def EnableGuardband(self, v):
+        self._flags[2] = bool(v)
+        self._apply()
+
+    def draw_meshlets(self, fb: Framebuffer, count: int, ctx: ShadingContext, shader: int = VisBufferShader) -> None:
+        _check(_lib.swr_draw_meshlets(self.h, fb.h, count, shader, C.byref(ctx.s)))
+
+    def counters(self) -> np.ndarray:
+        out = np.zeros(4, dtype=np.uint64)
+        _check(_lib.swr_rasterizer_get_counters(self.h, out.ctypes.data))
+        return out
+
+    def reset_counters(self) -> None:
+        _check(_lib.swr_rasterizer_reset_counters(self.h))

@@ -1,0 +1,423 @@
+// C ABI of libswr_gb300 (include/swr_gb300.h): handles, validation, errors and the host-side
+// orchestration of the raster kernels.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/swr/hostmath.h"
+#include "swr_device.cuh"
+#include "swr_internal.h"
+
+using namespace swr;
+
+namespace {
+
+thread_local std::string t_lastError;
+thread_local cudaStream_t t_stream = cudaStreamPerThread;
+
+swr_status fail(swr_status code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    t_lastError = buf;
+    return code;
+}
+
+swr_status cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? SWR_ENOMEM : SWR_ECUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define SWR_CUDA(call)                                   \
+    do {                                                 \
+        cudaError_t e_ = (call);                         \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+#define SWR_CHECK_LAUNCH(what)                           \
+    do {                                                 \
+        cudaError_t e_ = cudaGetLastError();             \
+        if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+    } while (0)
+
+int num_sms() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 148;
+    }
+    return n;
+}
+
+constexpr uint32_t kDefaultBigCapacity = 1u << 18;
+
+swr_status ensure_scratch(swr_rasterizer r) {
+    DrawScratch& s = r->scratch;
+    if (s.control != nullptr) return SWR_OK;
+    SWR_CUDA(cudaMalloc(&s.control, 16 * sizeof(unsigned long long)));
+    SWR_CUDA(cudaMemset(s.control, 0, 16 * sizeof(unsigned long long)));
+    s.bigCapacity = kDefaultBigCapacity;
+    SWR_CUDA(cudaMalloc(&s.big, (size_t)s.bigCapacity * sizeof(TriRec)));
+    SWR_CUDA(cudaMalloc(&s.bigBase, (size_t)s.bigCapacity * sizeof(unsigned long long)));
+    return SWR_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ tracing
+namespace {
+struct ProfRec {
+    const char* name;
+    cudaEvent_t start, stop;
+};
+thread_local bool t_profiling = false;
+thread_local std::vector<ProfRec> t_prof;
+std::atomic<unsigned long long> g_launches{ 0 };
+}  // namespace
+
+swr::LaunchScope::LaunchScope(const char* name, cudaStream_t s) : st(s), rec(-1) {
+    g_launches.fetch_add(1, std::memory_order_relaxed);
+    if (!t_profiling) return;
+    ProfRec r{ name, nullptr, nullptr };
+    if (cudaEventCreate(&r.start) != cudaSuccess || cudaEventCreate(&r.stop) != cudaSuccess) return;
+    cudaEventRecord(r.start, st);
+    t_prof.push_back(r);
+    rec = (int)t_prof.size() - 1;
+}
+swr::LaunchScope::~LaunchScope() {
+    if (rec >= 0) cudaEventRecord(t_prof[rec].stop, st);
+}
+
+swr_status swr_internal_fail(swr_status code, const char* msg) { return fail(code, "%s", msg); }
+swr_status swr_internal_cuda_fail(cudaError_t e, const char* what) { return cuda_fail(e, what); }
+cudaStream_t swr_internal_stream() { return t_stream; }
+
+extern "C" {
+
+const char* swr_last_error(void) { return t_lastError.c_str(); }
+
+swr_status swr_set_stream(void* cuda_stream) {
+    t_stream = cuda_stream ? (cudaStream_t)cuda_stream : cudaStreamPerThread;
+    return SWR_OK;
+}
+void* swr_get_stream(void) { return (void*)t_stream; }
+
+swr_status swr_synchronize(void) {
+    SWR_CUDA(cudaStreamSynchronize(t_stream));
+    return SWR_OK;
+}
+
+uint64_t swr_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+swr_status swr_profile_enable(int enable) {
+    t_profiling = enable != 0;
+    return SWR_OK;
+}
+
+swr_status swr_profile_collect(uint32_t max_records, const char** names, float* ms, uint32_t* count) {
+    if (!count || (max_records && (!names || !ms))) return fail(SWR_EINVAL, "swr_profile_collect: bad argument");
+    uint32_t n = 0;
+    for (ProfRec& r : t_prof) {
+        cudaError_t e = cudaEventSynchronize(r.stop);
+        float t = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, r.start, r.stop);
+        if (e != cudaSuccess) return cuda_fail(e, "swr_profile_collect");
+        if (n < max_records) names[n] = r.name, ms[n] = t;
+        n++;
+        cudaEventDestroy(r.start);
+        cudaEventDestroy(r.stop);
+    }
+    t_prof.clear();
+    *count = n;
+    return SWR_OK;
+}
+
+// ------------------------------------------------------------------ rasterizer
+swr_status swr_rasterizer_create(uint32_t num_threads, swr_rasterizer* out) {
+    (void)num_threads;
+    if (!out) return fail(SWR_EINVAL, "swr_rasterizer_create: out is NULL");
+    swr_rasterizer r = new (std::nothrow) swr_rasterizer_t();
+    if (!r) return fail(SWR_ENOMEM, "swr_rasterizer_create: host allocation failed");
+    r->enable_binning = 1, r->enable_clipping = 1, r->enable_guardband = 1;  // Rasterizer.h:206-208
+    swr_status st = ensure_scratch(r);
+    if (st != SWR_OK) {
+        swr_rasterizer_destroy(r);
+        return st;
+    }
+    *out = r;
+    return SWR_OK;
+}
+
+swr_status swr_rasterizer_destroy(swr_rasterizer r) {
+    if (!r) return SWR_OK;
+    cudaFree(r->scratch.control);
+    cudaFree(r->scratch.big);
+    cudaFree(r->scratch.bigBase);
+    delete r;
+    return SWR_OK;
+}
+
+swr_status swr_rasterizer_set_flags(swr_rasterizer r, int enable_binning, int enable_clipping, int enable_guardband) {
+    if (!r) return fail(SWR_EINVAL, "swr_rasterizer_set_flags: NULL rasterizer");
+    r->enable_binning = enable_binning != 0;
+    r->enable_clipping = enable_clipping != 0;
+    r->enable_guardband = enable_guardband != 0;
+    return SWR_OK;
+}
+
+swr_status swr_rasterizer_get_counters(swr_rasterizer r, uint64_t out[SWR_NUM_COUNTERS]) {
+    if (!r || !out) return fail(SWR_EINVAL, "swr_rasterizer_get_counters: NULL argument");
+    unsigned long long c[16];
+    SWR_CUDA(cudaMemcpyAsync(c, r->scratch.control, sizeof(c), cudaMemcpyDeviceToHost, t_stream));
+    SWR_CUDA(cudaStreamSynchronize(t_stream));
+    out[SWR_COUNTER_TRIANGLES_PROCESSED] = c[3];
+    out[SWR_COUNTER_TRIANGLES_RASTERIZED] = c[4];
+    out[SWR_COUNTER_TRIANGLES_CLIPPED] = c[5];
+    out[SWR_COUNTER_BIN_QUEUE_FLUSHES] = c[6];
+    return SWR_OK;
+}
+
+swr_status swr_rasterizer_reset_counters(swr_rasterizer r) {
+    if (!r) return fail(SWR_EINVAL, "swr_rasterizer_reset_counters: NULL rasterizer");
+    SWR_CUDA(cudaMemsetAsync(r->scratch.control + 3, 0, 4 * sizeof(unsigned long long), t_stream));
+    return SWR_OK;
+}
+
+// ------------------------------------------------------------------ framebuffer
+swr_status swr_framebuffer_create(uint32_t width, uint32_t height, uint32_t num_layers, swr_framebuffer* out) {
+    if (!out) return fail(SWR_EINVAL, "swr_framebuffer_create: out is NULL");
+    if (width == 0 || height == 0 || width % 4 || height % 4)
+        return fail(SWR_EINVAL, "swr_framebuffer_create: %ux%u is not a non-zero multiple of 4", width, height);
+    if (width > SWR_MAX_RENDER_SIZE || height > SWR_MAX_RENDER_SIZE)
+        return fail(SWR_EINVAL, "swr_framebuffer_create: %ux%u exceeds MaxRenderSize %u", width, height, SWR_MAX_RENDER_SIZE);
+    if (num_layers < 2 || num_layers > 8)
+        return fail(SWR_EINVAL, "swr_framebuffer_create: num_layers %u outside [2, 8]", num_layers);
+    swr_framebuffer fb = new (std::nothrow) swr_framebuffer_t();
+    if (!fb) return fail(SWR_ENOMEM, "swr_framebuffer_create: host allocation failed");
+    fb->width = width, fb->height = height, fb->tile_stride = width / 4;
+    fb->layer_stride = (width * height + 63) & ~63u;  // CreateFramebuffer, Rasterizer.h:69
+    fb->num_layers = num_layers;
+    cudaError_t e = cudaMalloc(&fb->layers, ((size_t)fb->layer_stride * num_layers + 64) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&fb->keys, (size_t)fb->layer_stride * 8);
+    if (e == cudaSuccess) e = cudaMemsetAsync(fb->layers, 0, ((size_t)fb->layer_stride * num_layers + 64) * 4, t_stream);
+    if (e != cudaSuccess) {
+        swr_framebuffer_destroy(fb);
+        return cuda_fail(e, "swr_framebuffer_create");
+    }
+    fb->keys_valid = false;
+    *out = fb;
+    return SWR_OK;
+}
+
+swr_status swr_framebuffer_destroy(swr_framebuffer fb) {
+    if (!fb) return SWR_OK;
+    cudaFree(fb->layers);
+    cudaFree(fb->keys);
+    delete fb;
+    return SWR_OK;
+}
+
+swr_status swr_framebuffer_clear(swr_framebuffer fb, uint32_t color, float depth) {
+    if (!fb) return fail(SWR_EINVAL, "swr_framebuffer_clear: NULL framebuffer");
+    uint32_t d;
+    memcpy(&d, &depth, 4);
+    launch_clear(fb->layers, fb->layers + fb->layer_stride, fb->keys, fb->width * fb->height, color, d, t_stream);
+    SWR_CHECK_LAUNCH("swr_framebuffer_clear");
+    fb->keys_valid = true;
+    return SWR_OK;
+}
+
+swr_status swr_framebuffer_clear_layer(swr_framebuffer fb, uint32_t layer, uint32_t value) {
+    if (!fb || layer >= fb->num_layers) return fail(SWR_EINVAL, "swr_framebuffer_clear_layer: bad framebuffer or layer");
+    launch_fill(fb->layers + (size_t)layer * fb->layer_stride, fb->width * fb->height, value, t_stream);
+    SWR_CHECK_LAUNCH("swr_framebuffer_clear_layer");
+    if (layer <= 1) fb->keys_valid = false;
+    return SWR_OK;
+}
+
+swr_status swr_framebuffer_get_pixels_device(swr_framebuffer fb, uint32_t layer, uint32_t* dest_device) {
+    if (!fb || layer >= fb->num_layers || !dest_device)
+        return fail(SWR_EINVAL, "swr_framebuffer_get_pixels_device: bad argument");
+    launch_detile(fb->layers + (size_t)layer * fb->layer_stride, dest_device, fb->width, fb->height, t_stream);
+    SWR_CHECK_LAUNCH("swr_framebuffer_get_pixels_device");
+    return SWR_OK;
+}
+
+swr_status swr_framebuffer_get_pixels(swr_framebuffer fb, uint32_t layer, uint32_t* dest, uint32_t stride) {
+    if (!fb || layer >= fb->num_layers || !dest || stride < fb->width)
+        return fail(SWR_EINVAL, "swr_framebuffer_get_pixels: bad argument");
+    uint32_t* tmp = nullptr;
+    SWR_CUDA(cudaMallocAsync(&tmp, (size_t)fb->width * fb->height * 4, t_stream));
+    launch_detile(fb->layers + (size_t)layer * fb->layer_stride, tmp, fb->width, fb->height, t_stream);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpy2DAsync(dest, (size_t)stride * 4, tmp, (size_t)fb->width * 4, (size_t)fb->width * 4, fb->height,
+                              cudaMemcpyDeviceToHost, t_stream);
+    cudaFreeAsync(tmp, t_stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(t_stream);
+    if (e != cudaSuccess) return cuda_fail(e, "swr_framebuffer_get_pixels");
+    return SWR_OK;
+}
+
+swr_status swr_framebuffer_layer_data(swr_framebuffer fb, uint32_t layer, void** out_device_ptr) {
+    if (!fb || layer >= fb->num_layers || !out_device_ptr) return fail(SWR_EINVAL, "swr_framebuffer_layer_data: bad argument");
+    *out_device_ptr = fb->layers + (size_t)layer * fb->layer_stride;
+    return SWR_OK;
+}
+
+swr_status swr_framebuffer_invalidate(swr_framebuffer fb) {
+    if (!fb) return fail(SWR_EINVAL, "swr_framebuffer_invalidate: NULL framebuffer");
+    fb->keys_valid = false;
+    return SWR_OK;
+}
+
+swr_status swr_framebuffer_size(swr_framebuffer fb, uint32_t* width, uint32_t* height, uint32_t* layer_stride,
+                                uint32_t* num_layers) {
+    if (!fb) return fail(SWR_EINVAL, "swr_framebuffer_size: NULL framebuffer");
+    if (width) *width = fb->width;
+    if (height) *height = fb->height;
+    if (layer_stride) *layer_stride = fb->layer_stride;
+    if (num_layers) *num_layers = fb->num_layers;
+    return SWR_OK;
+}
+
+// ------------------------------------------------------------------ scene
+swr_status swr_scene_create(swr_scene* out) {
+    if (!out) return fail(SWR_EINVAL, "swr_scene_create: out is NULL");
+    swr_scene s = new (std::nothrow) swr_scene_t();
+    if (!s) return fail(SWR_ENOMEM, "swr_scene_create: host allocation failed");
+    *out = s;
+    return SWR_OK;
+}
+
+swr_status swr_scene_destroy(swr_scene s) {
+    if (!s) return SWR_OK;
+    cudaFree(s->meshlets);
+    cudaFree(s->materials);
+    delete s;
+    return SWR_OK;
+}
+
+swr_status swr_scene_upload_meshlets(swr_scene s, const void* meshlets, uint32_t first, uint32_t count) {
+    if (!s || (!meshlets && count)) return fail(SWR_EINVAL, "swr_scene_upload_meshlets: bad argument");
+    uint64_t end = (uint64_t)first + count;
+    if (end > SWR_MAX_MESHLETS)
+        return fail(SWR_EINVAL, "swr_scene_upload_meshlets: %llu meshlets exceed the limit %u", (unsigned long long)end,
+                    SWR_MAX_MESHLETS);
+    // Records are not inspected on the host (that would cost a cache miss per meshlet); kernels
+    // clamp NumVertices to 64 and NumTriangles to 128, the sizes of the record's arrays.
+    if (end > s->capacity) {
+        uint32_t cap = (uint32_t)std::max<uint64_t>(end, (uint64_t)s->capacity * 3 / 2);
+        cap = std::min(cap, SWR_MAX_MESHLETS);
+        uint8_t* p = nullptr;
+        SWR_CUDA(cudaMalloc(&p, (size_t)cap * kMeshletSize));
+        if (s->meshlets) {
+            SWR_CUDA(cudaMemcpyAsync(p, s->meshlets, (size_t)s->count * kMeshletSize, cudaMemcpyDeviceToDevice, t_stream));
+            SWR_CUDA(cudaStreamSynchronize(t_stream));
+            cudaFree(s->meshlets);
+        }
+        s->meshlets = p;
+        s->capacity = cap;
+    }
+    if (count)
+        SWR_CUDA(cudaMemcpyAsync(s->meshlets + (size_t)first * kMeshletSize, meshlets, (size_t)count * kMeshletSize,
+                                 cudaMemcpyHostToDevice, t_stream));
+    s->count = std::max(s->count, (uint32_t)end);
+    return SWR_OK;
+}
+
+swr_status swr_scene_set_materials(swr_scene s, const swr_material* materials, uint32_t count) {
+    if (!s || (!materials && count)) return fail(SWR_EINVAL, "swr_scene_set_materials: bad argument");
+    std::vector<DevMaterial> h(count);
+    for (uint32_t i = 0; i < count; i++) {
+        DevMaterial& d = h[i];
+        memset(&d, 0, sizeof(d));
+        d.is_double_sided = materials[i].is_double_sided != 0;
+        d.alpha_cutoff = materials[i].alpha_cutoff;
+        if (materials[i].texture) {
+            d.has_texture = 1;
+            d.tex = materials[i].texture->d;
+        }
+    }
+    cudaFree(s->materials);
+    s->materials = nullptr;
+    s->num_materials = 0;
+    if (count) {
+        SWR_CUDA(cudaMalloc(&s->materials, count * sizeof(DevMaterial)));
+        SWR_CUDA(cudaMemcpy(s->materials, h.data(), count * sizeof(DevMaterial), cudaMemcpyHostToDevice));
+    }
+    s->num_materials = count;
+    return SWR_OK;
+}
+
+swr_status swr_scene_meshlet_count(swr_scene s, uint32_t* out) {
+    if (!s || !out) return fail(SWR_EINVAL, "swr_scene_meshlet_count: bad argument");
+    *out = s->count;
+    return SWR_OK;
+}
+
+// ------------------------------------------------------------------ draw
+swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t count, uint32_t shader_table,
+                             const swr_shading_context* ctx) {
+    if (!r || !fb || !ctx || !ctx->scene) return fail(SWR_EINVAL, "swr_draw_meshlets: NULL argument");
+    if (shader_table != SWR_SHADER_VISBUFFER) return fail(SWR_EINVAL, "swr_draw_meshlets: unknown shader table %u", shader_table);
+    swr_scene sc = ctx->scene;
+    if ((uint64_t)ctx->meshlet_offset + count > sc->count)
+        return fail(SWR_EINVAL, "swr_draw_meshlets: meshlets [%u, %llu) outside the scene's %u", ctx->meshlet_offset,
+                    (unsigned long long)ctx->meshlet_offset + count, sc->count);
+    if (count == 0) return SWR_OK;
+    swr_status st = ensure_scratch(r);
+    if (st != SWR_OK) return st;
+    if (!fb->keys_valid) {
+        launch_init_keys(fb->layers + fb->layer_stride, fb->keys, fb->width * fb->height, t_stream);
+        SWR_CHECK_LAUNCH("swr_draw_meshlets: init keys");
+        fb->keys_valid = true;
+    }
+    DrawArgs a = {};
+    a.meshlets = sc->meshlets;
+    a.materials = sc->materials;
+    a.numMaterials = sc->num_materials;
+    a.meshletOffset = ctx->meshlet_offset;
+    a.count = count;
+    a.cullBitmap = ctx->cull_bitmap;
+    memcpy(a.m, ctx->object_to_clip, sizeof(a.m));
+    a.halfW = (int)fb->width / 2, a.halfH = (int)fb->height / 2;
+    a.width = fb->width, a.height = fb->height;
+    // DrawMeshletsST honours EnableGuardband (Rasterizer.cpp:155-156); the binned path does not (509).
+    a.bx = (float)SWR_MAX_RENDER_SIZE / (float)fb->width;
+    a.by = (float)SWR_MAX_RENDER_SIZE / (float)fb->height;
+    if (!r->enable_binning && !r->enable_guardband) a.bx = a.by = 1.0f;
+    a.clipMode = (!r->enable_binning && r->enable_clipping) ? 1 : 0;
+    a.countClipped = (r->enable_binning || r->enable_clipping) ? 1 : 0;
+    a.keys = fb->keys;
+    a.s = r->scratch;
+    SWR_CUDA(cudaMemsetAsync(r->scratch.control, 0, 3 * sizeof(unsigned long long), t_stream));
+    launch_draw(a, t_stream, num_sms());
+    SWR_CHECK_LAUNCH("swr_draw_meshlets");
+    launch_finalize(fb->keys, fb->layers, fb->layers + fb->layer_stride, fb->width * fb->height, t_stream);
+    SWR_CHECK_LAUNCH("swr_draw_meshlets: finalize");
+    return SWR_OK;
+}
+
+swr_status swr_cull_meshlets(swr_scene, uint32_t, uint32_t, uint16_t*, const float*, const float*, const float*,
+                             const float*, float, float, swr_texture, uint32_t*) {
+    return fail(SWR_EINVAL, "swr_cull_meshlets: not built yet");
+}
+swr_status swr_downsample_depth(swr_framebuffer, swr_texture) {
+    return fail(SWR_EINVAL, "swr_downsample_depth: not built yet");
+}
+swr_status swr_resolve(swr_rasterizer, swr_framebuffer, const swr_shading_context*) {
+    return fail(SWR_EINVAL, "swr_resolve: not built yet");
+}
+
+}  // extern "C"

@@ -1,0 +1,120 @@
+// Host-side object definitions behind the opaque handles of swr_gb300.h.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "../../include/swr_gb300.h"
+
+namespace swr {
+
+// Device copy of a Texture2D header (Texture.h:314-329) with its storage pointer.
+struct DevTexture {
+    uint32_t width, height, mip_levels, num_layers;
+    uint32_t row_shift, layer_stride;
+    float scale_u, scale_v, scale_lerp_u, scale_lerp_v;
+    int32_t mask_u, mask_v, mask_lerp_u, mask_lerp_v;
+    uint32_t mip_offsets[16];
+    const uint32_t* data;
+};
+
+// Device copy of a Material (Scene.h:7-14).
+struct DevMaterial {
+    uint32_t has_texture;
+    uint32_t is_double_sided;
+    uint32_t alpha_cutoff;
+    uint32_t pad;
+    DevTexture tex;
+};
+
+// A triangle ready to rasterize: edge equations at pixel (0,0), depth plane and tie-break rank.
+struct TriRec {
+    int32_t E0, E1, E2;
+    int32_t A12, B12, A20, B20, A01, B01;
+    float Z0, Z10, Z20;
+    uint32_t bbMin, bbMax;  // packed (x | y << 16), 4-aligned, [min, max)
+    uint32_t lowword;       // 0xFFFFFFFE - rank
+    uint32_t pad;
+};
+static_assert(sizeof(TriRec) == 64, "TriRec");
+
+// Per-rasterizer device scratch, reused by every draw.
+struct DrawScratch {
+    unsigned long long* control;   // [0] meshlet work counter, [1] big-triangle queue (slots<<40 | chunks),
+                                   // [2] status flags, [3..6] perf counters
+    TriRec* big;                   // queue of triangles rasterized by the chunk kernel
+    unsigned long long* bigBase;   // first chunk index of each queued triangle
+    uint32_t bigCapacity;
+};
+
+enum : unsigned long long { kStatusBigOverflow = 1ull, kStatusClipOverflow = 2ull };
+
+struct DrawArgs {
+    const uint8_t* meshlets;
+    const DevMaterial* materials;
+    uint32_t numMaterials;
+    uint32_t meshletOffset;
+    uint32_t count;
+    const uint16_t* cullBitmap;
+    float m[16];
+    int halfW, halfH;
+    uint32_t width, height;
+    float bx, by;
+    int clipMode;     // 1: clip non-trivial triangles (Mode B), 0: drop them
+    int countClipped; // count non-trivial triangles in TrianglesClipped
+    unsigned long long* keys;
+    DrawScratch s;
+};
+
+void launch_draw(const DrawArgs& a, cudaStream_t st, int numSMs);
+void launch_init_keys(const uint32_t* depthLayer, unsigned long long* keys, uint32_t n, cudaStream_t st);
+void launch_clear(uint32_t* layer0, uint32_t* layer1, unsigned long long* keys, uint32_t n, uint32_t color,
+                  uint32_t depthBits, cudaStream_t st);
+void launch_fill(uint32_t* dst, uint32_t n, uint32_t value, cudaStream_t st);
+void launch_finalize(const unsigned long long* keys, uint32_t* layer0, uint32_t* layer1, uint32_t n, cudaStream_t st);
+void launch_detile(const uint32_t* src, uint32_t* dst, uint32_t width, uint32_t height, cudaStream_t st);
+
+}  // namespace swr
+
+// Error reporting and the calling thread's stream, shared by all translation units (swr_api.cu).
+swr_status swr_internal_fail(swr_status code, const char* msg);
+swr_status swr_internal_cuda_fail(cudaError_t e, const char* what);
+cudaStream_t swr_internal_stream();
+
+namespace swr {
+// Kernel tracing: every launch is counted; while profiling is enabled each launch is bracketed
+// by CUDA events on its stream (the GPU counterpart of the reference's Tracy zones).
+struct LaunchScope {
+    LaunchScope(const char* name, cudaStream_t st);
+    ~LaunchScope();
+    cudaStream_t st;
+    int rec;
+};
+}  // namespace swr
+
+struct swr_framebuffer_t {
+    uint32_t width, height, tile_stride, layer_stride, num_layers;
+    uint32_t* layers;              // num_layers * layer_stride words (+64 pad)
+    unsigned long long* keys;      // one vis-buffer key per pixel, tiled like the layers
+    bool keys_valid;
+};
+
+struct swr_scene_t {
+    uint8_t* meshlets;
+    uint32_t count, capacity;
+    swr::DevMaterial* materials;
+    uint32_t num_materials;
+};
+
+struct swr_texture_t {
+    uint32_t format;
+    swr::DevTexture d;             // d.data is the device storage
+    size_t words;
+};
+
+struct swr_rasterizer_t {
+    int enable_binning, enable_clipping, enable_guardband;
+    swr::DrawScratch scratch;
+};

@@ -1,0 +1,478 @@
+// Meshlet rasterizer kernels: mesh shader (ShadeMeshlet), clip codes, triangle setup, clipping and
+// vis-buffer rasterization (FS_EncodeSurfaceId<false>) for sm_103a.
+//
+// Work decomposition:
+//   k_draw_meshlets  one warp per meshlet (dynamic fetch). Lanes transform the 64 vertices into
+//                    shared memory, then own one triangle each: clip codes, setup and edge
+//                    equations in registers. Triangles whose 4-aligned box covers at most
+//                    kSmallTiles 4x4 tiles are rasterized by the whole warp, two tiles (32 pixels)
+//                    per step; larger and clipped triangles go to a device queue.
+//   k_raster_big     warps take 32x32-pixel chunks of queued triangles (flattened by a prefix of
+//                    chunk counts kept in the queue), reject empty chunks by their corners and
+//                    rasterize the rest two tiles per step.
+//   k_finalize       converts per-pixel keys to the reference's depth and surfaceId layers.
+// The depth test is a 64-bit atomicMax on (ordered depth, 0xFFFFFFFE - rank); the result is
+// independent of execution order and equals the single-threaded reference.
+#include "swr_device.cuh"
+#include "swr_internal.h"
+
+namespace swr {
+
+constexpr int kWarpsPerBlock = 8;
+constexpr int kSmallTiles = 16;
+constexpr int kChunkTiles = 8;  // chunk = 8x8 tiles = 32x32 pixels
+
+struct Vtx { float x, y, z, w; };
+
+// ------------------------------------------------------------------ setup (per lane)
+struct Setup {
+    uint32_t Pos0, Pos1, Pos2;
+    float Z0, Z1, Z2;
+};
+
+// TrianglePacket::GetBoundingBox / GetRenderBoundingBox (Rasterizer.cpp:331-351).
+__device__ __forceinline__ void render_bbox(const Setup& t, int halfW, int halfH, uint32_t& bbMin, uint32_t& bbMax) {
+    uint32_t minPos = __vmins2(__vmins2(t.Pos0, t.Pos1), t.Pos2);
+    uint32_t maxPos = __vmaxs2(__vmaxs2(t.Pos0, t.Pos1), t.Pos2);
+    minPos = srai16_4(minPos + 0x00070007u);  // 32-bit add, as the reference
+    maxPos = srai16_4(maxPos + 0x00070007u);
+    uint32_t vp = (uint32_t)halfW | ((uint32_t)halfH << 16);
+    uint32_t x = __vmins2(__vmaxs2(__vadd2(minPos, vp), 0u), vp * 2);
+    uint32_t y = __vmins2(__vmaxs2(__vadd2(maxPos, vp), 0u), vp * 2);
+    bbMin = x & ~0x00030003u;
+    bbMax = (y + 0x00030003u) & ~0x00030003u;
+}
+
+// TrianglePacket::Setup (Rasterizer.cpp:257-289); returns the lane's keep bit.
+__device__ __forceinline__ bool tri_setup(Vtx v0, Vtx v1, Vtx v2, int halfW, int halfH, int cullMode, Setup& t,
+                                          uint32_t& bbMin, uint32_t& bbMax) {
+    float rw0 = fdiv(1.0f, v0.w), rw1 = fdiv(1.0f, v1.w), rw2 = fdiv(1.0f, v2.w);
+    float x0 = fmul(v0.x, rw0), y0 = fmul(v0.y, rw0);
+    float x1 = fmul(v1.x, rw1), y1 = fmul(v1.y, rw1);
+    float x2 = fmul(v2.x, rw2), y2 = fmul(v2.y, rw2);
+    float det = fsub(fmul(fsub(x2, x0), fsub(y1, y0)), fmul(fsub(x0, x1), fsub(y0, y2)));
+    if (cullMode != kCullFrontCCW) {
+        bool flip = (cullMode == kCullFrontCW) ? true : (det < 0);
+        det = flip ? -det : det;
+    }
+    bool keep = det > 0;
+    float fsx = (float)(halfW * 16), fsy = (float)(halfH * 16);
+    int32_t ix0 = round2i(fmul(x0, fsx)), iy0 = round2i(fmul(y0, fsy));
+    int32_t ix1 = round2i(fmul(x1, fsx)), iy1 = round2i(fmul(y1, fsy));
+    int32_t ix2 = round2i(fmul(x2, fsx)), iy2 = round2i(fmul(y2, fsy));
+    t.Pos0 = ((uint32_t)ix0 & 0xFFFF) | ((uint32_t)iy0 << 16);
+    t.Pos1 = ((uint32_t)ix1 & 0xFFFF) | ((uint32_t)iy1 << 16);
+    t.Pos2 = ((uint32_t)ix2 & 0xFFFF) | ((uint32_t)iy2 << 16);
+    render_bbox(t, halfW, halfH, bbMin, bbMax);
+    if (lo16(bbMin) >= lo16(bbMax) || hi16(bbMin) >= hi16(bbMax)) keep = false;
+    t.Z0 = fmul(v0.z, rw0), t.Z1 = fmul(v1.z, rw1), t.Z2 = fmul(v2.z, rw2);
+    return keep;
+}
+
+// ComputeEdge (Rasterizer.cpp:291-295), wrapping int32.
+__device__ __forceinline__ int32_t compute_edge(int32_t a, int32_t x, int32_t b, int32_t y) {
+    int32_t w = (int32_t)((uint32_t)a * (uint32_t)x + (uint32_t)b * (uint32_t)y);
+    w = (int32_t)((uint32_t)w + ((a > 0 || (a == 0 && b > 0)) ? 0u : 0xFFFFFFFFu));
+    return w >> 4;
+}
+
+// TriangleEdgeVars::Setup (Rasterizer.cpp:296-329), depth terms only (the opaque vis-buffer
+// shader does not read the perspective-correct barycentrics).
+__device__ __forceinline__ void edge_setup(const Setup& t, int halfW, int halfH, uint32_t bbMin, uint32_t bbMax,
+                                           uint32_t rank, TriRec& r) {
+    int32_t x0 = lo16(t.Pos0), y0 = hi16(t.Pos0);
+    int32_t x1 = lo16(t.Pos1), y1 = hi16(t.Pos1);
+    int32_t x2 = lo16(t.Pos2), y2 = hi16(t.Pos2);
+    int32_t A01 = y1 - y0, B01 = x0 - x1;
+    int32_t A12 = y2 - y1, B12 = x1 - x2;
+    int32_t A20 = y0 - y2, B20 = x2 - x0;
+    int32_t det = (int32_t)((uint32_t)B20 * (uint32_t)A01 - (uint32_t)B01 * (uint32_t)A20);
+    if (det < 0) {
+        A01 = -A01, B01 = -B01, A12 = -A12, B12 = -B12, A20 = -A20, B20 = -B20;
+        det = -det;
+    }
+    int32_t sx = (int32_t)((uint32_t)(-halfW) << 4) + 8, sy = (int32_t)((uint32_t)(-halfH) << 4) + 8;
+    r.E0 = compute_edge(A12, sx - x1, B12, sy - y1);
+    r.E1 = compute_edge(A20, sx - x2, B20, sy - y2);
+    r.E2 = compute_edge(A01, sx - x0, B01, sy - y0);
+    r.A12 = A12, r.B12 = B12, r.A20 = A20, r.B20 = B20, r.A01 = A01, r.B01 = B01;
+    float rcpArea = fdiv(16.0f, __int2float_rn(det));
+    r.Z0 = t.Z0;
+    r.Z10 = fmul(fsub(t.Z1, t.Z0), rcpArea);
+    r.Z20 = fmul(fsub(t.Z2, t.Z0), rcpArea);
+    r.bbMin = bbMin, r.bbMax = bbMax;
+    r.lowword = 0xFFFFFFFEu - rank;
+    r.pad = 0;
+}
+
+// ------------------------------------------------------------------ fragments
+// DrawTriangle inner loop (Rasterizer.h:287-323) + FS_EncodeSurfaceId<false> (Shading.cpp:309-331)
+// for one pixel inside the triangle's render box.
+__device__ __forceinline__ void shade_fragment(const TriRec& r, uint32_t px, uint32_t py, unsigned long long* keys,
+                                               uint32_t width) {
+    int32_t e0 = (int32_t)((uint32_t)r.E0 + (uint32_t)r.A12 * px + (uint32_t)r.B12 * py);
+    int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
+    int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
+    if ((e0 | e1 | e2) < 0) return;
+    float depth = ffma(__int2float_rn(e1), r.Z10, ffma(__int2float_rn(e2), r.Z20, r.Z0));
+    if (depth != depth) return;  // NaN never passes `Depth > old`
+    unsigned long long key = ((unsigned long long)float_order(depth) << 32) | r.lowword;
+    unsigned long long* p = keys + pixel_offset(px, py, width);
+    if (key > *(volatile unsigned long long*)p) atomicMax(p, key);
+}
+
+// Rasterizes tiles [t0, t0 + n) of a box tilesX wide, two tiles per warp step.
+__device__ __forceinline__ void raster_tiles(const TriRec& r, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
+                                             unsigned long long* keys, uint32_t width, int lane) {
+    if (tilesX <= 0 || tilesY <= 0) return;
+    int T = tilesX * tilesY;
+    int tx = lane >> 4, ty = 0;
+    while (tx >= tilesX) tx -= tilesX, ty++;
+    uint32_t fx = lane & 3, fy = (lane >> 2) & 3;
+    for (int t0 = 0; t0 < T; t0 += 2) {
+        if (t0 + (lane >> 4) < T) shade_fragment(r, x0 + tx * 4 + fx, y0 + ty * 4 + fy, keys, width);
+        tx += 2;
+        while (tx >= tilesX) tx -= tilesX, ty++;
+    }
+}
+
+// One lane rasterizes a whole triangle (queue overflow fallback; slow but exact).
+__device__ __noinline__ void raster_serial(const TriRec& r, unsigned long long* keys, uint32_t width) {
+    uint32_t minX = r.bbMin & 0xFFFF, minY = r.bbMin >> 16, maxX = r.bbMax & 0xFFFF, maxY = r.bbMax >> 16;
+    for (uint32_t y = minY; y < maxY; y++)
+        for (uint32_t x = minX; x < maxX; x++) shade_fragment(r, x, y, keys, width);
+}
+
+__device__ __forceinline__ void enqueue_big(const TriRec& r, const DrawArgs& a) {
+    int tilesX = ((r.bbMax & 0xFFFF) - (r.bbMin & 0xFFFF)) >> 2;
+    int tilesY = ((r.bbMax >> 16) - (r.bbMin >> 16)) >> 2;
+    unsigned long long chunks = (unsigned long long)((tilesX + kChunkTiles - 1) / kChunkTiles) *
+                                (unsigned long long)((tilesY + kChunkTiles - 1) / kChunkTiles);
+    unsigned long long old = atomicAdd(&a.s.control[1], (1ull << 40) | chunks);
+    unsigned long long slot = old >> 40;
+    if (slot < a.s.bigCapacity) {
+        a.s.big[slot] = r;
+        a.s.bigBase[slot] = old & ((1ull << 40) - 1);
+    } else {
+        atomicOr(&a.s.control[2], kStatusBigOverflow);
+        raster_serial(r, a.keys, a.width);
+    }
+}
+
+// Clipper::ClipTriangles + FlushPacket (Rasterizer.cpp:398-491) for this lane's triangle; the
+// lanes of a packet are independent (each prim restarts its new-vertex slots). Fan outputs are
+// set up with TrianglePacket::Setup and queued with rank (packet, clipped, lane, fan index).
+__device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t outcodes, const DrawArgs& a,
+                                            int cullMode, uint32_t gMeshlet, uint32_t prim, unsigned long long& nRaster) {
+    float V[4][16];  // x, y, z, w of the polygon's vertices (barycentric rows are not needed here)
+    V[0][0] = v0.x, V[1][0] = v0.y, V[2][0] = v0.z, V[3][0] = v0.w;
+    V[0][1] = v1.x, V[1][1] = v1.y, V[2][1] = v1.z, V[3][1] = v1.w;
+    V[0][2] = v2.x, V[1][2] = v2.y, V[2][2] = v2.z, V[3][2] = v2.w;
+    uint8_t idx[16] = { 0, 1, 2 };
+    uint32_t vertCount = 3, nextIdx = 3;
+    const float guard[2] = { a.bx, a.by };
+
+    for (uint32_t planeId = 0; planeId < 6; planeId++) {
+        if (!((outcodes >> planeId) & 1)) continue;
+        uint8_t out[16];
+        uint32_t outCount = 0;
+        float planeScale = planeId < 4 ? guard[planeId / 2] : 1.0f;
+        for (uint32_t vi = 0; vi < vertCount; vi++) {
+            uint32_t ia = idx[vi], ib = idx[(vi + 1) % vertCount];
+            float aa = V[planeId / 2][ia], ab = V[planeId / 2][ib];
+            if (planeId & 1) aa = -aa, ab = -ab;
+            float da = fadd(aa, fmul(V[3][ia], planeScale));
+            float db = fadd(ab, fmul(V[3][ib], planeScale));
+            // A convex polygon gains at most one vertex per plane (at most 9 vertices, 12 new
+            // ones); a numerically non-convex one could exceed the buffers, which the reference
+            // only asserts (Rasterizer.cpp:441). Such a triangle is dropped and flagged.
+            if (outCount + 2 > 16 || nextIdx >= 16) {
+                atomicOr(&a.s.control[2], kStatusClipOverflow);
+                return;
+            }
+            if (da >= 0) out[outCount++] = (uint8_t)ia;
+            if ((da >= 0) != (db >= 0)) {
+                float t = fdiv(da, fsub(da, db));
+                for (int k = 0; k < 4; k++) V[k][nextIdx] = ffma(V[k][ib], t, ffma(-t, V[k][ia], V[k][ia]));
+                out[outCount++] = (uint8_t)nextIdx++;
+            }
+        }
+        if (vertCount < 3) break;  // stale count check, Rasterizer.cpp:443
+        vertCount = outCount;
+        for (int k = 0; k < 16; k++) idx[k] = out[k];
+    }
+    if (vertCount < 2) return;
+    for (uint32_t vi = 0; vi + 2 < vertCount; vi++) {
+        uint32_t i0 = idx[0], i1 = idx[vi + 1], i2 = idx[vi + 2];
+        Vtx a0 = { V[0][i0], V[1][i0], V[2][i0], V[3][i0] };
+        Vtx a1 = { V[0][i1], V[1][i1], V[2][i1], V[3][i1] };
+        Vtx a2 = { V[0][i2], V[1][i2], V[2][i2], V[3][i2] };
+        Setup t;
+        uint32_t bbMin, bbMax;
+        if (!tri_setup(a0, a1, a2, a.halfW, a.halfH, cullMode, t, bbMin, bbMax)) continue;
+        TriRec r;
+        edge_setup(t, a.halfW, a.halfH, bbMin, bbMax, make_rank(gMeshlet, prim, 1, vi), r);
+        enqueue_big(r, a);
+        nRaster++;
+    }
+}
+
+// ------------------------------------------------------------------ kernels
+__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs a) {
+    __shared__ float4 sPos[kWarpsPerBlock][64];
+    __shared__ uint32_t sIdx[kWarpsPerBlock][96];
+    __shared__ TriRec sTri[kWarpsPerBlock][32];
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float4* pos = sPos[warp];
+    const uint8_t* idxBytes = (const uint8_t*)sIdx[warp];
+    TriRec* tris = sTri[warp];
+    unsigned long long nProcessed = 0, nRaster = 0, nClipped = 0;
+
+    while (true) {
+        uint32_t m = 0;
+        if (lane == 0) m = (uint32_t)atomicAdd(&a.s.control[0], 1ull);
+        m = __shfl_sync(0xFFFFFFFFu, m, 0);
+        if (m >= a.count) break;
+        if (a.cullBitmap != nullptr && !((a.cullBitmap[m >> 4] >> (m & 15)) & 1)) continue;  // Shading.cpp:282-289
+
+        const uint32_t g = a.meshletOffset + m;
+        const uint8_t* mp = a.meshlets + (size_t)g * kMeshletSize;
+        const uint32_t hdr = *(const uint32_t*)(mp + kOffNumVertices);
+        const uint32_t matId = *(const uint32_t*)(mp + kOffMaterialId);
+        const uint32_t nv = hdr & 0xFF, nt = min((hdr >> 8) & 0xFF, 128u);  // record arrays hold 64 / 128
+        int cullMode = kCullFrontCCW;
+        if (matId != 0xFFFFFFFFu && matId < a.numMaterials)
+            cullMode = a.materials[matId].is_double_sided ? kCullNone : kCullFrontCCW;  // Shading.cpp:302-306
+        if (nt == 0) continue;
+        nProcessed += nt;
+
+        // ShadeMeshlet vertex loop (Shading.cpp:295-298): 16-vertex chunks up to NumVertices.
+        const uint32_t nvr = min((nv + 15) & ~15u, 64u);
+        const float* P = (const float*)(mp + kOffPositions);
+        for (uint32_t v = lane; v < 64; v += 32) {
+            float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (v < nvr) {
+                float x = P[v], y = P[64 + v], z = P[128 + v];
+                c.x = ffma(x, a.m[0], ffma(y, a.m[4], ffma(z, a.m[8], a.m[12])));
+                c.y = ffma(x, a.m[1], ffma(y, a.m[5], ffma(z, a.m[9], a.m[13])));
+                c.z = ffma(x, a.m[2], ffma(y, a.m[6], ffma(z, a.m[10], a.m[14])));
+                c.w = ffma(x, a.m[3], ffma(y, a.m[7], ffma(z, a.m[11], a.m[15])));
+            }
+            pos[v] = c;
+        }
+        const uint32_t* I = (const uint32_t*)(mp + kOffIndices);
+        for (uint32_t k = lane; k < 96; k += 32) sIdx[warp][k] = I[k];
+        __syncwarp();
+
+        for (uint32_t base = 0; base < nt; base += 32) {
+            const uint32_t p = base + lane;
+            const bool valid = p < nt;
+            const float4 q0 = pos[preload64_index(idxBytes[p & 127])];
+            const float4 q1 = pos[preload64_index(idxBytes[128 + (p & 127)])];
+            const float4 q2 = pos[preload64_index(idxBytes[256 + (p & 127)])];
+            Vtx v0 = { q0.x, q0.y, q0.z, q0.w }, v1 = { q1.x, q1.y, q1.z, q1.w }, v2 = { q2.x, q2.y, q2.z, q2.w };
+
+            // Clipper::ComputeClipCodes (Rasterizer.cpp:353-397), per lane.
+            uint32_t partial = 0, combined = 0x3F;
+            bool trivial = true;
+#pragma unroll
+            for (int i = 0; i < 3; i++) {
+                const Vtx& q = i == 0 ? v0 : (i == 1 ? v1 : v2);
+                uint32_t oc = 0;
+                oc |= (q.x < -q.w) ? 1u : 0u;
+                oc |= (q.x > q.w) ? 2u : 0u;
+                oc |= (q.y < -q.w) ? 4u : 0u;
+                oc |= (q.y > q.w) ? 8u : 0u;
+                oc |= (q.z < -q.w) ? 16u : 0u;
+                oc |= (q.z > q.w) ? 32u : 0u;
+                partial |= oc;
+                combined &= oc;
+                trivial = trivial && (fabsf(q.x) < fmul(q.w, a.bx) && fabsf(q.y) < fmul(q.w, a.by));
+            }
+            if (partial & 0x30u) trivial = false;
+            const bool accept = valid && combined == 0;
+            const bool acc = accept && trivial;
+            const bool nontriv = accept && !trivial;
+            if (a.countClipped) nClipped += __popc(__ballot_sync(0xFFFFFFFFu, nontriv)) * (lane == 0);
+
+            bool small = false;
+            if (acc) {
+                Setup t;
+                uint32_t bbMin, bbMax;
+                if (tri_setup(v0, v1, v2, a.halfW, a.halfH, cullMode, t, bbMin, bbMax)) {
+                    TriRec r;
+                    edge_setup(t, a.halfW, a.halfH, bbMin, bbMax, make_rank(g, p, 0, 0), r);
+                    nRaster++;
+                    int tilesX = ((bbMax & 0xFFFF) - (bbMin & 0xFFFF)) >> 2;
+                    int tilesY = ((bbMax >> 16) - (bbMin >> 16)) >> 2;
+                    if (tilesX * tilesY <= kSmallTiles) {
+                        tris[lane] = r;
+                        small = true;
+                    } else {
+                        enqueue_big(r, a);
+                    }
+                }
+            }
+            if (nontriv && a.clipMode) clip_and_queue(v0, v1, v2, partial, a, cullMode, g, p, nRaster);
+
+            unsigned smallMask = __ballot_sync(0xFFFFFFFFu, small);
+            __syncwarp();
+            while (smallMask) {
+                const int src = __ffs(smallMask) - 1;
+                smallMask &= smallMask - 1;
+                const TriRec r = tris[src];
+                const uint32_t x0 = r.bbMin & 0xFFFF, y0 = r.bbMin >> 16;
+                const int tilesX = (int)(((r.bbMax & 0xFFFF) - x0) >> 2), tilesY = (int)(((r.bbMax >> 16) - y0) >> 2);
+                raster_tiles(r, x0, y0, tilesX, tilesY, a.keys, a.width, lane);
+            }
+            __syncwarp();
+        }
+        __syncwarp();
+    }
+    // perf counters (Rasterizer.h:366-370)
+    nRaster = __reduce_add_sync(0xFFFFFFFFu, (unsigned)nRaster);
+    if (lane == 0) {
+        if (nProcessed) atomicAdd(&a.s.control[3], nProcessed);
+        if (nRaster) atomicAdd(&a.s.control[4], nRaster);
+        if (nClipped) atomicAdd(&a.s.control[5], nClipped);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_raster_big(const TriRec* __restrict__ big, const unsigned long long* __restrict__ bigBase,
+                                                    const unsigned long long* control, uint32_t capacity,
+                                                    unsigned long long* keys, uint32_t width) {
+    const unsigned long long q = control[1];
+    const uint32_t n = (uint32_t)min((unsigned long long)capacity, q >> 40);
+    if (n == 0) return;
+    const int lane = threadIdx.x & 31;
+    const TriRec& last = big[n - 1];
+    const int lastTX = (int)(((last.bbMax & 0xFFFF) - (last.bbMin & 0xFFFF)) >> 2);
+    const int lastTY = (int)(((last.bbMax >> 16) - (last.bbMin >> 16)) >> 2);
+    const unsigned long long total = bigBase[n - 1] + (unsigned long long)((lastTX + kChunkTiles - 1) / kChunkTiles) *
+                                                          ((lastTY + kChunkTiles - 1) / kChunkTiles);
+    const unsigned long long nWarps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    for (unsigned long long w = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < total; w += nWarps) {
+        // largest slot with bigBase[slot] <= w
+        uint32_t lo = 0, hi = n - 1;
+        while (lo < hi) {
+            uint32_t mid = (lo + hi + 1) >> 1;
+            if (bigBase[mid] <= w) lo = mid; else hi = mid - 1;
+        }
+        const TriRec r = big[lo];
+        const uint32_t c = (uint32_t)(w - bigBase[lo]);
+        const uint32_t minX = r.bbMin & 0xFFFF, minY = r.bbMin >> 16, maxX = r.bbMax & 0xFFFF, maxY = r.bbMax >> 16;
+        const uint32_t chunksX = (((maxX - minX) >> 2) + kChunkTiles - 1) / kChunkTiles;
+        const uint32_t cy = c / chunksX, cx = c - cy * chunksX;
+        const uint32_t x0 = minX + cx * (kChunkTiles * 4), y0 = minY + cy * (kChunkTiles * 4);
+        const uint32_t x1 = min(x0 + kChunkTiles * 4, maxX), y1 = min(y0 + kChunkTiles * 4, maxY);
+        // Conservative chunk rejection: an edge negative at all four corner samples is negative
+        // over the whole chunk (edge functions are affine in the pixel position).
+        bool empty = false;
+        {
+            const int32_t E[3] = { r.E0, r.E1, r.E2 };
+            const int32_t A[3] = { r.A12, r.A20, r.A01 }, B[3] = { r.B12, r.B20, r.B01 };
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                int32_t c00 = (int32_t)((uint32_t)E[k] + (uint32_t)A[k] * x0 + (uint32_t)B[k] * y0);
+                int32_t c10 = (int32_t)((uint32_t)E[k] + (uint32_t)A[k] * (x1 - 1) + (uint32_t)B[k] * y0);
+                int32_t c01 = (int32_t)((uint32_t)E[k] + (uint32_t)A[k] * x0 + (uint32_t)B[k] * (y1 - 1));
+                int32_t c11 = (int32_t)((uint32_t)E[k] + (uint32_t)A[k] * (x1 - 1) + (uint32_t)B[k] * (y1 - 1));
+                if ((c00 & c10 & c01 & c11) < 0) empty = true;
+            }
+        }
+        if (empty) continue;
+        raster_tiles(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), keys, width, lane);
+    }
+}
+
+__global__ void k_init_keys(const uint32_t* __restrict__ depth, unsigned long long* __restrict__ keys, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        keys[i] = ((unsigned long long)float_order(__uint_as_float(depth[i])) << 32) | kKeyEmptyLow;
+}
+
+__global__ void k_clear(uint32_t* __restrict__ l0, uint32_t* __restrict__ l1, unsigned long long* __restrict__ keys,
+                        uint32_t n, uint32_t color, uint32_t depthBits) {
+    const unsigned long long key = ((unsigned long long)float_order(__uint_as_float(depthBits)) << 32) | kKeyEmptyLow;
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) * 4; i < n; i += gridDim.x * blockDim.x * 4) {
+        // n is a multiple of 16 (4x4 tiles), so the 16-byte vectors never straddle the end
+        *(uint4*)&l0[i] = make_uint4(color, color, color, color);
+        if (l1) *(uint4*)&l1[i] = make_uint4(depthBits, depthBits, depthBits, depthBits);
+        if (keys) {
+            *(ulonglong2*)&keys[i] = make_ulonglong2(key, key);
+            *(ulonglong2*)&keys[i + 2] = make_ulonglong2(key, key);
+        }
+    }
+}
+
+__global__ void k_fill(uint32_t* __restrict__ dst, uint32_t n, uint32_t v) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) dst[i] = v;
+}
+
+__global__ void k_finalize(const unsigned long long* __restrict__ keys, uint32_t* __restrict__ l0,
+                           uint32_t* __restrict__ l1, uint32_t n) {
+    for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) * 2; i < n; i += gridDim.x * blockDim.x * 2) {
+        const ulonglong2 k = *(const ulonglong2*)&keys[i];
+        const unsigned long long kk[2] = { k.x, k.y };
+#pragma unroll
+        for (int j = 0; j < 2; j++) {
+            const uint32_t low = (uint32_t)kk[j];
+            if (low == kKeyEmptyLow) continue;
+            l1[i + j] = __float_as_uint(float_unorder((uint32_t)(kk[j] >> 32)));
+            l0[i + j] = rank_surface_id(0xFFFFFFFEu - low);
+        }
+    }
+}
+
+// Framebuffer::GetPixels de-tiling (ImageHelpers.cpp:109-147) into a row-major device buffer.
+__global__ void k_detile(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, uint32_t width, uint32_t height) {
+    const uint32_t n = width * height;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t y = i / width, x = i - y * width;
+        dst[i] = src[pixel_offset(x, y, width)];
+    }
+}
+
+static int grid_for(uint32_t n, int perThread, int block) {
+    long long g = ((long long)n / perThread + block - 1) / block;
+    return (int)max(1ll, min(g, 152ll * 16));
+}
+
+void launch_draw(const DrawArgs& a, cudaStream_t st, int numSMs) {
+    {
+        LaunchScope ls("k_draw_meshlets", st);
+        k_draw_meshlets<<<numSMs * 4, kWarpsPerBlock * 32, 0, st>>>(a);
+    }
+    {
+        LaunchScope ls("k_raster_big", st);
+        k_raster_big<<<numSMs * 8, 256, 0, st>>>(a.s.big, a.s.bigBase, a.s.control, a.s.bigCapacity, a.keys, a.width);
+    }
+}
+
+void launch_init_keys(const uint32_t* depthLayer, unsigned long long* keys, uint32_t n, cudaStream_t st) {
+    LaunchScope ls("k_init_keys", st);
+    k_init_keys<<<grid_for(n, 1, 256), 256, 0, st>>>(depthLayer, keys, n);
+}
+
+void launch_clear(uint32_t* l0, uint32_t* l1, unsigned long long* keys, uint32_t n, uint32_t color, uint32_t depthBits,
+                  cudaStream_t st) {
+    LaunchScope ls("k_clear", st);
+    k_clear<<<grid_for(n, 4, 256), 256, 0, st>>>(l0, l1, keys, n, color, depthBits);
+}
+
+void launch_fill(uint32_t* dst, uint32_t n, uint32_t value, cudaStream_t st) {
+    LaunchScope ls("k_fill", st);
+    k_fill<<<grid_for(n, 1, 256), 256, 0, st>>>(dst, n, value);
+}
+
+void launch_finalize(const unsigned long long* keys, uint32_t* l0, uint32_t* l1, uint32_t n, cudaStream_t st) {
+    LaunchScope ls("k_finalize", st);
+    k_finalize<<<grid_for(n, 2, 256), 256, 0, st>>>(keys, l0, l1, n);
+}
+
+void launch_detile(const uint32_t* src, uint32_t* dst, uint32_t width, uint32_t height, cudaStream_t st) {
+    LaunchScope ls("k_detile", st);
+    k_detile<<<grid_for(width * height, 1, 256), 256, 0, st>>>(src, dst, width, height);
+}
+
+}  // namespace swr

@@ -1,0 +1,313 @@
+"""Seeded synthetic scenes for the meshlet raster pipeline.
+
+The reference loads glTF assets and splits them with meshoptimizer (src/SwRast/Scene.cpp:156-368);
+neither the assets of the benchmark scenes nor those libraries exist here, so scenes are generated
+directly in the reference's ``Meshlet`` record layout (src/SwRast/Scene.h:15-30, 1728 bytes).
+
+Every meshlet is a closed, genus-0 "icosphere-like" patch: 64 points of a spherical Fibonacci
+lattice triangulated by their convex hull (2*64-4 = 124 triangles), outward-facing triangles wound
+counter-clockwise (the reference's FaceCullMode::FrontCCW keeps them), radially displaced by
+Gaussian noise (sigma 0.02) per meshlet. Cameras follow the reference's reversed-Z infinite
+projection (src/SwRast/Camera.h:38-48).
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+MESHLET_SIZE = 1728
+
+MESHLET_DTYPE = np.dtype({
+    "names": ["BoundCenter", "BoundRadius", "ConeApex", "ConeAxis", "ConeCutoff", "NumVertices",
+              "NumTriangles", "AlphaCutoff", "MaterialId", "TangentHandedness", "Positions",
+              "TexCoords", "NormalTangents", "Indices"],
+    "formats": [("<f4", 3), "<f4", ("<f4", 3), ("<f4", 3), "<f4", "u1", "u1", "u1", "<u4", "<u8",
+                ("<f4", (3, 64)), ("<u4", 64), ("<u4", 64), ("u1", (3, 128))],
+    "offsets": [0, 12, 16, 28, 40, 44, 45, 46, 48, 56, 64, 832, 1088, 1344],
+    "itemsize": MESHLET_SIZE,
+})
+
+MATERIAL_DTYPE = np.dtype([("texture", "<u4"), ("is_double_sided", "u1"), ("alpha_cutoff", "u1"),
+                           ("pad", "u1", 2)])
+
+
+def concat_meshlets(parts) -> np.ndarray:
+    """Concatenates meshlet arrays keeping the 1728-byte record (np.concatenate would canonicalise
+    the structured dtype and drop the trailing padding)."""
+    n = sum(len(p) for p in parts)
+    out = np.zeros(n, dtype=MESHLET_DTYPE)
+    i = 0
+    for p in parts:
+        out[i:i + len(p)] = p
+        i += len(p)
+    return out
+
+
+# --------------------------------------------------------------------------- meshlet template
+def _fibonacci_sphere(n: int) -> np.ndarray:
+    i = np.arange(n, dtype=np.float64) + 0.5
+    phi = np.arccos(1.0 - 2.0 * i / n)
+    theta = math.pi * (1.0 + 5.0 ** 0.5) * i
+    return np.stack([np.cos(theta) * np.sin(phi), np.cos(phi), np.sin(theta) * np.sin(phi)], axis=1)
+
+
+def _hull_triangles(p: np.ndarray) -> np.ndarray:
+    """Convex hull of points on a sphere, wound so (b-a)x(c-a) points outward."""
+    from scipy.spatial import ConvexHull
+
+    tris = ConvexHull(p).simplices.astype(np.int64)
+    a, b, c = p[tris[:, 0]], p[tris[:, 1]], p[tris[:, 2]]
+    n = np.cross(b - a, c - a)
+    flip = np.einsum("ij,ij->i", n, (a + b + c) / 3.0) < 0
+    tris[flip] = tris[flip][:, [0, 2, 1]]
+    # deterministic, spatially coherent order: by latitude band then longitude of the centroid
+    cen = (p[tris[:, 0]] + p[tris[:, 1]] + p[tris[:, 2]]) / 3.0
+    band = np.floor((cen[:, 1] + 1.0) * 4.0)
+    lon = np.arctan2(cen[:, 2], cen[:, 0])
+    order = np.lexsort((lon, band))
+    return tris[order]
+
+
+_TEMPLATE: tuple[np.ndarray, np.ndarray] | None = None
+
+
+def meshlet_template() -> tuple[np.ndarray, np.ndarray]:
+    """(64x3 unit positions, 124x3 triangle indices)."""
+    global _TEMPLATE
+    if _TEMPLATE is None:
+        p = _fibonacci_sphere(64)
+        _TEMPLATE = (p, _hull_triangles(p))
+    return _TEMPLATE
+
+
+def _oct_encode(n: np.ndarray) -> np.ndarray:
+    """Octahedral map of unit vectors to [0,1]^2 (the reference's MapOctahedron, Texture.h:282-288)."""
+    w = 1.0 / (np.abs(n[..., 0]) + np.abs(n[..., 1]) + np.abs(n[..., 2]))
+    t = np.maximum(-n[..., 2] * w, 0.0)
+    u = n[..., 0] * w + np.copysign(t, n[..., 0])
+    v = n[..., 1] * w + np.copysign(t, n[..., 1])
+    return np.stack([u, v], axis=-1) * 0.5 + 0.5
+
+
+def _pack_unorm8(v: np.ndarray) -> np.ndarray:
+    return np.round(np.clip(v, 0.0, 1.0) * 255.0).astype(np.uint32)
+
+
+def build_meshlets(centers: np.ndarray, scales: np.ndarray, yaws: np.ndarray, material_ids: np.ndarray,
+                   rng: np.random.Generator, sigma: float = 0.02, uv_repeat: float = 2.0) -> np.ndarray:
+    """Instantiates the template once per meshlet: displaced, scaled, yawed and translated."""
+    n = len(centers)
+    base, tris = meshlet_template()
+    nv, nt = base.shape[0], tris.shape[0]
+    out = np.zeros(n, dtype=MESHLET_DTYPE)
+
+    disp = 1.0 + sigma * rng.standard_normal((n, nv))
+    local = base[None, :, :] * disp[:, :, None]                       # (n, 64, 3) object space
+    c, s = np.cos(yaws), np.sin(yaws)
+    rx = c[:, None] * local[:, :, 0] + s[:, None] * local[:, :, 2]
+    rz = -s[:, None] * local[:, :, 0] + c[:, None] * local[:, :, 2]
+    world = np.stack([rx, local[:, :, 1], rz], axis=2) * scales[:, None, None] + centers[:, None, :]
+    world32 = world.astype(np.float32)
+
+    out["Positions"] = np.transpose(world32, (0, 2, 1))
+    out["NumVertices"] = nv
+    out["NumTriangles"] = nt
+    out["AlphaCutoff"] = 255
+    out["MaterialId"] = material_ids.astype(np.uint32)
+    out["BoundCenter"] = centers.astype(np.float32)
+    d = np.linalg.norm(world32.astype(np.float64) - centers[:, None, :], axis=2).max(axis=1)
+    out["BoundRadius"] = (d * (1.0 + 1e-6)).astype(np.float32)
+    out["ConeApex"] = centers.astype(np.float32)
+    out["ConeAxis"] = np.array([0.0, 1.0, 0.0], dtype=np.float32)
+    out["ConeCutoff"] = 1.0
+    idx = np.zeros((3, 128), dtype=np.uint8)
+    idx[:, :nt] = tris.T
+    out["Indices"] = idx[None]
+
+    # texture coordinates: planar projection of the unit template, as float16 pairs
+    uv = (base[:, [0, 1]] * 0.5 + 0.5) * uv_repeat
+    uv16 = uv.astype(np.float16).view(np.uint16).astype(np.uint32)
+    tc = uv16[:, 0] | (uv16[:, 1] << 16)
+    out["TexCoords"][:, :nv] = tc[None]
+
+    # oct-encoded normal / tangent pairs (packUnorm4x8 order: nx, ny, tx, ty)
+    normal = local / np.linalg.norm(local, axis=2, keepdims=True)
+    nrm = np.stack([c[:, None] * normal[:, :, 0] + s[:, None] * normal[:, :, 2], normal[:, :, 1],
+                    -s[:, None] * normal[:, :, 0] + c[:, None] * normal[:, :, 2]], axis=2)
+    up = np.array([0.0, 1.0, 0.0])
+    tan = np.cross(up[None, None, :], nrm)
+    tl = np.linalg.norm(tan, axis=2, keepdims=True)
+    tan = np.where(tl > 1e-6, tan / np.maximum(tl, 1e-12), np.array([1.0, 0.0, 0.0]))
+    on, ot = _pack_unorm8(_oct_encode(nrm)), _pack_unorm8(_oct_encode(tan))
+    out["NormalTangents"][:, :nv] = on[..., 0] | (on[..., 1] << 8) | (ot[..., 0] << 16) | (ot[..., 1] << 24)
+    out["TangentHandedness"] = 0
+    return out
+
+
+# --------------------------------------------------------------------------------- cameras
+def look_at(eye, target, up=(0.0, 1.0, 0.0)) -> np.ndarray:
+    """Right-handed view matrix (camera looks down -z), column-major float32[16]."""
+    eye, target, up = (np.asarray(v, dtype=np.float64) for v in (eye, target, up))
+    f = target - eye
+    f /= np.linalg.norm(f)
+    r = np.cross(f, up)
+    r /= np.linalg.norm(r)
+    u = np.cross(r, f)
+    m = np.eye(4)
+    m[0, :3], m[1, :3], m[2, :3] = r, u, -f
+    m[0, 3], m[1, 3], m[2, 3] = -r @ eye, -u @ eye, f @ eye
+    return m.T.astype(np.float32).reshape(16)  # row-major math -> glm column-major storage
+
+
+def proj_reversed_z(fov_deg: float, aspect: float, near: float) -> np.ndarray:
+    """Camera::GetProjMatrix (Camera.h:38-48): infinite reversed-Z, y flipped, column-major."""
+    f = 1.0 / math.tan(math.radians(fov_deg) / 2.0)
+    m = np.zeros((4, 4), dtype=np.float32)  # [col][row]
+    m[0, 0] = f / aspect
+    m[1, 1] = -f
+    m[2, 3] = -1.0
+    m[3, 2] = near
+    return m.reshape(16)
+
+
+def mat_mul(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Column-major float32 product with the summation order of the host matrix helpers."""
+    A, B = a.reshape(4, 4), b.reshape(4, 4)
+    r = np.zeros((4, 4), dtype=np.float32)
+    for c in range(4):
+        for row in range(4):
+            s = np.float32(A[0, row] * B[c, 0])
+            s = np.float32(s + np.float32(A[1, row] * B[c, 1]))
+            s = np.float32(s + np.float32(A[2, row] * B[c, 2]))
+            s = np.float32(s + np.float32(A[3, row] * B[c, 3]))
+            r[c, row] = s
+    return r.reshape(16)
+
+
+IDENTITY = np.eye(4, dtype=np.float32).reshape(16)
+
+
+@dataclass
+class View:
+    width: int
+    height: int
+    view: np.ndarray
+    proj: np.ndarray
+    eye: np.ndarray
+    depth_only: bool = False
+
+    @property
+    def world_to_clip(self) -> np.ndarray:
+        return mat_mul(self.proj, self.view)
+
+
+def make_view(width, height, eye, target, fov=60.0, near=0.1, depth_only=False) -> View:
+    return View(width, height, look_at(eye, target), proj_reversed_z(fov, width / height, near),
+                np.asarray(eye, dtype=np.float32), depth_only)
+
+
+# ---------------------------------------------------------------------------------- textures
+def value_noise_rgba(size: int, seed: int, cells: int = 32, layer: int = 0) -> np.ndarray:
+    """Seeded RGBA8 value noise (bilinear over a cells x cells lattice, wrapping), uint32[size, size]."""
+    rng = np.random.default_rng(seed * 7919 + layer)
+    lat = rng.integers(0, 256, size=(cells, cells, 4), dtype=np.int64)
+    if layer == 1:
+        # layer 1 = tangent-space normal XY (centred near 128), metallic, roughness (Scene.h:8-10)
+        lat[..., 0] = 128 + (lat[..., 0] - 128) // 3
+        lat[..., 1] = 128 + (lat[..., 1] - 128) // 3
+    step = size // cells
+    t = (np.arange(size) % step) * 256 // step                       # 8-bit fraction
+    i0 = np.arange(size) // step
+    i1 = (i0 + 1) % cells
+    ty, tx = t[:, None, None], t[None, :, None]
+    a = lat[i0[:, None], i0[None, :]]
+    b = lat[i0[:, None], i1[None, :]]
+    c = lat[i1[:, None], i0[None, :]]
+    d = lat[i1[:, None], i1[None, :]]
+    top = a * (256 - tx) + b * tx
+    bot = c * (256 - tx) + d * tx
+    v = ((top * (256 - ty) + bot * ty) >> 16).astype(np.uint32)
+    if layer == 0:
+        v[..., 3] = 255
+    return v[..., 0] | (v[..., 1] << 8) | (v[..., 2] << 16) | (v[..., 3] << 24)
+
+
+def env_map_r11g11b10(size: int, seed: int) -> np.ndarray:
+    """Octahedral sky radiance: a smooth gradient plus noise quantised to 8 bits, then packed
+    R11G11B10 (HdrTexture2D, Texture.h:216) with the reference's clamp-only packing."""
+    u = (np.arange(size) + 0.5) / size
+    uu, vv = np.meshgrid(u, u)
+    noise = (value_noise_rgba(size, seed, cells=16) & 0xFF).astype(np.float64) / 255.0
+    base = np.stack([0.3 + 0.5 * vv, 0.5 + 0.3 * uu, 0.9 - 0.2 * vv], axis=-1) * (0.75 + 0.5 * noise[..., None])
+    q = np.round(np.clip(base, 0, 1) * 255.0) / 255.0 * 4.0            # 8-bit quantised, HDR scale 4
+    q = q.astype(np.float32)
+
+    def pack(x, mbits):
+        x = np.maximum(x, np.float32(1.0 / (1 << 15)))
+        x = np.minimum(x, np.float32(130048.0 if mbits == 6 else 129024.0))
+        b = x.view(np.uint32)
+        if mbits == 6:
+            return ((b >> 17) & 0x3FFF) - 0x1C00
+        return ((b >> 18) & 0x1FFF) - 0x0E00
+    return (pack(q[..., 0], 6) << 21) | (pack(q[..., 1], 6) << 10) | pack(q[..., 2], 5)
+
+
+# ------------------------------------------------------------------------------------ scenes
+@dataclass
+class Scene:
+    meshlets: np.ndarray                      # MESHLET_DTYPE[n]
+    materials: np.ndarray                     # MATERIAL_DTYPE[m]
+    texture_size: int
+    texture_layers: int
+    views: list = field(default_factory=list)
+    texture_seed: int = 0
+    env_size: int = 0
+    name: str = ""
+
+    @property
+    def num_meshlets(self) -> int:
+        return len(self.meshlets)
+
+    def texture_pixels(self, i: int, layer: int) -> np.ndarray:
+        return value_noise_rgba(self.texture_size, self.texture_seed + i, layer=layer)
+
+
+def grid_scene(n_side: int = 32, width: int = 1280, height: int = 720, seed: int = 1,
+               texture_size: int = 512) -> Scene:
+    """Small plain-path scene: n_side^2 meshlets on a grid over [-16,16]^2 with random yaw,
+    one value-noise material (full mips), one camera."""
+    rng = np.random.default_rng(seed)
+    g = (np.arange(n_side) + 0.5) / n_side * 32.0 - 16.0
+    gx, gz = np.meshgrid(g, g)
+    centers = np.stack([gx.ravel(), np.zeros(gx.size), gz.ravel()], axis=1)
+    n = len(centers)
+    scales = np.full(n, 1.0)
+    m = build_meshlets(centers, scales, rng.uniform(0, 2 * math.pi, n), np.zeros(n, np.int64), rng)
+    mats = np.zeros(1, dtype=MATERIAL_DTYPE)
+    mats["alpha_cutoff"] = 255
+    view = make_view(width, height, eye=(0.0, 14.0, 24.0), target=(0.0, 0.0, -2.0))
+    return Scene(m, mats, texture_size, 1, [view], texture_seed=seed, name=f"grid{n}@{width}x{height}")
+
+
+def volume_scene(n: int = 100_000, width: int = 1920, height: int = 1080, n_materials: int = 64,
+                 seed: int = 2, texture_size: int = 2048, extent: float = 100.0,
+                 env_size: int = 1024) -> Scene:
+    """Large plain-path scene: n meshlets scattered in a (2*extent)^3 volume with log-uniform
+    scale 0.1-10 and random yaw, n_materials materials of two RGBA8 layers, seen by a camera on
+    the volume's -z face looking in (plus a perturbed second camera for the Hi-Z frame)."""
+    rng = np.random.default_rng(seed)
+    centers = rng.uniform(-extent, extent, size=(n, 3))
+    scales = np.exp(rng.uniform(math.log(0.1), math.log(10.0), n))
+    yaws = rng.uniform(0, 2 * math.pi, n)
+    mat_ids = rng.integers(0, n_materials, n)
+    m = build_meshlets(centers, scales, yaws, mat_ids, rng)
+    mats = np.zeros(n_materials, dtype=MATERIAL_DTYPE)
+    mats["texture"] = np.arange(n_materials)
+    mats["alpha_cutoff"] = 255
+    eye = np.array([0.0, 0.0, -1.3 * extent])
+    v0 = make_view(width, height, eye=eye, target=(0.0, 0.0, 0.0))
+    v1 = make_view(width, height, eye=eye + np.array([0.4, 0.2, 0.6]), target=(1.0, 0.5, 0.0))
+    return Scene(m, mats, texture_size, 2, [v0, v1], texture_seed=seed * 1000, env_size=env_size,
+                 name=f"volume{n}@{width}x{height}")

@@ -1,0 +1,111 @@
+// Host-side 4x4 matrix helpers used wherever the pipeline derives matrices from the caller's
+// (the frustum planes of ShadingContext::CullMeshlets, Shading.cpp:779-794, and
+// GetInverseScreenProjMatrix, Camera.h:140-146). The reference uses glm for these; this
+// header restates the same definitions in plain float32 code with a fixed operation order,
+// so every consumer of a given camera derives bit-identical matrices. Column-major storage,
+// m[c * 4 + r] = column c, row r, as glm lays out mat4.
+#pragma once
+#include <math.h>
+#include <stdint.h>
+#include <string.h>
+
+namespace swr_hostmath {
+
+// a * b, each output summed over k in ascending order.
+inline void mat4_mul(const float* a, const float* b, float* out) {
+    float r[16];
+    for (int c = 0; c < 4; c++) {
+        for (int row = 0; row < 4; row++) {
+            float s = a[0 * 4 + row] * b[c * 4 + 0];
+            s = s + a[1 * 4 + row] * b[c * 4 + 1];
+            s = s + a[2 * 4 + row] * b[c * 4 + 2];
+            s = s + a[3 * 4 + row] * b[c * 4 + 3];
+            r[c * 4 + row] = s;
+        }
+    }
+    memcpy(out, r, sizeof(r));
+}
+
+// Inverse by Gauss-Jordan elimination with partial pivoting in double precision, rounded to
+// float at the end. Returns false for a singular matrix (out is then left unchanged).
+inline bool mat4_inverse(const float* m, float* out) {
+    double a[4][8];
+    for (int r = 0; r < 4; r++) {
+        for (int c = 0; c < 4; c++) a[r][c] = (double)m[c * 4 + r];
+        for (int c = 0; c < 4; c++) a[r][4 + c] = (r == c) ? 1.0 : 0.0;
+    }
+    for (int col = 0; col < 4; col++) {
+        int piv = col;
+        for (int r = col + 1; r < 4; r++)
+            if (fabs(a[r][col]) > fabs(a[piv][col])) piv = r;
+        if (a[piv][col] == 0.0) return false;
+        if (piv != col)
+            for (int c = 0; c < 8; c++) { double t = a[col][c]; a[col][c] = a[piv][c]; a[piv][c] = t; }
+        double inv = 1.0 / a[col][col];
+        for (int c = 0; c < 8; c++) a[col][c] *= inv;
+        for (int r = 0; r < 4; r++) {
+            if (r == col) continue;
+            double f = a[r][col];
+            if (f == 0.0) continue;
+            for (int c = 0; c < 8; c++) a[r][c] -= f * a[col][c];
+        }
+    }
+    for (int r = 0; r < 4; r++)
+        for (int c = 0; c < 4; c++) out[c * 4 + r] = (float)a[r][4 + c];
+    return true;
+}
+
+// m * translation(v): column 3 becomes m0*v.x + m1*v.y + m2*v.z + m3.
+inline void mat4_translate(float* m, float vx, float vy, float vz) {
+    for (int r = 0; r < 4; r++) {
+        float s = m[0 * 4 + r] * vx;
+        s = s + m[1 * 4 + r] * vy;
+        s = s + m[2 * 4 + r] * vz;
+        s = s + m[3 * 4 + r];
+        m[3 * 4 + r] = s;
+    }
+}
+// m * scale(v): columns 0..2 scaled.
+inline void mat4_scale(float* m, float sx, float sy, float sz) {
+    for (int r = 0; r < 4; r++) {
+        m[0 * 4 + r] = m[0 * 4 + r] * sx;
+        m[1 * 4 + r] = m[1 * 4 + r] * sy;
+        m[2 * 4 + r] = m[2 * 4 + r] * sz;
+    }
+}
+
+// GetInverseScreenProjMatrix (Camera.h:140-146) with the default half-pixel offset: maps
+// (pixel x, pixel y, ndc z, 1) to world space.
+inline bool inverse_screen_proj(const float* worldToClip, uint32_t width, uint32_t height, float* out) {
+    float inv[16];
+    if (!mat4_inverse(worldToClip, inv)) return false;
+    mat4_translate(inv, -1.0f, -1.0f, 0.0f);
+    mat4_scale(inv, 2.0f / (float)width, 2.0f / (float)height, 1.0f);
+    mat4_translate(inv, 0.5f, 0.5f, 0.0f);
+    memcpy(out, inv, sizeof(inv));
+    return true;
+}
+
+// Gribb & Hartmann frustum planes of CullMeshlets (Shading.cpp:779-791): for i = 0..2,
+// plane 2i = row3 + row_i, plane 2i+1 = row3 - row_i, each divided by |xyz|.
+inline void frustum_planes(const float* objectToClip, float planes[6][4]) {
+    for (int i = 0; i < 3; i++) {
+        float a[4], b[4];
+        for (int k = 0; k < 4; k++) {
+            float r3 = objectToClip[k * 4 + 3], ri = objectToClip[k * 4 + i];
+            a[k] = r3 + ri;
+            b[k] = r3 - ri;
+        }
+        float la = sqrtf(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        float lb = sqrtf(b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+        for (int k = 0; k < 4; k++) {
+            planes[i * 2 + 0][k] = a[k] / la;
+            planes[i * 2 + 1][k] = b[k] / lb;
+        }
+    }
+}
+
+// glm::length(vec3(m[0])): uniform-scale estimate of a model matrix (Shading.cpp:793).
+inline float column0_length(const float* m) { return sqrtf(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]); }
+
+}  // namespace swr_hostmath

@@ -1,0 +1,181 @@
+/*
+ * libswr_gb300 — C ABI of the GB300 (sm_103a) meshlet raster pipeline.
+ *
+ * Each entry point replaces one entry point of GLimpSW's C++ API (src/SwRast/..., cited per
+ * function). Handles own device memory; callers keep their host copies. No exception crosses
+ * this boundary: every function returns an swr_status and swr_last_error() describes the last
+ * failure on the calling thread.
+ *
+ * Execution model: work is enqueued on the calling thread's current stream (swr_set_stream;
+ * default: the per-thread default stream) and runs asynchronously, in stream order. Functions
+ * that return data to host memory (swr_framebuffer_get_pixels, swr_cull_meshlets' count,
+ * swr_rasterizer_get_counters, swr_texture_get_data) synchronise that stream first, which gives
+ * the reference's blocking semantics at the points where it matters.
+ */
+#ifndef SWR_GB300_H
+#define SWR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    SWR_OK = 0,
+    SWR_EINVAL = 1,      /* bad argument: size above 2896 or not a multiple of 4, bad handle, ... */
+    SWR_ECAPACITY = 2,   /* an internal bound was exceeded (message says which) */
+    SWR_ETIMEOUT = 3,    /* a bounded device-side wait gave up */
+    SWR_ECUDA = 4,       /* CUDA runtime error (message carries the CUDA error string) */
+    SWR_ENOMEM = 5       /* device allocation failed */
+} swr_status;
+
+typedef struct swr_rasterizer_t* swr_rasterizer;
+typedef struct swr_framebuffer_t* swr_framebuffer;
+typedef struct swr_scene_t* swr_scene;
+typedef struct swr_texture_t* swr_texture;
+
+/* Limits: Rasterizer::MaxRenderSize (Rasterizer.h:203); the vis-buffer tie-break rank packs
+ * the global meshlet index into 21 bits. */
+#define SWR_MAX_RENDER_SIZE 2896u
+#define SWR_MAX_MESHLETS (1u << 21)
+#define SWR_MESHLET_SIZE 1728u
+
+/* ShadingContext::VisBufferShader (Shading.cpp:649-654): mesh shader ShadeMeshlet with fragment
+ * entry points FS_EncodeSurfaceId<false> (0) and FS_EncodeSurfaceId<true> (1). */
+#define SWR_SHADER_VISBUFFER 0u
+
+/* Texel formats (pixfmt::*, Texture.h:23-200). */
+#define SWR_FORMAT_RGBA8U 0u
+#define SWR_FORMAT_R11G11B10F 1u
+#define SWR_FORMAT_R32F 2u
+
+/* Perf counters (PerfCounter, Rasterizer.h:366-370). */
+#define SWR_COUNTER_TRIANGLES_PROCESSED 0
+#define SWR_COUNTER_TRIANGLES_RASTERIZED 1
+#define SWR_COUNTER_TRIANGLES_CLIPPED 2
+#define SWR_COUNTER_BIN_QUEUE_FLUSHES 3
+#define SWR_NUM_COUNTERS 4
+
+/* Material (Scene.h:7-14); texture may be NULL. */
+typedef struct {
+    swr_texture texture;
+    uint8_t is_double_sided;
+    uint8_t alpha_cutoff;
+} swr_material;
+
+/* Light (Scene.h:52-75), with the precomputed InvRadiusSq/SpotScale/SpotOffset. */
+typedef struct {
+    uint32_t type; /* 0 directional, 1 point, 2 spot */
+    float position[3], direction[3], color[3];
+    float intensity, radius, spot_inner_angle, spot_outer_angle;
+    float inv_radius_sq, spot_scale, spot_offset;
+} swr_light;
+
+/* ShadingContext (Shading.h:12-39). Matrices are column-major (glm layout). */
+typedef struct {
+    swr_scene scene;                 /* Meshlets + Materials */
+    uint32_t meshlet_offset;         /* MeshletOffset */
+    const uint16_t* cull_bitmap;     /* device pointer, one bit per meshlet of the draw, or NULL */
+    float world_to_clip[16];
+    float object_to_clip[16];
+    float object_to_world[9];        /* glm::mat3 */
+    swr_texture skybox;              /* R11G11B10 octahedral map, or NULL */
+    float view_pos[3];
+    float exposure;
+    const swr_light* lights;         /* host array, copied at call time */
+    uint32_t num_lights;
+} swr_shading_context;
+
+/* ---- errors and streams ---- */
+const char* swr_last_error(void);
+swr_status swr_set_stream(void* cuda_stream);      /* cudaStream_t; NULL = per-thread default */
+void* swr_get_stream(void);
+swr_status swr_synchronize(void);
+
+/* ---- tracing: the reference's Tracy zones and SWR_PERF timers (Rasterizer.cpp:494-643,
+ * Rasterizer.h:397-399) become per-kernel CUDA events ---- */
+uint64_t swr_launch_count(void);                   /* kernels launched by this library so far */
+swr_status swr_profile_enable(int enable);         /* record events around each launch (this thread) */
+/* Synchronises, returns up to max_records (kernel name, milliseconds) pairs recorded since the
+ * last collect, and clears the record list; *count receives the number recorded. */
+swr_status swr_profile_collect(uint32_t max_records, const char** names, float* ms, uint32_t* count);
+
+/* ---- Rasterizer (Rasterizer.h:202-213) ---- */
+/* Rasterizer::Rasterizer(uint32_t numThreads): numThreads has no GPU meaning and is ignored. */
+swr_status swr_rasterizer_create(uint32_t num_threads, swr_rasterizer* out);
+swr_status swr_rasterizer_destroy(swr_rasterizer r);
+/* EnableBinning / EnableClipping / EnableGuardband (Rasterizer.h:205-208). Binning selects the
+ * reference's binned semantics (non-trivial triangles dropped, guard band always on); otherwise
+ * non-trivial triangles are clipped when clipping is enabled. */
+swr_status swr_rasterizer_set_flags(swr_rasterizer r, int enable_binning, int enable_clipping,
+                                    int enable_guardband);
+/* perf::GetCurrent / perf::Reset (Rasterizer.h:381-395): device-side counters. */
+swr_status swr_rasterizer_get_counters(swr_rasterizer r, uint64_t out[SWR_NUM_COUNTERS]);
+swr_status swr_rasterizer_reset_counters(swr_rasterizer r);
+
+/* Rasterizer::DrawMeshlets(Framebuffer&, count, ShaderBinding) (Rasterizer.h:213,
+ * Rasterizer.cpp:493-644) with ShaderBinding{VisBufferShader, &ctx}. Depth test GREATER with
+ * equal depths resolved to the first-submitted triangle of a single-threaded draw. */
+swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t count, uint32_t shader_table,
+                             const swr_shading_context* ctx);
+
+/* ---- Framebuffer (Rasterizer.h:10-78, ImageHelpers.cpp:109-147) ---- */
+/* CreateFramebuffer(width, height, numLayers): width/height multiples of 4, at most 2896. */
+swr_status swr_framebuffer_create(uint32_t width, uint32_t height, uint32_t num_layers, swr_framebuffer* out);
+swr_status swr_framebuffer_destroy(swr_framebuffer fb);
+swr_status swr_framebuffer_clear(swr_framebuffer fb, uint32_t color, float depth);       /* Clear */
+swr_status swr_framebuffer_clear_layer(swr_framebuffer fb, uint32_t layer, uint32_t value); /* ClearLayer */
+/* GetPixels(layer, dest, stride): de-tiles a layer into host memory (stride in pixels). */
+swr_status swr_framebuffer_get_pixels(swr_framebuffer fb, uint32_t layer, uint32_t* dest, uint32_t stride);
+/* Device copy of a de-tiled layer (row-major, width*height words); no host synchronisation. */
+swr_status swr_framebuffer_get_pixels_device(swr_framebuffer fb, uint32_t layer, uint32_t* dest_device);
+/* Raw tiled layer storage (GetLayerData, Rasterizer.h:24-33), device pointer. Writing through it
+ * must be followed by swr_framebuffer_invalidate. */
+swr_status swr_framebuffer_layer_data(swr_framebuffer fb, uint32_t layer, void** out_device_ptr);
+swr_status swr_framebuffer_invalidate(swr_framebuffer fb);
+swr_status swr_framebuffer_size(swr_framebuffer fb, uint32_t* width, uint32_t* height, uint32_t* layer_stride,
+                                uint32_t* num_layers);
+
+/* ---- Scene: Meshlet and Material pools (Scene.h:117-128) ---- */
+swr_status swr_scene_create(swr_scene* out);
+swr_status swr_scene_destroy(swr_scene s);
+/* Copies count 1728-byte Meshlet records (Scene.h:15-30) from host memory to the device pool,
+ * starting at record first (the pool grows as needed). */
+swr_status swr_scene_upload_meshlets(swr_scene s, const void* meshlets, uint32_t first, uint32_t count);
+swr_status swr_scene_set_materials(swr_scene s, const swr_material* materials, uint32_t count);
+swr_status swr_scene_meshlet_count(swr_scene s, uint32_t* out);
+
+/* ---- Textures (Texture.h:314-636) ---- */
+/* CreateTexture2D<format>(width, height, maxLevels, numLayers): power-of-two sizes. */
+swr_status swr_texture_create(uint32_t format, uint32_t width, uint32_t height, uint32_t max_levels,
+                              uint32_t num_layers, swr_texture* out);
+swr_status swr_texture_destroy(swr_texture t);
+/* SetPixels(pixels, stride, layer, 0): row-major host texels into mip 0 of a layer. */
+swr_status swr_texture_set_pixels(swr_texture t, const uint32_t* pixels, uint32_t stride, uint32_t layer);
+swr_status swr_texture_generate_mips(swr_texture t);                                     /* GenerateMips */
+/* Raw storage (Data[], MipOffsets[16], levels) for inspection; words = layer_stride*layers. */
+swr_status swr_texture_info(swr_texture t, uint32_t* mip_levels, uint32_t* layer_stride, uint32_t mip_offsets[16]);
+swr_status swr_texture_get_data(swr_texture t, uint32_t* dest, size_t words);
+swr_status swr_texture_set_data(swr_texture t, const uint32_t* src, size_t words);
+
+/* ---- Culling, Hi-Z, resolve ---- */
+/* ShadingContext::CullMeshlets (Shading.cpp:775-869). bitmap_device receives one uint16 per 16
+ * meshlets of [first, first+count) of the scene. depth_map (R32f Hi-Z from
+ * swr_downsample_depth) may be NULL. If visible_count is not NULL the stream is synchronised and
+ * the number of visible meshlets is returned. */
+swr_status swr_cull_meshlets(swr_scene s, uint32_t first, uint32_t count, uint16_t* bitmap_device,
+                             const float proj[16], const float view[16], const float model[16],
+                             const float prev_view[16], float frame_width, float frame_height,
+                             swr_texture depth_map, uint32_t* visible_count);
+/* texutil::DownsampleDepth(Framebuffer&, Texture2D<R32f>&) (Texture.h:243, ImageHelpers.cpp:150-247). */
+swr_status swr_downsample_depth(swr_framebuffer fb, swr_texture dest);
+/* ShadingContext::Resolve(Rasterizer&, Framebuffer&) (Shading.cpp:658-690): shades the vis-buffer
+ * into RGBA8 colour written over layer 0. The light-sprite overlay (691-731) is not drawn. */
+swr_status swr_resolve(swr_rasterizer r, swr_framebuffer fb, const swr_shading_context* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SWR_GB300_H */

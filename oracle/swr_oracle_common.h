@@ -1,0 +1,90 @@
+// Oracle internals shared by its translation units (test infrastructure only).
+#pragma once
+#include "swr_oracle.h"
+
+#include <cfloat>
+#include <cmath>
+#include <cstddef>
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+namespace orc {
+
+// Meshlet, Scene.h:15-30 (1728 bytes, positions 64-byte aligned).
+struct Meshlet {
+    float BoundCenter[3];
+    float BoundRadius;
+    float ConeApex[3], ConeAxis[3];
+    float ConeCutoff;
+    uint8_t NumVertices, NumTriangles;
+    uint8_t AlphaCutoff;
+    uint32_t MaterialId;
+    uint64_t TangentHandedness;
+    alignas(64) float Positions[3][64];
+    uint32_t TexCoords[64];
+    uint32_t NormalTangents[64];
+    uint8_t Indices[3][128];
+};
+static_assert(sizeof(Meshlet) == 1728, "Meshlet layout");
+static_assert(offsetof(Meshlet, NumVertices) == 44 && offsetof(Meshlet, MaterialId) == 48, "Meshlet header");
+static_assert(offsetof(Meshlet, Positions) == 64 && offsetof(Meshlet, TexCoords) == 832, "Meshlet SoA");
+static_assert(offsetof(Meshlet, NormalTangents) == 1088 && offsetof(Meshlet, Indices) == 1344, "Meshlet SoA");
+
+enum { CULL_NONE = 0, CULL_FRONT_CCW = 1, CULL_FRONT_CW = 2 };  // FaceCullMode, Rasterizer.h:80
+
+// simd::round2i (SIMD.h:304): cvtps2dq with the default round-to-nearest-even mode;
+// NaN and out-of-range inputs give the x86 "integer indefinite" 0x80000000.
+static inline int32_t round2i(float x) {
+    if (!(x >= -2147483648.0f && x < 2147483648.0f)) return INT32_MIN;
+    return (int32_t)std::nearbyint(x);
+}
+// simd::conv<int> (truncation, cvttps2dq) with the same indefinite value.
+static inline int32_t trunc2i(float x) {
+    if (!(x > -2147483649.0f && x < 2147483648.0f)) return INT32_MIN;
+    return (int32_t)x;
+}
+// simd::max_abs (SIMD.h:335): vrangeps imm 0b1011, |larger magnitude| (NaN inputs are
+// outside the oracle's contract).
+static inline float max_abs(float a, float b) {
+    float fa = std::fabs(a), fb = std::fabs(b);
+    return fa > fb ? fa : fb;
+}
+// simd::min/max on floats (SIMD.h:308-328) compile to vminps/vmaxps under -ffast-math:
+// the second operand is returned when the compare is false (including NaN).
+static inline float vmin(float a, float b) { return a < b ? a : b; }
+static inline float vmax(float a, float b) { return a > b ? a : b; }
+
+// simd::ilog2, SIMD.h:426.
+static inline int32_t ilog2(float x) {
+    int32_t b;
+    memcpy(&b, &x, 4);
+    return (int32_t)((uint32_t)b - (127u << 23)) >> 23;
+}
+
+static inline uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
+static inline float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
+
+// AVX-512 rcp14/rsqrt14 (SIMD.h:294-296) or their correctly rounded model.
+float approx_rcp(float x);
+float approx_rsqrt(float x);
+static inline float approx_sqrt(float x) { return approx_rsqrt(x) * x; }
+
+// simd::gather_preload64 (SIMD.h:219-227): permutex2var over two 32-entry halves, so an
+// index selects entry idx for idx < 32 and 32 + (idx & 31) otherwise.
+static inline uint32_t preload64_index(uint32_t idx) { return idx < 32 ? idx : 32 + (idx & 31); }
+
+struct V4 { float x, y, z, w; };
+
+// simd::mul(mat4, v_float4) with w = 1 (SIMD.h:457-464), m column-major.
+static inline V4 transform_point(const float* m, float x, float y, float z) {
+    V4 r;
+    r.x = std::fma(x, m[0], std::fma(y, m[4], std::fma(z, m[8], 1.0f * m[12])));
+    r.y = std::fma(x, m[1], std::fma(y, m[5], std::fma(z, m[9], 1.0f * m[13])));
+    r.z = std::fma(x, m[2], std::fma(y, m[6], std::fma(z, m[10], 1.0f * m[14])));
+    r.w = std::fma(x, m[3], std::fma(y, m[7], std::fma(z, m[11], 1.0f * m[15])));
+    return r;
+}
+
+}  // namespace orc

@@ -1,0 +1,457 @@
+// Oracle (test infrastructure, see swr_oracle.h): framebuffer, mesh shader, clipper,
+// triangle setup and the vis-buffer fragment shader of GLimpSW's meshlet rasterizer,
+// restated lane by lane in the reference's operation order.
+#include "swr_oracle_common.h"
+
+#include <algorithm>
+#include <thread>
+#include <vector>
+
+namespace orc {
+
+// ---------------------------------------------------------------- framebuffer
+// CreateFramebuffer, Rasterizer.h:66-78: layer stride rounded to 64 words.
+uint32_t fb_layer_stride(uint32_t w, uint32_t h) { return (w * h + 63) & ~63u; }
+
+// Framebuffer::GetPixelOffset, Rasterizer.h:50-56 (4x4 tiles).
+static inline uint32_t pixel_offset(const orc_framebuffer* fb, uint32_t x, uint32_t y) {
+    uint32_t tileOffset = ((x & ~3u) << 2) + (y & ~3u) * fb->width;
+    uint32_t pixelOffset = (x & 3) + (y & 3) * 4;
+    return pixelOffset + tileOffset;
+}
+
+// ----------------------------------------------------------- packed int16 ops
+// The reference keeps (x, y) viewport positions as two int16 halves of one int32
+// lane and mixes per-16-bit ops (_mm512_*_epi16) with 32-bit adds/ands.
+static inline int32_t lo16(uint32_t v) { return (int16_t)(v & 0xFFFF); }
+static inline int32_t hi16(uint32_t v) { return (int16_t)(v >> 16); }
+static inline uint32_t pack16(int32_t lo, int32_t hi) { return (uint32_t)(uint16_t)lo | ((uint32_t)(uint16_t)hi << 16); }
+static inline uint32_t min16(uint32_t a, uint32_t b) { return pack16(std::min(lo16(a), lo16(b)), std::min(hi16(a), hi16(b))); }
+static inline uint32_t max16(uint32_t a, uint32_t b) { return pack16(std::max(lo16(a), lo16(b)), std::max(hi16(a), hi16(b))); }
+static inline uint32_t add16(uint32_t a, uint32_t b) { return pack16(lo16(a) + lo16(b), hi16(a) + hi16(b)); }
+static inline uint32_t srai16(uint32_t a, int s) { return pack16(lo16(a) >> s, hi16(a) >> s); }
+
+// ------------------------------------------------------------ triangle packet
+using Vtx = V4;
+
+struct TriSetup {   // one lane of TrianglePacket (Rasterizer.h:145-161)
+    uint32_t Pos0, Pos1, Pos2;
+    float Z0, Z1, Z2, W0, W1, W2;
+};
+struct EdgeVars {   // one lane of TriangleEdgeVars (Rasterizer.h:162-176)
+    int32_t Edge0, Edge1, Edge2, A01, A12, A20, B01, B12, B20;
+    float Z0, Z10, Z20, W0, W0S, W1S, W2S;
+};
+
+// simd::perspective_div, SIMD.h:473-476.
+static inline Vtx perspective_div(Vtx v) {
+    float rw = 1.0f / v.w;
+    return { v.x * rw, v.y * rw, v.z * rw, rw };
+}
+
+// TrianglePacket::GetBoundingBox / GetRenderBoundingBox, Rasterizer.cpp:331-351.
+static inline void render_bbox(const TriSetup& t, int halfW, int halfH, uint32_t& bbMin, uint32_t& bbMax) {
+    uint32_t minPos = min16(min16(t.Pos0, t.Pos1), t.Pos2);
+    uint32_t maxPos = max16(max16(t.Pos0, t.Pos1), t.Pos2);
+    minPos = srai16(minPos + 0x00070007u, 4);  // 32-bit add: a carry out of x reaches y
+    maxPos = srai16(maxPos + 0x00070007u, 4);
+
+    uint32_t vpSize = (uint32_t)halfW | ((uint32_t)halfH << 16);
+    uint32_t x = min16(max16(add16(minPos, vpSize), 0), vpSize * 2);
+    uint32_t y = min16(max16(add16(maxPos, vpSize), 0), vpSize * 2);
+    bbMin = (x + 0x00000000u) & ~0x00030003u;
+    bbMax = (y + 0x00030003u) & ~0x00030003u;
+}
+
+// TrianglePacket::Setup, Rasterizer.cpp:257-289. Returns the lane's keep bit.
+static bool tri_setup(Vtx v0, Vtx v1, Vtx v2, int halfW, int halfH, int cullMode, TriSetup& t) {
+    v0 = perspective_div(v0);
+    v1 = perspective_div(v1);
+    v2 = perspective_div(v2);
+
+    float det = (v2.x - v0.x) * (v1.y - v0.y) - (v0.x - v1.x) * (v0.y - v2.y);
+    if (cullMode != CULL_FRONT_CCW) {
+        bool flip = (cullMode == CULL_FRONT_CW) ? true : (det < 0);
+        det = flip ? -det : det;
+    }
+    bool keep = det > 0;
+
+    float fsx = (float)(halfW * 16), fsy = (float)(halfH * 16);
+    int32_t x0 = round2i(v0.x * fsx), y0 = round2i(v0.y * fsy);
+    int32_t x1 = round2i(v1.x * fsx), y1 = round2i(v1.y * fsy);
+    int32_t x2 = round2i(v2.x * fsx), y2 = round2i(v2.y * fsy);
+    t.Pos0 = ((uint32_t)x0 & 0xFFFF) | ((uint32_t)y0 << 16);
+    t.Pos1 = ((uint32_t)x1 & 0xFFFF) | ((uint32_t)y1 << 16);
+    t.Pos2 = ((uint32_t)x2 & 0xFFFF) | ((uint32_t)y2 << 16);
+
+    uint32_t bbMin, bbMax;
+    render_bbox(t, halfW, halfH, bbMin, bbMax);
+    // cmpge_epi16 on both halves, kept only if neither half has min >= max.
+    if (lo16(bbMin) >= lo16(bbMax) || hi16(bbMin) >= hi16(bbMax)) keep = false;
+
+    t.Z0 = v0.z, t.Z1 = v1.z, t.Z2 = v2.z;
+    t.W0 = v0.w, t.W1 = v1.w, t.W2 = v2.w;
+    return keep;
+}
+
+// ComputeEdge, Rasterizer.cpp:291-295 (wrapping int32 arithmetic).
+static inline int32_t compute_edge(int32_t a, int32_t x, int32_t b, int32_t y) {
+    int32_t w = (int32_t)((uint32_t)a * (uint32_t)x + (uint32_t)b * (uint32_t)y);
+    w = (int32_t)((uint32_t)w + ((a > 0 || (a == 0 && b > 0)) ? 0u : 0xFFFFFFFFu));
+    return w >> 4;
+}
+
+// TriangleEdgeVars::Setup, Rasterizer.cpp:296-329.
+static void edge_setup(const TriSetup& t, int halfW, int halfH, EdgeVars& e) {
+    int32_t x0 = (int32_t)(t.Pos0 << 16) >> 16, y0 = (int32_t)t.Pos0 >> 16;
+    int32_t x1 = (int32_t)(t.Pos1 << 16) >> 16, y1 = (int32_t)t.Pos1 >> 16;
+    int32_t x2 = (int32_t)(t.Pos2 << 16) >> 16, y2 = (int32_t)t.Pos2 >> 16;
+
+    int32_t A01 = y1 - y0, B01 = x0 - x1;
+    int32_t A12 = y2 - y1, B12 = x1 - x2;
+    int32_t A20 = y0 - y2, B20 = x2 - x0;
+    int32_t det = (int32_t)((uint32_t)B20 * (uint32_t)A01 - (uint32_t)B01 * (uint32_t)A20);
+    if (det < 0) {  // per-lane flip of the `any(det < 0)` block
+        A01 = -A01, B01 = -B01, A12 = -A12, B12 = -B12, A20 = -A20, B20 = -B20;
+        det = -det;
+    }
+    int32_t sampleX = (int32_t)((uint32_t)(-halfW) << 4) + 8, sampleY = (int32_t)((uint32_t)(-halfH) << 4) + 8;
+    e.Edge0 = compute_edge(A12, sampleX - x1, B12, sampleY - y1);
+    e.Edge1 = compute_edge(A20, sampleX - x2, B20, sampleY - y2);
+    e.Edge2 = compute_edge(A01, sampleX - x0, B01, sampleY - y0);
+    e.A01 = A01, e.A12 = A12, e.A20 = A20, e.B01 = B01, e.B12 = B12, e.B20 = B20;
+
+    float rcpArea = 16.0f / (float)det;
+    e.Z0 = t.Z0;
+    e.Z10 = (t.Z1 - t.Z0) * rcpArea;
+    e.Z20 = (t.Z2 - t.Z0) * rcpArea;
+    e.W0 = t.W0;
+    e.W0S = t.W0 * rcpArea;
+    e.W1S = t.W1 * rcpArea;
+    e.W2S = t.W2 * rcpArea;
+}
+
+// ----------------------------------------------------------------- clip codes
+enum { PLANE_LEFT = 0, PLANE_RIGHT, PLANE_TOP, PLANE_BOTTOM, PLANE_NEAR, PLANE_FAR };
+
+struct ClipCodes { uint16_t AcceptMask, NonTrivialMask; uint8_t OutCodes[16]; };
+
+// Clipper::ComputeClipCodes, Rasterizer.cpp:353-397.
+static ClipCodes compute_clip_codes(const Vtx v[3][16], float bx, float by) {
+    ClipCodes cc = {};
+    bool allInside = true;
+    for (int l = 0; l < 16; l++) {
+        for (int i = 0; i < 3; i++) {
+            const Vtx& p = v[i][l];
+            float m = max_abs(max_abs(p.x, p.y), p.z);
+            if (!(m < p.w)) allInside = false;
+        }
+    }
+    if (allInside) { cc.AcceptMask = 0xFFFF; return cc; }
+
+    for (int l = 0; l < 16; l++) {
+        uint8_t partial = 0, combined = 255;
+        bool trivial = true;
+        for (int i = 0; i < 3; i++) {
+            const Vtx& p = v[i][l];
+            uint8_t oc = 0;
+            oc |= (p.x < -p.w) ? (1 << PLANE_LEFT) : 0;
+            oc |= (p.x > +p.w) ? (1 << PLANE_RIGHT) : 0;
+            oc |= (p.y < -p.w) ? (1 << PLANE_TOP) : 0;
+            oc |= (p.y > +p.w) ? (1 << PLANE_BOTTOM) : 0;
+            oc |= (p.z < -p.w) ? (1 << PLANE_NEAR) : 0;
+            oc |= (p.z > +p.w) ? (1 << PLANE_FAR) : 0;
+            partial |= oc;
+            combined &= oc;
+            trivial = trivial && (std::fabs(p.x) < p.w * bx && std::fabs(p.y) < p.w * by);
+        }
+        if (partial & ((1 << PLANE_NEAR) | (1 << PLANE_FAR))) trivial = false;
+        bool accept = combined == 0;
+        if (accept && trivial) cc.AcceptMask |= 1u << l;
+        if (accept && !trivial) cc.NonTrivialMask |= 1u << l;
+        cc.OutCodes[l] = partial;
+    }
+    return cc;
+}
+
+// ---------------------------------------------------------------- draw state
+struct DrawCtx {
+    orc_framebuffer* fb;
+    const orc_shading_context* sc;
+    int halfW, halfH;
+    uint32_t rowBegin, rowEnd;  // rows this call may write
+    uint64_t* counters;
+};
+
+// Rasterizer::DrawTriangle<FS_EncodeSurfaceId<false>, IsClipped> (Rasterizer.h:250-328 with
+// Shading.cpp:309-331). The opaque vis-buffer shader uses only Depth and the ids, so the
+// perspective-correct barycentrics (rcp14 + Newton) do not affect its output.
+static void draw_triangle(DrawCtx& dc, const EdgeVars& e, uint32_t bbMin, uint32_t bbMax,
+                          uint32_t meshletId, uint32_t primId) {
+    orc_framebuffer* fb = dc.fb;
+    uint32_t minX = bbMin & 0xFFFF, minY = bbMin >> 16;
+    uint32_t maxX = bbMax & 0xFFFF, maxY = bbMax >> 16;
+    uint32_t y0 = std::max(minY, dc.rowBegin), y1 = std::min(maxY, dc.rowEnd);
+    float* depthBuf = (float*)&fb->data[1 * fb->layer_stride];
+    uint32_t* colorBuf = &fb->data[0];
+    uint32_t surfaceId = (dc.sc->meshlet_offset + meshletId) * 128u + primId;
+
+    for (uint32_t y = y0; y < y1; y++) {
+        for (uint32_t x = minX; x < maxX; x++) {
+            int32_t e0 = (int32_t)((uint32_t)e.Edge0 + (uint32_t)e.A12 * x + (uint32_t)e.B12 * y);
+            int32_t e1 = (int32_t)((uint32_t)e.Edge1 + (uint32_t)e.A20 * x + (uint32_t)e.B20 * y);
+            int32_t e2 = (int32_t)((uint32_t)e.Edge2 + (uint32_t)e.A01 * x + (uint32_t)e.B01 * y);
+            if ((e0 | e1 | e2) < 0) continue;
+
+            float u = (float)e1, v = (float)e2;
+            float depth = std::fma(u, e.Z10, std::fma(v, e.Z20, e.Z0));
+            uint32_t off = pixel_offset(fb, x, y);
+            if (!(depth > depthBuf[off])) continue;  // FS_EncodeSurfaceId depth test, Shading.cpp:312-313
+            depthBuf[off] = depth;
+            colorBuf[off] = surfaceId;
+        }
+    }
+}
+
+// ShadeMeshlet, Shading.cpp:281-307. ShadedMeshlet (Rasterizer.h:82-99) with vertices past the
+// transformed 16-vertex chunks zero-initialised (uninitialised stack memory in the reference).
+struct Shaded {
+    uint32_t PrimCount;
+    int CullMode;
+    uint32_t FragmentShaderId;
+    uint8_t Indices[3][128];
+    Vtx Pos[64];
+};
+
+static void shade_meshlet(const orc_shading_context* sc, uint32_t index, Shaded& out) {
+    out.PrimCount = 0;
+    out.CullMode = CULL_FRONT_CCW;
+    out.FragmentShaderId = 0;
+    if (sc->cull_bitmap != nullptr) {
+        uint16_t mask = sc->cull_bitmap[index / 16];
+        if (((mask >> (index % 16)) & 1) == 0) return;
+    }
+    const Meshlet& mesh = ((const Meshlet*)sc->meshlets)[sc->meshlet_offset + index];
+    const float* m = sc->object_to_clip;
+    for (uint32_t i = 0; i < 64; i++) out.Pos[i] = { 0, 0, 0, 0 };
+    for (uint32_t i0 = 0; i0 < mesh.NumVertices; i0 += 16) {
+        for (uint32_t i = i0; i < i0 + 16; i++) {
+            float x = mesh.Positions[0][i], y = mesh.Positions[1][i], z = mesh.Positions[2][i];
+            out.Pos[i] = transform_point(m, x, y, z);
+        }
+    }
+    out.PrimCount = mesh.NumTriangles;
+    memcpy(out.Indices, mesh.Indices, sizeof(mesh.Indices));
+    if (mesh.MaterialId != UINT32_MAX) {
+        const orc_material& mat = sc->materials[mesh.MaterialId];
+        out.CullMode = mat.is_double_sided ? CULL_NONE : CULL_FRONT_CCW;
+        out.FragmentShaderId = mat.alpha_cutoff < 255 ? 1 : 0;
+    }
+}
+
+// Clipper::ClipTriangles + FlushPacket, Rasterizer.cpp:398-491, for one packet. Emits the
+// clipped triangles in output order (prim id, then fan index); a callback draws each one.
+struct ClipOut { TriSetup t; bool keep; uint32_t primId; };
+
+static void clip_packet(const Vtx v[3][16], const ClipCodes& cc, uint16_t nonTrivialMask, float bx, float by,
+                        int halfW, int halfH, int cullMode, std::vector<ClipOut>& outs) {
+    float V[6][16 * 3 + 16];
+    for (uint32_t i = 0; i < 3; i++) {
+        for (uint32_t l = 0; l < 16; l++) {
+            uint32_t j = i * 16 + l;
+            V[0][j] = v[i][l].x, V[1][j] = v[i][l].y, V[2][j] = v[i][l].z, V[3][j] = v[i][l].w;
+            V[4][j] = (i == 1) ? 1.0f : 0.0f;
+            V[5][j] = (i == 2) ? 1.0f : 0.0f;
+        }
+    }
+    const float guard[2] = { bx, by };
+    uint32_t outIdx = 0;
+    for (uint32_t primId = 0; primId < 16; primId++) {
+        if (!((nonTrivialMask >> primId) & 1)) continue;
+        uint8_t indices[32] = { (uint8_t)(primId), (uint8_t)(primId + 16), (uint8_t)(primId + 32) };
+        uint32_t vertCount = 3, nextIdx = 48;
+
+        for (uint32_t planeId = 0; planeId < 8; planeId++) {
+            if (!((cc.OutCodes[primId] >> planeId) & 1)) continue;
+            uint8_t outIndices[32];
+            uint32_t outCount = 0;
+            float planeScale = planeId < 4 ? guard[planeId / 2] : 1.0f;
+
+            for (uint32_t vi = 0; vi < vertCount; vi++) {
+                uint8_t ia = indices[vi], ib = indices[(vi + 1) % vertCount];
+                // Clipper::GetIntersectDist, Rasterizer.cpp:76-81
+                float aa = V[planeId / 2][ia], ab = V[planeId / 2][ib];
+                if (planeId % 2) aa = -aa, ab = -ab;
+                float da = aa + V[3][ia] * planeScale;
+                float db = ab + V[3][ib] * planeScale;
+
+                if (da >= 0) outIndices[outCount++] = ia;
+                if ((da >= 0) != (db >= 0)) {
+                    float t = da / (da - db);
+                    for (uint32_t k = 0; k < 6; k++) {
+                        V[k][nextIdx] = std::fma(V[k][ib], t, std::fma(-t, V[k][ia], V[k][ia]));
+                    }
+                    outIndices[outCount++] = (uint8_t)nextIdx++;
+                }
+            }
+            if (vertCount < 3) break;  // stale count check, Rasterizer.cpp:443
+            vertCount = outCount;
+            memcpy(indices, outIndices, sizeof(indices));
+        }
+        if (vertCount < 2) continue;
+
+        for (uint32_t vi = 0; vi + 2 < vertCount; vi++) {
+            uint32_t i0 = indices[0], i1 = indices[vi + 1], i2 = indices[vi + 2];
+            Vtx a = { V[0][i0], V[1][i0], V[2][i0], V[3][i0] };
+            Vtx b = { V[0][i1], V[1][i1], V[2][i1], V[3][i1] };
+            Vtx c = { V[0][i2], V[1][i2], V[2][i2], V[3][i2] };
+            ClipOut co;
+            co.keep = tri_setup(a, b, c, halfW, halfH, cullMode, co.t);
+            co.primId = primId;
+            outs.push_back(co);
+            if (++outIdx >= 8 * 16) return;  // output truncation, Rasterizer.cpp:470-472
+        }
+    }
+}
+
+static void draw_meshlets(DrawCtx& dc, uint32_t count, const orc_raster_flags* flags) {
+    const orc_shading_context* sc = dc.sc;
+    orc_framebuffer* fb = dc.fb;
+    int halfW = (int)fb->width / 2, halfH = (int)fb->height / 2;
+    dc.halfW = halfW, dc.halfH = halfH;
+    // DrawMeshletsST (Rasterizer.cpp:154-156) honours EnableGuardband; the binned path does not (509).
+    float bx = 2896.0f / (float)fb->width, by = 2896.0f / (float)fb->height;
+    bool binned = flags->enable_binning != 0;
+    if (!binned && !flags->enable_guardband) bx = 1.0f, by = 1.0f;
+    bool clip = !binned && flags->enable_clipping;
+
+    Shaded mesh;
+    std::vector<ClipOut> clipOuts;
+    clipOuts.reserve(128);
+
+    for (uint32_t meshIdx = 0; meshIdx < count; meshIdx++) {
+        shade_meshlet(sc, meshIdx, mesh);
+        if (mesh.PrimCount == 0) continue;
+        if (dc.counters) dc.counters[ORC_TRIS_PROCESSED] += mesh.PrimCount;
+        if (mesh.FragmentShaderId != 0) {
+            // FS_EncodeSurfaceId<true> samples the material with barycentrics from rcp14;
+            // this oracle restates only the opaque entry point.
+            fprintf(stderr, "orc_draw_meshlets: alpha-tested materials are not supported by the oracle\n");
+            abort();
+        }
+
+        for (uint32_t primOffset = 0; primOffset < mesh.PrimCount; primOffset += 16) {
+            Vtx v[3][16];
+            for (uint32_t l = 0; l < 16; l++) {
+                for (uint32_t k = 0; k < 3; k++) v[k][l] = mesh.Pos[preload64_index(mesh.Indices[k][primOffset + l])];
+            }
+            ClipCodes cc = compute_clip_codes(v, bx, by);
+            if (primOffset + 16 > mesh.PrimCount) {
+                uint16_t trail = (uint16_t)((1u << (mesh.PrimCount % 16)) - 1);
+                cc.AcceptMask &= trail;
+                cc.NonTrivialMask &= trail;
+            }
+            if (cc.NonTrivialMask && dc.counters && (binned || clip))
+                dc.counters[ORC_TRIS_CLIPPED] += (uint64_t)__builtin_popcount(cc.NonTrivialMask);
+
+            if (cc.AcceptMask != 0) {
+                for (uint32_t l = 0; l < 16; l++) {
+                    if (!((cc.AcceptMask >> l) & 1)) continue;
+                    TriSetup t;
+                    if (!tri_setup(v[0][l], v[1][l], v[2][l], halfW, halfH, mesh.CullMode, t)) continue;
+                    uint32_t bbMin, bbMax;
+                    render_bbox(t, halfW, halfH, bbMin, bbMax);
+                    EdgeVars e;
+                    edge_setup(t, halfW, halfH, e);
+                    draw_triangle(dc, e, bbMin, bbMax, meshIdx, primOffset + l);
+                    if (dc.counters) dc.counters[ORC_TRIS_RASTERIZED]++;
+                }
+            }
+            if (cc.NonTrivialMask != 0 && clip) {
+                clipOuts.clear();
+                clip_packet(v, cc, cc.NonTrivialMask, bx, by, halfW, halfH, mesh.CullMode, clipOuts);
+                for (const ClipOut& co : clipOuts) {
+                    if (!co.keep) continue;
+                    uint32_t bbMin, bbMax;
+                    render_bbox(co.t, halfW, halfH, bbMin, bbMax);
+                    EdgeVars e;
+                    edge_setup(co.t, halfW, halfH, e);
+                    draw_triangle(dc, e, bbMin, bbMax, meshIdx, primOffset + co.primId);
+                    if (dc.counters) dc.counters[ORC_TRIS_RASTERIZED]++;
+                }
+            }
+        }
+    }
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+extern "C" {
+
+uint32_t orc_meshlet_size(void) { return (uint32_t)sizeof(Meshlet); }
+
+uint32_t orc_fb_layer_stride(uint32_t width, uint32_t height) { return fb_layer_stride(width, height); }
+
+void orc_fb_init(orc_framebuffer* fb, uint32_t width, uint32_t height, uint32_t num_layers, uint32_t* storage) {
+    fb->width = width;
+    fb->height = height;
+    fb->tile_stride = width / 4;
+    fb->layer_stride = fb_layer_stride(width, height);
+    fb->num_layers = num_layers;
+    fb->data = storage;
+}
+
+// Framebuffer::ClearLayer, Rasterizer.h:39-48 (fills Width*Height words of the layer).
+void orc_fb_clear_layer(orc_framebuffer* fb, uint32_t layer, uint32_t value) {
+    uint32_t* p = &fb->data[(size_t)layer * fb->layer_stride];
+    for (uint32_t i = 0; i < fb->width * fb->height; i++) p[i] = value;
+}
+
+// Framebuffer::Clear, Rasterizer.h:35-38.
+void orc_fb_clear(orc_framebuffer* fb, uint32_t color, float depth) {
+    orc_fb_clear_layer(fb, 0, color);
+    uint32_t d;
+    memcpy(&d, &depth, 4);
+    orc_fb_clear_layer(fb, 1, d);
+}
+
+// Framebuffer::GetPixels, ImageHelpers.cpp:109-147 (de-tiles a layer to row-major).
+void orc_fb_get_pixels(const orc_framebuffer* fb, uint32_t layer, uint32_t* dest, uint32_t stride) {
+    const uint32_t* src = &fb->data[(size_t)layer * fb->layer_stride];
+    for (uint32_t y = 0; y < fb->height; y++)
+        for (uint32_t x = 0; x < fb->width; x++) dest[(size_t)y * stride + x] = src[pixel_offset(fb, x, y)];
+}
+
+void orc_draw_meshlets_rows(orc_framebuffer* fb, uint32_t count, const orc_shading_context* ctx,
+                            const orc_raster_flags* flags, uint64_t counters[4], uint32_t row_begin, uint32_t row_end) {
+    DrawCtx dc = {};
+    dc.fb = fb;
+    dc.sc = ctx;
+    dc.rowBegin = row_begin;
+    dc.rowEnd = std::min(row_end, fb->height);
+    dc.counters = counters;
+    draw_meshlets(dc, count, flags);
+}
+
+void orc_draw_meshlets(orc_framebuffer* fb, uint32_t count, const orc_shading_context* ctx,
+                       const orc_raster_flags* flags, uint64_t counters[4]) {
+    orc_draw_meshlets_rows(fb, count, ctx, flags, counters, 0, fb->height);
+}
+
+void orc_draw_meshlets_mt(orc_framebuffer* fb, uint32_t count, const orc_shading_context* ctx,
+                          const orc_raster_flags* flags, uint32_t num_threads) {
+    if (num_threads <= 1) { orc_draw_meshlets(fb, count, ctx, flags, nullptr); return; }
+    std::vector<std::thread> threads;
+    uint32_t rows = (fb->height + num_threads - 1) / num_threads;
+    rows = (rows + 3) & ~3u;
+    for (uint32_t t = 0; t < num_threads; t++) {
+        uint32_t r0 = t * rows, r1 = std::min(fb->height, r0 + rows);
+        if (r0 >= r1) break;
+        threads.emplace_back([=]() { orc_draw_meshlets_rows(fb, count, ctx, flags, nullptr, r0, r1); });
+    }
+    for (auto& th : threads) th.join();
+}
+
+}  // extern "C"

@@ -1,0 +1,89 @@
+"""Shared test helpers: render a scene with the CUDA library and with the CPU oracle."""
+from __future__ import annotations
+
+import numpy as np
+
+from glimpsw_gb300 import scenes
+
+
+def meshlet_from_clip_triangles(tris, material_id=0):
+    """One meshlet whose object positions map to the given clip-space vertices through
+    CLIP_FROM_OBJECT (x, y, near, z): pass (x, y, w) per vertex."""
+    m = np.zeros(1, dtype=scenes.MESHLET_DTYPE)
+    tris = np.asarray(tris, dtype=np.float32).reshape(-1, 3, 3)
+    n = len(tris)
+    assert n <= 21
+    pos = tris.reshape(-1, 3)
+    m["Positions"][0, :, : len(pos)] = pos.T
+    m["NumVertices"] = len(pos)
+    m["NumTriangles"] = n
+    m["AlphaCutoff"] = 255
+    m["MaterialId"] = material_id
+    idx = np.zeros((3, 128), dtype=np.uint8)
+    idx[:, :n] = np.arange(3 * n).reshape(n, 3).T
+    m["Indices"] = idx[None]
+    return m
+
+
+# clip = (x, y, 0.1, z_obj): a projection with f = 1 and NearZ 0.1, so w = object z.
+CLIP_FROM_OBJECT = np.array([1, 0, 0, 0,
+                             0, 1, 0, 0,
+                             0, 0, 0, 1,
+                             0, 0, 0.1, 0], dtype=np.float32)
+
+
+def render_oracle(meshlets, materials, object_to_clip, width, height, count=None, binning=False, clipping=True,
+                  guardband=True, meshlet_offset=0, cull_bitmap=None, clear=(0xFF000000, 0.0), fb=None):
+    from oracle import oracle as O
+    if fb is None:
+        fb = O.Framebuffer(width, height)
+        fb.clear(*clear)
+    ctx = O.Context(meshlets, materials, object_to_clip, meshlet_offset=meshlet_offset, cull_bitmap=cull_bitmap)
+    n = len(meshlets) - meshlet_offset if count is None else count
+    counters = O.draw_meshlets(fb, ctx, n, binning=binning, clipping=clipping, guardband=guardband)
+    return fb, counters
+
+
+class GpuRenderer:
+    def __init__(self, meshlets, materials, textures=None):
+        from glimpsw_gb300 import api
+        self.api = api
+        api.load_library()
+        self.scene = api.Scene()
+        self.scene.upload_meshlets(np.ascontiguousarray(meshlets))
+        self.scene.set_materials(materials, textures)
+        self.rast = api.Rasterizer()
+
+    def render(self, object_to_clip, width, height, count=None, binning=False, clipping=True, guardband=True,
+               meshlet_offset=0, cull_bitmap=None, clear=(0xFF000000, 0.0), fb=None):
+        api = self.api
+        if fb is None:
+            fb = api.Framebuffer(width, height)
+            fb.clear(*clear)
+        self.rast.EnableBinning = binning
+        self.rast.EnableClipping = clipping
+        self.rast.EnableGuardband = guardband
+        ctx = api.ShadingContext(self.scene, object_to_clip, meshlet_offset=meshlet_offset, cull_bitmap=cull_bitmap)
+        n = (self._count() - meshlet_offset) if count is None else count
+        self.rast.reset_counters()
+        self.rast.draw_meshlets(fb, n, ctx)
+        return fb, self.rast.counters()
+
+    def _count(self):
+        import ctypes as C
+        c = C.c_uint32()
+        self.api._check(self.api._lib.swr_scene_meshlet_count(self.scene.h, C.byref(c)))
+        return c.value
+
+
+def assert_visbuffer_equal(gpu_fb, orc_fb):
+    g_ids, o_ids = gpu_fb.get_pixels(0), orc_fb.get_pixels(0)
+    g_d, o_d = gpu_fb.get_pixels(1), orc_fb.get_pixels(1)
+    bad_d = np.argwhere(g_d != o_d)
+    bad_i = np.argwhere(g_ids != o_ids)
+    msg = ""
+    if len(bad_d) or len(bad_i):
+        y, x = (bad_d if len(bad_d) else bad_i)[0]
+        msg = (f"{len(bad_d)} depth / {len(bad_i)} id mismatches; first at (x={x}, y={y}): gpu depth "
+               f"{g_d[y, x]:#010x} id {g_ids[y, x]} vs oracle depth {o_d[y, x]:#010x} id {o_ids[y, x]}")
+    assert not msg, msg
