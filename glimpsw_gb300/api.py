@@ -63,6 +63,7 @@ _SIGS = {
     "swr_rasterizer_destroy": [C.c_void_p],
     "swr_rasterizer_set_flags": [C.c_void_p, C.c_int, C.c_int, C.c_int],
     "swr_rasterizer_get_counters": [C.c_void_p, C.c_void_p],
+    "swr_rasterizer_set_queue_capacity": [C.c_void_p, C.c_uint32],
     "swr_rasterizer_reset_counters": [C.c_void_p],
     "swr_draw_meshlets": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p],
     "swr_framebuffer_create": [C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p],
@@ -364,6 +365,9 @@ class Rasterizer:
 
     def draw_meshlets(self, fb: Framebuffer, count: int, ctx: ShadingContext, shader: int = VisBufferShader) -> None:
         _check(_lib.swr_draw_meshlets(self.h, fb.h, count, shader, C.byref(ctx.s)))
+
+    def set_queue_capacity(self, triangles: int) -> None:
+        _check(_lib.swr_rasterizer_set_queue_capacity(self.h, triangles))
 
     def counters(self) -> np.ndarray:
         out = np.zeros(4, dtype=np.uint64)

@@ -67,8 +67,39 @@ swr_status ensure_scratch(swr_rasterizer r) {
     SWR_CUDA(cudaMalloc(&s.control, 16 * sizeof(unsigned long long)));
     SWR_CUDA(cudaMemset(s.control, 0, 16 * sizeof(unsigned long long)));
     s.bigCapacity = kDefaultBigCapacity;
-    SWR_CUDA(cudaMalloc(&s.big, (size_t)s.bigCapacity * sizeof(TriRec)));
-    SWR_CUDA(cudaMalloc(&s.bigBase, (size_t)s.bigCapacity * sizeof(unsigned long long)));
+    // stream-ordered allocations, so size_queue can replace them with cudaFreeAsync
+    SWR_CUDA(cudaMallocAsync(&s.big, (size_t)s.bigCapacity * sizeof(TriRec), t_stream));
+    SWR_CUDA(cudaMallocAsync(&s.bigBase, (size_t)s.bigCapacity * sizeof(unsigned long long), t_stream));
+    SWR_CUDA(cudaStreamSynchronize(t_stream));
+    SWR_CUDA(cudaMallocHost(&r->hostStatus, sizeof(unsigned long long)));
+    *r->hostStatus = 0;
+    SWR_CUDA(cudaEventCreateWithFlags(&r->statusEvent, cudaEventDisableTiming));
+    return SWR_OK;
+}
+
+// Sizes the large-triangle queue for a draw of `count` meshlets: a quarter of their triangles by
+// default, all of them once a draw has overflowed. Reallocation is stream-ordered. A full queue
+// never loses triangles (the draw kernel rasterizes them itself); it only costs time.
+swr_status size_queue(swr_rasterizer r, uint32_t count) {
+    if (r->statusPending && cudaEventQuery(r->statusEvent) == cudaSuccess) {
+        r->statusPending = false;
+        if (*r->hostStatus & kStatusBigOverflow) r->sawOverflow = true;
+    }
+    uint64_t want = (uint64_t)count * (r->sawOverflow ? 128u : 32u);
+    want = std::min<uint64_t>(std::max<uint64_t>(want, kDefaultBigCapacity), 1u << 26);
+    DrawScratch& s = r->scratch;
+    if (r->fixedCapacity) {
+        if (s.bigCapacity != r->fixedCapacity) s.bigCapacity = std::min(r->fixedCapacity, s.bigCapacity);
+        if (s.bigCapacity == r->fixedCapacity) return SWR_OK;
+        want = r->fixedCapacity;
+    }
+    if (want <= s.bigCapacity) return SWR_OK;
+    SWR_CUDA(cudaFreeAsync(s.big, t_stream));
+    SWR_CUDA(cudaFreeAsync(s.bigBase, t_stream));
+    s.big = nullptr, s.bigBase = nullptr, s.bigCapacity = 0;
+    SWR_CUDA(cudaMallocAsync(&s.big, (size_t)want * sizeof(TriRec), t_stream));
+    SWR_CUDA(cudaMallocAsync(&s.bigBase, (size_t)want * sizeof(unsigned long long), t_stream));
+    s.bigCapacity = (uint32_t)want;
     return SWR_OK;
 }
 
@@ -161,8 +192,10 @@ swr_status swr_rasterizer_create(uint32_t num_threads, swr_rasterizer* out) {
 swr_status swr_rasterizer_destroy(swr_rasterizer r) {
     if (!r) return SWR_OK;
     cudaFree(r->scratch.control);
-    cudaFree(r->scratch.big);
+    cudaFree(r->scratch.big);  // cudaFree synchronises for stream-ordered allocations
     cudaFree(r->scratch.bigBase);
+    if (r->hostStatus) cudaFreeHost(r->hostStatus);
+    if (r->statusEvent) cudaEventDestroy(r->statusEvent);
     delete r;
     return SWR_OK;
 }
@@ -172,6 +205,12 @@ swr_status swr_rasterizer_set_flags(swr_rasterizer r, int enable_binning, int en
     r->enable_binning = enable_binning != 0;
     r->enable_clipping = enable_clipping != 0;
     r->enable_guardband = enable_guardband != 0;
+    return SWR_OK;
+}
+
+swr_status swr_rasterizer_set_queue_capacity(swr_rasterizer r, uint32_t triangles) {
+    if (!r) return fail(SWR_EINVAL, "swr_rasterizer_set_queue_capacity: NULL rasterizer");
+    r->fixedCapacity = triangles;
     return SWR_OK;
 }
 
@@ -377,6 +416,7 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
                     (unsigned long long)ctx->meshlet_offset + count, sc->count);
     if (count == 0) return SWR_OK;
     swr_status st = ensure_scratch(r);
+    if (st == SWR_OK) st = size_queue(r, count);
     if (st != SWR_OK) return st;
     if (!fb->keys_valid) {
         launch_init_keys(fb->layers + fb->layer_stride, fb->keys, fb->width * fb->height, t_stream);
@@ -404,6 +444,12 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
     SWR_CUDA(cudaMemsetAsync(r->scratch.control, 0, 3 * sizeof(unsigned long long), t_stream));
     launch_draw(a, t_stream, num_sms());
     SWR_CHECK_LAUNCH("swr_draw_meshlets");
+    if (!r->statusPending) {
+        SWR_CUDA(cudaMemcpyAsync(r->hostStatus, r->scratch.control + 2, sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, t_stream));
+        SWR_CUDA(cudaEventRecord(r->statusEvent, t_stream));
+        r->statusPending = true;
+    }
     launch_finalize(fb->keys, fb->layers, fb->layers + fb->layer_stride, fb->width * fb->height, t_stream);
     SWR_CHECK_LAUNCH("swr_draw_meshlets: finalize");
     return SWR_OK;

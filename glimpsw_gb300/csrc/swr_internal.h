@@ -117,4 +117,11 @@ struct swr_texture_t {
 struct swr_rasterizer_t {
     int enable_binning, enable_clipping, enable_guardband;
     swr::DrawScratch scratch;
+    // Queue sizing: the status word of each draw is copied to pinned memory; a later draw that
+    // sees an overflow reported sizes the queue for every triangle of a draw.
+    unsigned long long* hostStatus;   // pinned
+    cudaEvent_t statusEvent;
+    bool statusPending;
+    bool sawOverflow;
+    uint32_t fixedCapacity;           // 0: automatic sizing
 };

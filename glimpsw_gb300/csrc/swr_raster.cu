@@ -121,29 +121,16 @@ __device__ __forceinline__ void shade_fragment(const TriRec& r, uint32_t px, uin
     if (key > *(volatile unsigned long long*)p) atomicMax(p, key);
 }
 
-// Rasterizes tiles [t0, t0 + n) of a box tilesX wide, two tiles per warp step.
-__device__ __forceinline__ void raster_tiles(const TriRec& r, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
-                                             unsigned long long* keys, uint32_t width, int lane) {
-    if (tilesX <= 0 || tilesY <= 0) return;
-    int T = tilesX * tilesY;
-    int tx = lane >> 4, ty = 0;
-    while (tx >= tilesX) tx -= tilesX, ty++;
-    uint32_t fx = lane & 3, fy = (lane >> 2) & 3;
-    for (int t0 = 0; t0 < T; t0 += 2) {
-        if (t0 + (lane >> 4) < T) shade_fragment(r, x0 + tx * 4 + fx, y0 + ty * 4 + fy, keys, width);
-        tx += 2;
-        while (tx >= tilesX) tx -= tilesX, ty++;
-    }
-}
-
-// One lane rasterizes a whole triangle (queue overflow fallback; slow but exact).
+// One lane rasterizes a whole triangle (fallback of the rare clipped triangle that finds the
+// queue full; slow but exact).
 __device__ __noinline__ void raster_serial(const TriRec& r, unsigned long long* keys, uint32_t width) {
     uint32_t minX = r.bbMin & 0xFFFF, minY = r.bbMin >> 16, maxX = r.bbMax & 0xFFFF, maxY = r.bbMax >> 16;
     for (uint32_t y = minY; y < maxY; y++)
         for (uint32_t x = minX; x < maxX; x++) shade_fragment(r, x, y, keys, width);
 }
 
-__device__ __forceinline__ void enqueue_big(const TriRec& r, const DrawArgs& a) {
+// Appends a triangle to the chunk queue; false when the queue is full (the caller rasterizes it).
+__device__ __forceinline__ bool enqueue_big(const TriRec& r, const DrawArgs& a) {
     int tilesX = ((r.bbMax & 0xFFFF) - (r.bbMin & 0xFFFF)) >> 2;
     int tilesY = ((r.bbMax >> 16) - (r.bbMin >> 16)) >> 2;
     unsigned long long chunks = (unsigned long long)((tilesX + kChunkTiles - 1) / kChunkTiles) *
@@ -153,9 +140,51 @@ __device__ __forceinline__ void enqueue_big(const TriRec& r, const DrawArgs& a) 
     if (slot < a.s.bigCapacity) {
         a.s.big[slot] = r;
         a.s.bigBase[slot] = old & ((1ull << 40) - 1);
-    } else {
-        atomicOr(&a.s.control[2], kStatusBigOverflow);
-        raster_serial(r, a.keys, a.width);
+        return true;
+    }
+    atomicOr(&a.s.control[2], kStatusBigOverflow);
+    return false;
+}
+
+// Largest value over the tile [px, px+3] x [py, py+3] of the affine edge function e(px, py) + A*dx + B*dy.
+__device__ __forceinline__ int32_t tile_max_edge(int32_t e, int32_t A, int32_t B) {
+    return e + (A > 0 ? 3 * A : 0) + (B > 0 ? 3 * B : 0);
+}
+// True if no sample of the 4x4 tile at (px, py) can pass all three edges.
+__device__ __forceinline__ bool tile_empty(const TriRec& r, uint32_t px, uint32_t py) {
+    int32_t e0 = (int32_t)((uint32_t)r.E0 + (uint32_t)r.A12 * px + (uint32_t)r.B12 * py);
+    int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
+    int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
+    return tile_max_edge(e0, r.A12, r.B12) < 0 || tile_max_edge(e1, r.A20, r.B20) < 0 ||
+           tile_max_edge(e2, r.A01, r.B01) < 0;
+}
+
+// Rasterizes the tiles of [x0, x0 + 4*tilesX) x [y0, y0 + 4*tilesY) that are not provably empty:
+// 32 tiles are tested at a time (one per lane), then the surviving tiles are shaded two at a time.
+__device__ __forceinline__ void raster_region(const TriRec& r, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
+                                              unsigned long long* keys, uint32_t width, int lane) {
+    const int T = tilesX * tilesY;
+    const uint32_t fx = lane & 3, fy = (lane >> 2) & 3, half = lane >> 4;
+    for (int tb = 0; tb < T; tb += 32) {
+        const int t = tb + lane;
+        bool live = false;
+        uint32_t tpx = 0, tpy = 0;
+        if (t < T) {
+            int ty = t / tilesX, tx = t - ty * tilesX;
+            tpx = x0 + tx * 4, tpy = y0 + ty * 4;
+            live = !tile_empty(r, tpx, tpy);
+        }
+        unsigned mask = __ballot_sync(0xFFFFFFFFu, live);
+        while (mask) {
+            int s0 = __ffs(mask) - 1;
+            mask &= mask - 1;
+            int s1 = mask ? __ffs(mask) - 1 : -1;
+            if (s1 >= 0) mask &= mask - 1;
+            const int src = half ? s1 : s0;
+            const uint32_t qx = __shfl_sync(0xFFFFFFFFu, tpx, src & 31);
+            const uint32_t qy = __shfl_sync(0xFFFFFFFFu, tpy, src & 31);
+            if (src >= 0) shade_fragment(r, qx + fx, qy + fy, keys, width);
+        }
     }
 }
 
@@ -212,7 +241,7 @@ __device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t out
         if (!tri_setup(a0, a1, a2, a.halfW, a.halfH, cullMode, t, bbMin, bbMax)) continue;
         TriRec r;
         edge_setup(t, a.halfW, a.halfH, bbMin, bbMax, make_rank(gMeshlet, prim, 1, vi), r);
-        enqueue_big(r, a);
+        if (!enqueue_big(r, a)) raster_serial(r, a.keys, a.width);
         nRaster++;
     }
 }
@@ -296,7 +325,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs 
             const bool nontriv = accept && !trivial;
             if (a.countClipped) nClipped += __popc(__ballot_sync(0xFFFFFFFFu, nontriv)) * (lane == 0);
 
-            bool small = false;
+            int myTiles = 0;     // tiles of this lane's small triangle (0 if none)
+            bool overflow = false;
             if (acc) {
                 Setup t;
                 uint32_t bbMin, bbMax;
@@ -304,27 +334,55 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs 
                     TriRec r;
                     edge_setup(t, a.halfW, a.halfH, bbMin, bbMax, make_rank(g, p, 0, 0), r);
                     nRaster++;
-                    int tilesX = ((bbMax & 0xFFFF) - (bbMin & 0xFFFF)) >> 2;
-                    int tilesY = ((bbMax >> 16) - (bbMin >> 16)) >> 2;
+                    const int tilesX = ((bbMax & 0xFFFF) - (bbMin & 0xFFFF)) >> 2;
+                    const int tilesY = ((bbMax >> 16) - (bbMin >> 16)) >> 2;
                     if (tilesX * tilesY <= kSmallTiles) {
+                        // tile index -> row by a multiply-shift (exact for tile < 16, tilesX <= 16)
+                        r.pad = (uint32_t)tilesX | ((uint32_t)((256 + tilesX - 1) / tilesX) << 8);
                         tris[lane] = r;
-                        small = true;
-                    } else {
-                        enqueue_big(r, a);
+                        myTiles = tilesX * tilesY;
+                    } else if (!enqueue_big(r, a)) {
+                        tris[lane] = r;
+                        overflow = true;
                     }
                 }
             }
             if (nontriv && a.clipMode) clip_and_queue(v0, v1, v2, partial, a, cullMode, g, p, nRaster);
-
-            unsigned smallMask = __ballot_sync(0xFFFFFFFFu, small);
             __syncwarp();
-            while (smallMask) {
-                const int src = __ffs(smallMask) - 1;
-                smallMask &= smallMask - 1;
+
+            // Small triangles: the warp walks the concatenated tile lists of all of them, two
+            // tiles (32 pixels) per step, so tiny triangles share steps.
+            int incl = myTiles;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+                if (lane >= o) incl += v;
+            }
+            const int excl = incl - myTiles;
+            const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
+            const uint32_t fx = lane & 3, fy = (lane >> 2) & 3, half = lane >> 4;
+            for (int b = 0; b < total; b += 2) {
+                const unsigned m0 = __ballot_sync(0xFFFFFFFFu, incl > b);
+                const unsigned m1 = __ballot_sync(0xFFFFFFFFu, incl > b + 1);
+                const int owner = __ffs(half ? m1 : m0) - 1;
+                const int ownerExcl = __shfl_sync(0xFFFFFFFFu, excl, owner & 31);
+                if (owner >= 0) {
+                    const TriRec& r = tris[owner];
+                    const int tile = b + (int)half - ownerExcl;
+                    const int tilesX = r.pad & 0xFF, magic = r.pad >> 8;
+                    const int ty = (tile * magic) >> 8, tx = tile - ty * tilesX;
+                    shade_fragment(r, (r.bbMin & 0xFFFF) + tx * 4 + fx, (r.bbMin >> 16) + ty * 4 + fy, a.keys, a.width);
+                }
+            }
+            // Triangles the full queue turned away are rasterized here by the whole warp.
+            unsigned ovMask = __ballot_sync(0xFFFFFFFFu, overflow);
+            while (ovMask) {
+                const int src = __ffs(ovMask) - 1;
+                ovMask &= ovMask - 1;
                 const TriRec r = tris[src];
                 const uint32_t x0 = r.bbMin & 0xFFFF, y0 = r.bbMin >> 16;
-                const int tilesX = (int)(((r.bbMax & 0xFFFF) - x0) >> 2), tilesY = (int)(((r.bbMax >> 16) - y0) >> 2);
-                raster_tiles(r, x0, y0, tilesX, tilesY, a.keys, a.width, lane);
+                raster_region(r, x0, y0, (int)(((r.bbMax & 0xFFFF) - x0) >> 2), (int)(((r.bbMax >> 16) - y0) >> 2),
+                              a.keys, a.width, lane);
             }
             __syncwarp();
         }
@@ -366,23 +424,8 @@ __global__ void __launch_bounds__(256) k_raster_big(const TriRec* __restrict__ b
         const uint32_t cy = c / chunksX, cx = c - cy * chunksX;
         const uint32_t x0 = minX + cx * (kChunkTiles * 4), y0 = minY + cy * (kChunkTiles * 4);
         const uint32_t x1 = min(x0 + kChunkTiles * 4, maxX), y1 = min(y0 + kChunkTiles * 4, maxY);
-        // Conservative chunk rejection: an edge negative at all four corner samples is negative
-        // over the whole chunk (edge functions are affine in the pixel position).
-        bool empty = false;
-        {
-            const int32_t E[3] = { r.E0, r.E1, r.E2 };
-            const int32_t A[3] = { r.A12, r.A20, r.A01 }, B[3] = { r.B12, r.B20, r.B01 };
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                int32_t c00 = (int32_t)((uint32_t)E[k] + (uint32_t)A[k] * x0 + (uint32_t)B[k] * y0);
-                int32_t c10 = (int32_t)((uint32_t)E[k] + (uint32_t)A[k] * (x1 - 1) + (uint32_t)B[k] * y0);
-                int32_t c01 = (int32_t)((uint32_t)E[k] + (uint32_t)A[k] * x0 + (uint32_t)B[k] * (y1 - 1));
-                int32_t c11 = (int32_t)((uint32_t)E[k] + (uint32_t)A[k] * (x1 - 1) + (uint32_t)B[k] * (y1 - 1));
-                if ((c00 & c10 & c01 & c11) < 0) empty = true;
-            }
-        }
-        if (empty) continue;
-        raster_tiles(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), keys, width, lane);
+        // Empty tiles of the chunk are rejected by their corner samples inside raster_region.
+        raster_region(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), keys, width, lane);
     }
 }
 

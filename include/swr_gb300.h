@@ -111,6 +111,12 @@ swr_status swr_rasterizer_destroy(swr_rasterizer r);
  * non-trivial triangles are clipped when clipping is enabled. */
 swr_status swr_rasterizer_set_flags(swr_rasterizer r, int enable_binning, int enable_clipping,
                                     int enable_guardband);
+/* Capacity (triangles) of the device queue that carries large and clipped triangles from the
+ * mesh stage to the chunk rasterizer; 0 (default) sizes it per draw. The reference bounds the
+ * equivalent per-bin queues at compile time (MaxBinSize/MaxWorkerBatch, Rasterizer.cpp:14) and
+ * flushes early when they fill; here a full queue makes the mesh stage rasterize the triangle
+ * itself, so any capacity gives the same image. Used to exercise that path in tests. */
+swr_status swr_rasterizer_set_queue_capacity(swr_rasterizer r, uint32_t triangles);
 /* perf::GetCurrent / perf::Reset (Rasterizer.h:381-395): device-side counters. */
 swr_status swr_rasterizer_get_counters(swr_rasterizer r, uint64_t out[SWR_NUM_COUNTERS]);
 swr_status swr_rasterizer_reset_counters(swr_rasterizer r);

@@ -52,7 +52,8 @@ def test_inside_volume_bit_exact(inside, binning, clipping, guardband):
                                 clipping=clipping, guardband=guardband)
         assert_visbuffer_equal(gfb, ofb)
         assert list(gc[:3]) == list(oc[:3])
-        assert oc[2] > 0  # the case really exercises non-trivial triangles
+        if binning or clipping:  # TrianglesClipped counts only then (Rasterizer.cpp:209-210, 567-568)
+            assert oc[2] > 0  # the case really exercises non-trivial triangles
 
 
 def test_crafted_triangles_bit_exact():
@@ -121,3 +122,20 @@ def test_clear_values_and_layers(grid):
         gfb, _ = g.render(v.world_to_clip, v.width, v.height, clear=clear)
         ofb, _ = render_oracle(sc.meshlets, sc.materials, v.world_to_clip, v.width, v.height, clear=clear)
         assert_visbuffer_equal(gfb, ofb)
+
+
+@pytest.mark.parametrize("capacity", [1, 64])
+def test_full_queue_gives_the_same_image(inside, capacity):
+    """With a tiny large-triangle queue the mesh stage rasterizes the overflow itself (and clipped
+    triangles fall back to per-lane rasterization); the image must not change."""
+    sc, mats, g = inside
+    v = sc.views[0]
+    view = scenes.make_view(v.width, v.height, eye=(0.0, 0.0, 0.0), target=(0.3, 0.1, 1.0))
+    g.rast.set_queue_capacity(capacity)
+    try:
+        gfb, gc = g.render(view.world_to_clip, v.width, v.height, binning=False)
+    finally:
+        g.rast.set_queue_capacity(0)
+    ofb, oc = render_oracle(sc.meshlets, mats, view.world_to_clip, v.width, v.height, binning=False)
+    assert_visbuffer_equal(gfb, ofb)
+    assert list(gc[:3]) == list(oc[:3])
