@@ -66,6 +66,9 @@ _SIGS = {
     "swr_rasterizer_set_queue_capacity": [C.c_void_p, C.c_uint32],
     "swr_rasterizer_reset_counters": [C.c_void_p],
     "swr_draw_meshlets": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p],
+    "swr_draw_meshlets_noalloc": [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p,
+                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_int, C.c_int,
+                                  C.c_int],
     "swr_framebuffer_create": [C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p],
     "swr_framebuffer_destroy": [C.c_void_p],
     "swr_framebuffer_clear": [C.c_void_p, C.c_uint32, C.c_float],

@@ -127,6 +127,24 @@ swr_status swr_rasterizer_reset_counters(swr_rasterizer r);
 swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t count, uint32_t shader_table,
                              const swr_shading_context* ctx);
 
+/* No counterpart in the reference. The vis-buffer draw of swr_draw_meshlets for callers that
+ * cannot allocate device memory (their memory belongs to another allocator, or they run where
+ * cudaMalloc is not allowed): every input and output is a caller-owned device pointer and the call
+ * allocates nothing. meshlets: Meshlet records (device); material_flags: one byte per material,
+ * bit 0 = double-sided (device, or NULL with num_materials 0); cull_bitmap as in
+ * swr_shading_context; object_to_clip: host. surface_ids and depth are the framebuffer's layers 0
+ * and 1 in the 4x4-tiled layout (width*height words each, device): they are read for the depth
+ * test and updated like the layers of a framebuffer. Limits: width*height <= 1048576 pixels and
+ * at most 1024 materials, else SWR_ECAPACITY. Working memory is one fixed device array (about
+ * 9.3 MiB, held by every GPU that loads the library until the process exits), shared by every
+ * call: calls whose work overlaps on the GPU race, so serialise them (one stream). The first call
+ * on each device looks up that array's device address; make it before any stream capture. */
+swr_status swr_draw_meshlets_noalloc(const void* meshlets, uint32_t meshlet_offset, uint32_t count,
+                                     const uint8_t* material_flags, uint32_t num_materials,
+                                     const uint16_t* cull_bitmap, const float object_to_clip[16],
+                                     uint32_t* surface_ids, float* depth, uint32_t width, uint32_t height,
+                                     int enable_binning, int enable_clipping, int enable_guardband);
+
 /* ---- Framebuffer (Rasterizer.h:10-78, ImageHelpers.cpp:109-147) ---- */
 /* CreateFramebuffer(width, height, numLayers): width/height multiples of 4, at most 2896. */
 swr_status swr_framebuffer_create(uint32_t width, uint32_t height, uint32_t num_layers, swr_framebuffer* out);
