@@ -455,15 +455,4 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
     return SWR_OK;
 }
 
-swr_status swr_cull_meshlets(swr_scene, uint32_t, uint32_t, uint16_t*, const float*, const float*, const float*,
-                             const float*, float, float, swr_texture, uint32_t*) {
-    return fail(SWR_EINVAL, "swr_cull_meshlets: not built yet");
-}
-swr_status swr_downsample_depth(swr_framebuffer, swr_texture) {
-    return fail(SWR_EINVAL, "swr_downsample_depth: not built yet");
-}
-swr_status swr_resolve(swr_rasterizer, swr_framebuffer, const swr_shading_context*) {
-    return fail(SWR_EINVAL, "swr_resolve: not built yet");
-}
-
 }  // extern "C"

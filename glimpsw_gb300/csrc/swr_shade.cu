@@ -1,0 +1,618 @@
+// Meshlet culling (ShadingContext::CullMeshlets), the Hi-Z depth pyramid (texutil::DownsampleDepth)
+// and the vis-buffer resolve (ShadingContext::Resolve) for sm_103a.
+//
+// The translation unit is compiled with -fmad=false, so every float expression below is evaluated
+// in source order with one rounding per operation, as the reference's C++ is written; fmaf()
+// stands for the reference's explicit simd::fma. rcp14/rsqrt14 are modelled as 1/x and
+// 1/sqrtf(x) (IEEE), matching the oracle's portable model.
+//
+// Resolve layout: a half-warp shades one 4x4 tile (lane = pixel), so the reference's tile-wide
+// decisions (`any(mipLevel > 0)` filter choice, normal-map enable, light skipping, sky branch)
+// become ballots over the half-warp, evaluated over all 16 pixels like the 16 AVX-512 lanes.
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cstring>
+#include <vector>
+
+#include "../../include/swr/hostmath.h"
+#include "swr_device.cuh"
+#include "swr_internal.h"
+
+namespace swr {
+namespace {
+
+struct F3 { float x, y, z; };
+
+__device__ __forceinline__ float approx_rcp(float x) { return 1.0f / x; }
+__device__ __forceinline__ float approx_rsqrt(float x) { return 1.0f / sqrtf(x); }
+__device__ __forceinline__ float approx_sqrt(float x) { return approx_rsqrt(x) * x; }
+__device__ __forceinline__ int32_t ilog2_x86(float x) {  // simd::ilog2, NaN read as 0xFFC00000
+    uint32_t b = (x != x) ? 0xFFC00000u : __float_as_uint(x);
+    return (int32_t)(b - (127u << 23)) >> 23;
+}
+__device__ __forceinline__ float mulsign(float x, float y) {
+    return __uint_as_float(__float_as_uint(x) ^ (__float_as_uint(y) & 0x80000000u));
+}
+__device__ __forceinline__ float dot3(F3 a, F3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ F3 normalize3(F3 a) {
+    float r = approx_rsqrt(dot3(a, a));
+    return { a.x * r, a.y * r, a.z * r };
+}
+__device__ __forceinline__ float lerpf(float a, float b, float t) { return fmaf(t, b, fmaf(-t, a, a)); }
+__device__ __forceinline__ uint32_t texel_offset(int32_t x, int32_t y, int32_t stride) {
+    return (uint32_t)((y & 7) | (x << 3) | ((y & ~7) << stride));
+}
+__device__ __forceinline__ F3 xform4(const float* m, F3 p, float& w) {  // simd::mul(mat4, (p, 1))
+    F3 r = { fmaf(p.x, m[0], fmaf(p.y, m[4], fmaf(p.z, m[8], 1.0f * m[12]))),
+             fmaf(p.x, m[1], fmaf(p.y, m[5], fmaf(p.z, m[9], 1.0f * m[13]))),
+             fmaf(p.x, m[2], fmaf(p.y, m[6], fmaf(p.z, m[10], 1.0f * m[14]))) };
+    w = fmaf(p.x, m[3], fmaf(p.y, m[7], fmaf(p.z, m[11], 1.0f * m[15])));
+    return r;
+}
+
+// =========================================================================== culling
+struct CullArgs {
+    const uint8_t* meshlets;
+    uint32_t first, count;
+    uint16_t* bitmap;
+    unsigned int* visibleCount;
+    float planes[5][4];
+    float objectToPrevView[16];
+    float objectToWorldScale;
+    float projFactors[3];
+    float frameW, frameH;
+    const uint32_t* depthData;  // R32f Hi-Z storage or null
+    uint32_t mipOffsets[16];
+    uint32_t mipLevels, rowShift;
+};
+
+// ShadingContext::CullMeshlets (Shading.cpp:775-869) + ProjectSphere (264-279), one meshlet per
+// thread; a warp's ballot gives two of the reference's 16-bit masks.
+__global__ void __launch_bounds__(256) k_cull(CullArgs a) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool visible = i < a.count;
+    if (visible) {
+        const float* b = (const float*)(a.meshlets + (size_t)(a.first + i) * kMeshletSize);  // BoundCenter, BoundRadius
+        const float4 s = *(const float4*)b;
+        const F3 c = { s.x, s.y, s.z };
+        const float r = s.w;
+        for (int k = 0; k < 5; k++) {
+            float dist = fmaf(c.x, a.planes[k][0], fmaf(c.y, a.planes[k][1], c.z * a.planes[k][2])) + a.planes[k][3];
+            visible = visible && (dist > -r);
+        }
+        if (a.depthData != nullptr && visible) {
+            float vw;
+            F3 vs = xform4(a.objectToPrevView, c, vw);
+            const float rvs = r * a.objectToWorldScale;
+            // ProjectSphere
+            float cx = vs.x, cy = vs.y, cz = vs.z * -1.0f;
+            bool projMask = cz >= rvs + a.projFactors[0];
+            if (projMask) {
+                float crx = cx * rvs, cry = cy * rvs, crz = cz * rvs;
+                float vx = approx_sqrt(cx * cx + cz * cz - rvs * rvs);
+                float vy = approx_sqrt(cy * cy + cz * cz - rvs * rvs);
+                float sx = a.projFactors[1] * 0.5f, sy = a.projFactors[2] * 0.5f;
+                float bb0 = (vx * cx - crz) * approx_rcp(vx * cz + crx) * sx + 0.5f;
+                float bb1 = (vy * cy + crz) * approx_rcp(vy * cz - cry) * sy + 0.5f;
+                float bb2 = (vx * cx + crz) * approx_rcp(vx * cz - crx) * sx + 0.5f;
+                float bb3 = (vy * cy - crz) * approx_rcp(vy * cz + cry) * sy + 0.5f;
+                float bw = (bb2 - bb0) * a.frameW, bh = (bb3 - bb1) * a.frameH;
+                int32_t mip = ilog2_x86(vmax(bw, bh));
+                mip = min(max(mip, 1), (int32_t)a.mipLevels - 1);
+                int32_t x0 = max(trunc2i(bb0 * a.frameW), 0) >> mip;
+                int32_t y0 = max(trunc2i(bb1 * a.frameH), 0) >> mip;
+                int32_t x1 = min(trunc2i(bb2 * a.frameW), (int32_t)a.frameW - 1) >> mip;
+                int32_t y1 = min(trunc2i(bb3 * a.frameH), (int32_t)a.frameH - 1) >> mip;
+                float depthSphere = a.projFactors[0] / (-vs.z - rvs);
+                float depthVisible = FLT_MAX;
+                const uint32_t level = (uint32_t)(mip - 1);
+                const int32_t stride = (int32_t)a.rowShift - (int32_t)level;
+                const uint32_t* base = a.depthData + a.mipOffsets[level & 15];
+                for (int32_t y = y0; y <= y1; y++)
+                    for (int32_t x = x0; x <= x1; x++)
+                        depthVisible = vmin(depthVisible, __uint_as_float(base[texel_offset(x, y, stride)]));
+                visible = depthSphere > depthVisible;
+            }
+        }
+    }
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, visible);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t w0 = i & ~31u;
+    if (lane == 0 && w0 < a.count) {
+        a.bitmap[w0 / 16] = (uint16_t)(m & 0xFFFF);
+        if (w0 + 16 < a.count) a.bitmap[w0 / 16 + 1] = (uint16_t)(m >> 16);
+        if (a.visibleCount) atomicAdd(a.visibleCount, (unsigned)__popc(m));
+    }
+}
+
+// =========================================================================== Hi-Z
+// texutil::DownsampleDepth (ImageHelpers.cpp:150-247). Mip m texels hold the min of the frame
+// depths they cover (FLT_MAX where they cover none). The reference writes mip m (m <= root-4) in
+// 8x8-texel blocks of 2^(m+4)-pixel regions whose origin lies inside the frame, and mip root-3
+// as one 4x4 tile; this kernel writes exactly those texels, level by level, reading mip m-1.
+__global__ void k_hiz_level(const float* __restrict__ depth, uint32_t fbW, uint32_t fbH, uint32_t* tex,
+                            uint32_t dstOff, uint32_t srcOff, int32_t rowShift, uint32_t m, uint32_t regionsX,
+                            uint32_t numTexels, uint32_t blockTexels) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= numTexels) return;
+    const uint32_t bs = blockTexels == 64 ? 8 : 4;
+    const uint32_t blk = t / blockTexels, within = t - blk * blockTexels;
+    const uint32_t by = blk / regionsX, bx = blk - by * regionsX;
+    const uint32_t tx = bx * bs + within % bs, ty = by * bs + within / bs;
+    float v;
+    if (m == 0) {
+        auto d = [&](uint32_t x, uint32_t y) -> float {
+            return (x < fbW && y < fbH) ? depth[pixel_offset(x, y, fbW)] : FLT_MAX;
+        };
+        uint32_t x = tx * 2, y = ty * 2;
+        v = vmin(vmin(d(x, y), d(x, y + 1)), vmin(d(x + 1, y), d(x + 1, y + 1)));
+    } else {
+        // children at mip m-1 cover 2^m pixels; one whose origin is outside the frame covers none
+        const int32_t sstride = rowShift - (int32_t)(m - 1);
+        auto c = [&](uint32_t x, uint32_t y) -> float {
+            if ((x << m) >= fbW || (y << m) >= fbH) return FLT_MAX;
+            return __uint_as_float(tex[srcOff + texel_offset(x, y, sstride)]);
+        };
+        uint32_t x = tx * 2, y = ty * 2;
+        v = vmin(vmin(c(x, y), c(x, y + 1)), vmin(c(x + 1, y), c(x + 1, y + 1)));
+    }
+    tex[dstOff + texel_offset(tx, ty, rowShift - (int32_t)m)] = __float_as_uint(v);
+}
+
+// =========================================================================== resolve
+struct ResolveArgs {
+    const uint8_t* meshlets;
+    uint32_t numMeshlets;
+    const DevMaterial* materials;
+    uint32_t numMaterials;
+    uint32_t* color;        // layer 0 (surface ids in, RGBA8 out)
+    const float* depth;     // layer 1
+    uint32_t width, height;
+    float objectToClip[16];
+    float objectToWorld[9];
+    float invProj[16];
+    float viewPos[3];
+    float exposure;
+    const swr_light* lights;  // device copy
+    uint32_t numLights;
+    DevTexture sky;
+    int hasSky;
+};
+
+__device__ __forceinline__ uint32_t lerp16(uint32_t a, uint32_t b, uint32_t t) {
+    uint32_t r = 0;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        int32_t ah = (int16_t)(a >> (16 * h)), bh = (int16_t)(b >> (16 * h)), th = (int16_t)(t >> (16 * h));
+        int32_t d = (int16_t)(bh - ah);
+        int32_t mm = (int16_t)((d * th + 0x4000) >> 15);
+        r |= (uint32_t)(uint16_t)(ah + mm) << (16 * h);
+    }
+    return r;
+}
+__device__ __forceinline__ uint32_t sat_u8(int32_t v) { return (uint32_t)min(max(min(max(v, -32768), 32767), 0), 255); }
+__device__ __forceinline__ float unpack_f11(uint32_t x) { x <<= 17; return __uint_as_float((x & 0x0FFE0000u) + 0x38000000u); }
+__device__ __forceinline__ float unpack_f10(uint32_t x) { x <<= 18; return __uint_as_float((x & 0x0FFC0000u) + 0x38000000u); }
+__device__ __forceinline__ F3 unpack_r11(uint32_t p) { return { unpack_f11(p >> 21), unpack_f11(p >> 10), unpack_f10(p) }; }
+__device__ __forceinline__ float h2f(uint32_t h) { return __half2float(__ushort_as_half((unsigned short)h)); }
+__device__ __forceinline__ F3 unmap_oct(float u, float v) {
+    u = u * 2.0f - 1.0f, v = v * 2.0f - 1.0f;
+    F3 n = { u, v, 1.0f - fabsf(u) - fabsf(v) };
+    float t = vmax(-n.z, 0.0f);
+    n.x -= mulsign(t, n.x);
+    n.y -= mulsign(t, n.y);
+    return normalize3(n);
+}
+
+// SampleLevel<SurfaceSampler> for one lane once the tile's filter is known (Texture.h:412-459).
+__device__ uint32_t sample_rgba8(const DevTexture& t, float u, float v, int layer, int32_t mipIn, bool nearest) {
+    int32_t ix = round2i(u * t.scale_lerp_u) & t.mask_lerp_u;
+    int32_t iy = round2i(v * t.scale_lerp_v) & t.mask_lerp_v;
+    int32_t m = min(max(mipIn, 0), (int32_t)t.mip_levels - 1);
+    int32_t stride = (int32_t)t.row_shift - m;
+    ix >>= m, iy >>= m;
+    const uint32_t* base = t.data + (size_t)layer * t.layer_stride + t.mip_offsets[m & 15];
+    if (nearest) return base[texel_offset(ix >> 8, iy >> 8, stride)];
+    int32_t xf = max(ix - 127, 0), yf = max(iy - 127, 0);
+    int32_t tx = xf >> 8, ty = yf >> 8;
+    bool inX = ((tx + 1) << m) < (int32_t)t.width, inY = ((ty + 1) << m) < (int32_t)t.height;
+    uint32_t i00 = texel_offset(tx, ty, stride), i01 = texel_offset(tx, ty + (inY ? 1 : 0), stride);
+    uint32_t d00 = base[i00], d10 = base[i00 + 8], d01 = base[i01], d11 = base[i01 + 8];
+    uint32_t fx = (uint32_t)(xf & 255) << 7, fy = (uint32_t)(yf & 255) << 7;
+    fx = (fx << 16) | fx, fy = (fy << 16) | fy;
+    if (!inX) fx = 0;
+    uint32_t rb1 = lerp16(d00 & 0x00FF00FF, d10 & 0x00FF00FF, fx), ga1 = lerp16((d00 >> 8) & 0x00FF00FF, (d10 >> 8) & 0x00FF00FF, fx);
+    uint32_t rb2 = lerp16(d01 & 0x00FF00FF, d11 & 0x00FF00FF, fx), ga2 = lerp16((d01 >> 8) & 0x00FF00FF, (d11 >> 8) & 0x00FF00FF, fx);
+    return lerp16(rb1, rb2, fy) | (lerp16(ga1, ga2, fy) << 8);
+}
+
+// SampleOctLevel<EnvSampler>(dir, 1) on an R11G11B10 map (Texture.h:467-480; level 1 has no fraction).
+__device__ F3 sample_env(const DevTexture& t, F3 dir) {
+    float w = approx_rcp(fabsf(dir.x) + fabsf(dir.y) + fabsf(dir.z));
+    float tt = vmax(-dir.z * w, 0.0f);
+    float u = fmaf(dir.x, w, mulsign(tt, dir.x)) * 0.5f + 0.5f;
+    float v = fmaf(dir.y, w, mulsign(tt, dir.y)) * 0.5f + 0.5f;
+    int32_t m = min(max(1, 0), (int32_t)t.mip_levels - 1);
+    int32_t x = min(max(round2i(u * t.scale_lerp_u), 0), t.mask_lerp_u);
+    int32_t y = min(max(round2i(v * t.scale_lerp_v), 0), t.mask_lerp_v);
+    int32_t stride = (int32_t)t.row_shift - m;
+    x >>= m, y >>= m;
+    const uint32_t* base = t.data + t.mip_offsets[m & 15];
+    int32_t xf = max(x - 127, 0), yf = max(y - 127, 0);
+    int32_t tx = xf >> 8, ty = yf >> 8;
+    bool inX = ((tx + 1) << m) < (int32_t)t.width, inY = ((ty + 1) << m) < (int32_t)t.height;
+    uint32_t i00 = texel_offset(tx, ty, stride), i01 = texel_offset(tx, ty + (inY ? 1 : 0), stride);
+    F3 c00 = unpack_r11(base[i00]), c10 = unpack_r11(base[i00 + 8]), c01 = unpack_r11(base[i01]), c11 = unpack_r11(base[i01 + 8]);
+    const float fs = 1.0f / 256;
+    float fx = (float)(xf & 255) * fs, fy = (float)(yf & 255) * fs;
+    if (!inX) fx = 0;
+    F3 ra = { c00.x + (c10.x - c00.x) * fx, c00.y + (c10.y - c00.y) * fx, c00.z + (c10.z - c00.z) * fx };
+    F3 rb = { c01.x + (c11.x - c01.x) * fx, c01.y + (c11.y - c01.y) * fx, c01.z + (c11.z - c01.z) * fx };
+    return { ra.x + (rb.x - ra.x) * fy, ra.y + (rb.y - ra.y) * fy, ra.z + (rb.z - ra.z) * fy };
+}
+
+__global__ void __launch_bounds__(256) k_resolve(ResolveArgs a) {
+    const uint32_t lane = threadIdx.x & 31, l = lane & 15, half = lane >> 4;
+    const unsigned hm = 0xFFFFu << (16 * half);
+    const uint32_t tilesX = a.width >> 2, numTiles = tilesX * (a.height >> 2);
+    const uint32_t tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 4;
+    if (tile >= numTiles) return;  // whole half-warps leave together
+    const uint32_t ty = tile / tilesX, tx = tile - ty * tilesX;
+    const uint32_t x0 = tx * 4, y0 = ty * 4;
+    const uint32_t px = x0 + (l & 3), py = y0 + (l >> 2);
+    const uint32_t off = pixel_offset(x0, y0, a.width) + l;
+
+    const uint32_t id = a.color[off];
+    const float d = a.depth[off];
+    const bool isSky = d <= 0.0f;
+    const float fpx = (float)(int32_t)px, fpy = (float)(int32_t)py;
+    float qw;
+    F3 q = xform4(a.invProj, { fpx, fpy, isSky ? 1.0f : d }, qw);
+    const float rw = 1.0f / qw;
+    const F3 world = { q.x * rw, q.y * rw, q.z * rw };
+    const float W = (float)a.width, H = (float)a.height;
+    const float scaleU = 2.0f / W, scaleV = 2.0f / H;
+    const float su = fpx * scaleU + (0.5f * scaleU - 1.0f), sv = fpy * scaleV + (0.5f * scaleV - 1.0f);
+    const unsigned skyBits = (__ballot_sync(hm, isSky) >> (16 * half)) & 0xFFFF;
+
+    F3 color = { 0.f, 0.f, 0.f };
+    if (skyBits != 0xFFFF) {
+        // ---- ResolveSurface (Shading.cpp:471-579): waterfall over the tile's surface ids
+        F3 pos[3] = {};
+        uint32_t tc[3] = {}, ntg[3] = {}, hand = 0, matId = 0;
+        unsigned pending = (~skyBits) & 0xFFFF;
+        while (pending) {
+            const int src = __ffs(pending) - 1;
+            const uint32_t sid = __shfl_sync(hm, id, src + 16 * half);
+            const unsigned iter = (__ballot_sync(hm, id == sid) >> (16 * half)) & 0xFFFF;
+            pending &= ~iter;
+            const uint32_t mId = sid / 128, tri = sid % 128;
+            if (((iter >> l) & 1) && mId < a.numMeshlets) {
+                const uint8_t* mp = a.meshlets + (size_t)mId * kMeshletSize;
+                const float* P = (const float*)(mp + kOffPositions);
+                const uint32_t* TC = (const uint32_t*)(mp + kOffTexCoords);
+                const uint32_t* NT = (const uint32_t*)(mp + kOffNormalTangents);
+                const uint8_t* I = mp + kOffIndices;
+                const unsigned long long handBits = *(const unsigned long long*)(mp + kOffHandedness);
+#pragma unroll
+                for (int vi = 0; vi < 3; vi++) {
+                    const uint32_t idx = I[vi * 128 + tri] & 63;
+                    pos[vi] = { P[idx], P[64 + idx], P[128 + idx] };
+                    tc[vi] = TC[idx];
+                    ntg[vi] = NT[idx];
+                    if (vi == 0 && ((handBits >> idx) & 1)) hand = 1u << 31;
+                }
+                matId = *(const uint32_t*)(mp + kOffMaterialId);
+            }
+        }
+        // IntersectTriangle (Shading.cpp:417-464)
+        float w0, w1, w2;
+        F3 c0 = xform4(a.objectToClip, pos[0], w0), c1 = xform4(a.objectToClip, pos[1], w1), c2 = xform4(a.objectToClip, pos[2], w2);
+        const float iw0 = 1.0f / w0, iw1 = 1.0f / w1, iw2 = 1.0f / w2;
+        const float p0x = c0.x * iw0, p0y = c0.y * iw0, p1x = c1.x * iw1, p1y = c1.y * iw1, p2x = c2.x * iw2, p2y = c2.y * iw2;
+        const float m0x = p2x - p1x, m0y = p2y - p1y, m1x = p0x - p1x, m1y = p0y - p1y;
+        const float invDet = 1.0f / (m0x * m1y - m1x * m0y);
+        const float s0 = invDet * iw0, s1 = invDet * iw1, s2 = invDet * iw2;
+        float dx[3] = { (p1y - p2y) * s0, (p2y - p0y) * s1, (p0y - p1y) * s2 };
+        float dy[3] = { (p2x - p1x) * s0, (p0x - p2x) * s1, (p1x - p0x) * s2 };
+        float dxs = dx[0] + dx[1] + dx[2], dys = dy[0] + dy[1] + dy[2];
+        const float r0x = su - p0x, r0y = sv - p0y;
+        const float interpInvW = iw0 + r0x * dxs + r0y * dys;
+        const float interpW = 1.0f / interpInvW;
+        float b[3];
+        b[1] = interpW * (r0x * dx[1] + r0y * dy[1]);
+        b[2] = interpW * (r0x * dx[2] + r0y * dy[2]);
+        b[0] = 1 - b[1] - b[2];
+        const float kx = 2.0f / W, ky = -(2.0f / H);
+#pragma unroll
+        for (int k = 0; k < 3; k++) dx[k] *= kx, dy[k] *= ky;
+        dxs *= kx, dys *= ky;
+        const float wdx = 1.0f / (interpInvW + dxs), wdy = 1.0f / (interpInvW + dys);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            dx[k] = wdx * (b[k] * interpInvW + dx[k]) - b[k];
+            dy[k] = wdy * (b[k] * interpInvW + dy[k]) - b[k];
+        }
+        const float t0x = h2f(tc[0] & 0xFFFF), t0y = h2f(tc[0] >> 16);
+        const float t10x = h2f(tc[1] & 0xFFFF) - t0x, t10y = h2f(tc[1] >> 16) - t0y;
+        const float t20x = h2f(tc[2] & 0xFFFF) - t0x, t20y = h2f(tc[2] >> 16) - t0y;
+        const float texU = t0x + t10x * b[1] + t20x * b[2];
+        const float texV = t0y + t10y * b[1] + t20y * b[2];
+        const float g0 = t10x * dx[1] + t20x * dx[2], g1 = t10y * dx[1] + t20y * dx[2];
+        const float g2 = t10x * dy[1] + t20x * dy[2], g3 = t10y * dy[1] + t20y * dy[2];
+
+        // waterfall over materials: filter chosen over the whole tile per material
+        uint32_t albedo = 0, nmr = 0;
+        unsigned pm = (__ballot_sync(hm, !isSky && matId != 0xFFFFFFFFu) >> (16 * half)) & 0xFFFF;
+        while (pm) {
+            const int src = __ffs(pm) - 1;
+            const uint32_t mid = __shfl_sync(hm, matId, src + 16 * half);
+            const unsigned iter = (__ballot_sync(hm, matId == mid) >> (16 * half)) & 0xFFFF;
+            pm &= ~iter;
+            if (mid >= a.numMaterials || !a.materials[mid].has_texture) continue;
+            const DevTexture& tex = a.materials[mid].tex;
+            const float ssu = tex.scale_u * tex.scale_u, ssv = tex.scale_v * tex.scale_v;
+            const float ddx2 = fmaf(g0, g0, g1 * g1) * ssu, ddy2 = fmaf(g2, g2, g3 * g3) * ssv;
+            const int32_t mip = ilog2_x86(vmax(ddx2, ddy2)) >> 1;
+            const bool nearest = __ballot_sync(hm, mip > 0) & hm;
+            if ((iter >> l) & 1) {
+                albedo = sample_rgba8(tex, texU, texV, 0, mip, nearest);
+                if (tex.num_layers >= 2) nmr = sample_rgba8(tex, texU, texV, 1, mip, nearest);
+            }
+        }
+        F3 nrm[3], tan[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const uint32_t p = ntg[k];
+            const float s = 1.0f / 255;
+            nrm[k] = unmap_oct((float)(p & 255) * s, (float)((p >> 8) & 255) * s);
+            tan[k] = unmap_oct((float)((p >> 16) & 255) * s, (float)(p >> 24) * s);
+        }
+        const float* M = a.objectToWorld;
+        auto bl = [&](const F3* v) {
+            return F3{ fmaf(v[0].x, b[0], fmaf(v[1].x, b[1], v[2].x * b[2])), fmaf(v[0].y, b[0], fmaf(v[1].y, b[1], v[2].y * b[2])),
+                       fmaf(v[0].z, b[0], fmaf(v[1].z, b[1], v[2].z * b[2])) };
+        };
+        auto m3 = [&](F3 n) {
+            return F3{ fmaf(n.x, M[0], fmaf(n.y, M[3], n.z * M[6])), fmaf(n.x, M[1], fmaf(n.y, M[4], n.z * M[7])),
+                       fmaf(n.x, M[2], fmaf(n.y, M[5], n.z * M[8])) };
+        };
+        const F3 nws = normalize3(m3(bl(nrm)));
+        F3 N = nws;
+        if (__ballot_sync(hm, (nmr & 0xFFFF) != 0) & hm) {
+            const F3 tws = normalize3(m3(bl(tan)));
+            F3 bws = { fmaf(nws.y, tws.z, -nws.z * tws.y), fmaf(nws.z, tws.x, -nws.x * tws.z), fmaf(nws.x, tws.y, -nws.y * tws.x) };
+            bws = { __uint_as_float(__float_as_uint(bws.x) ^ hand), __uint_as_float(__float_as_uint(bws.y) ^ hand),
+                    __uint_as_float(__float_as_uint(bws.z) ^ hand) };
+            const float tx_ = (float)(nmr & 255) * (1.0f / 127.5f) - 1.0f;
+            const float ty_ = (float)((nmr >> 8) & 255) * (1.0f / 127.5f) - 1.0f;
+            const float tz_ = approx_sqrt(1.0f - (tx_ * tx_ + ty_ * ty_));
+            N = normalize3({ tx_ * tws.x + ty_ * bws.x + tz_ * nws.x, tx_ * tws.y + ty_ * bws.y + tz_ * nws.y,
+                             tx_ * tws.z + ty_ * bws.z + tz_ * nws.z });
+        }
+        const float metallic = (float)((nmr >> 16) & 255) * (1.0f / 255);
+        const float roughness = (float)((nmr >> 24) & 255) * (1.0f / 255);
+
+        // ---- EvalLighting (Shading.cpp:602-645)
+        const float invPi = 0.3183098861837907f;
+        uint32_t rb1 = ((albedo << 8) & 0xFF00FF00u) + 0x00FF00FFu, ag1 = (albedo & 0xFF00FF00u) + 0x00FF00FFu;
+        uint32_t rb2 = (((rb1 & 0xFFFF) * (rb1 & 0xFFFF)) >> 16) | ((((rb1 >> 16) * (rb1 >> 16)) >> 16) << 16);
+        uint32_t ag2 = (((ag1 & 0xFFFF) * (ag1 & 0xFFFF)) >> 16) | ((((ag1 >> 16) * (ag1 >> 16)) >> 16) << 16);
+        const float s65 = 1.0f / 65535;
+        const F3 base = { (float)(rb2 & 65535) * s65, (float)(ag2 & 65535) * s65, (float)(rb2 >> 16) * s65 };
+        const float alphaR = vmax(roughness * roughness, 1e-4f);
+        const float f0d = 0.16f * 0.5f * 0.5f;
+        const F3 f0 = { lerpf(f0d, base.x, metallic), lerpf(f0d, base.y, metallic), lerpf(f0d, base.z, metallic) };
+        const float dm = 1.0f - metallic;
+        const F3 diffuse = { base.x * dm, base.y * dm, base.z * dm };
+        const F3 vp = { a.viewPos[0], a.viewPos[1], a.viewPos[2] };
+        const F3 viewDir = normalize3({ vp.x - world.x, vp.y - world.y, vp.z - world.z });
+        const float NoV = fabsf(dot3(N, viewDir)) + 1e-5f;
+        const float exposure = a.exposure * 0.001f;
+        for (uint32_t i = 0; i < a.numLights; i++) {
+            const swr_light& li = a.lights[i];
+            F3 ld = li.type == 0 ? F3{ -li.direction[0], -li.direction[1], -li.direction[2] }
+                                 : normalize3({ li.position[0] - world.x, li.position[1] - world.y, li.position[2] - world.z });
+            const float NoL = dot3(N, ld);
+            if ((__ballot_sync(hm, NoL < 1e-4f) & hm) == hm) continue;
+            float att = 1.0f;
+            if (li.type != 0) {
+                const F3 p2l = { li.position[0] - world.x, li.position[1] - world.y, li.position[2] - world.z };
+                const float d2 = dot3(p2l, p2l);
+                const float f = d2 * li.inv_radius_sq;
+                const float sm = vmax(1.0f - f * f, 0.0f);
+                att = (sm * sm) * approx_rcp(vmax(d2, 1e-4f));
+                if (li.type == 2) {
+                    const float cd = dot3({ -li.direction[0], -li.direction[1], -li.direction[2] }, normalize3(p2l));
+                    const float sa = vmin(vmax(cd * li.spot_scale + li.spot_offset, 0.0f), 1.0f);
+                    att *= sa * sa;
+                }
+            }
+            att = att * li.intensity * exposure;
+            if ((__ballot_sync(hm, NoL * att < 1e-4f) & hm) == hm) continue;
+            const F3 h = normalize3({ viewDir.x + ld.x, viewDir.y + ld.y, viewDir.z + ld.z });
+            const float NoH = vmin(vmax(dot3(N, h), 0.0f), 1.0f);
+            const float LoH = vmin(vmax(dot3(ld, h), 0.0f), 1.0f);
+            const float aa = NoH * alphaR;
+            const float k = alphaR * approx_rcp(1.0f - NoH * NoH + aa * aa);
+            const float D = k * k * invPi;
+            const float V = 0.5f / lerpf(2.0f * NoL * NoV, NoL + NoV, alphaR);
+            const float x = 1.0f - LoH;
+            const float f = (x * x) * (x * x) * x;
+            const F3 F = { f + f0.x * (1.0f - f), f + f0.y * (1.0f - f), f + f0.z * (1.0f - f) };
+            const float DV = D * V;
+            const float wgt = vmax(NoL * att, 0.0f);
+            color.x += (diffuse.x * invPi + DV * F.x) * li.color[0] * wgt;
+            color.y += (diffuse.y * invPi + DV * F.y) * li.color[1] * wgt;
+            color.z += (diffuse.z * invPi + DV * F.z) * li.color[2] * wgt;
+        }
+        color.x += base.x * 0.05f;
+        color.y += base.y * 0.05f;
+        color.z += base.z * 0.05f;
+    }
+    if (skyBits != 0 && a.hasSky && isSky) color = sample_env(a.sky, { world.x - a.viewPos[0], world.y - a.viewPos[1], world.z - a.viewPos[2] });
+    // Tonemap_Unreal (Shading.cpp:221-226) + RGBA8u::Pack
+    const float e = a.exposure;
+    const F3 c = { color.x * e, color.y * e, color.z * e };
+    const uint32_t r = sat_u8(round2i(c.x / (c.x + 0.155f) * 1.019f * 255.0f));
+    const uint32_t g = sat_u8(round2i(c.y / (c.y + 0.155f) * 1.019f * 255.0f));
+    const uint32_t bch = sat_u8(round2i(c.z / (c.z + 0.155f) * 1.019f * 255.0f));
+    a.color[off] = r | (g << 8) | (bch << 16) | (255u << 24);
+}
+
+}  // namespace
+}  // namespace swr
+
+using namespace swr;
+
+extern "C" {
+
+swr_status swr_cull_meshlets(swr_scene s, uint32_t first, uint32_t count, uint16_t* bitmap_device, const float proj[16],
+                             const float view[16], const float model[16], const float prev_view[16], float frame_width,
+                             float frame_height, swr_texture depth_map, uint32_t* visible_count) {
+    if (!s || !bitmap_device || !proj || !view || !model || !prev_view)
+        return swr_internal_fail(SWR_EINVAL, "swr_cull_meshlets: NULL argument");
+    if ((uint64_t)first + count > s->count) return swr_internal_fail(SWR_EINVAL, "swr_cull_meshlets: range outside the scene");
+    if (depth_map && depth_map->format != SWR_FORMAT_R32F)
+        return swr_internal_fail(SWR_EINVAL, "swr_cull_meshlets: the depth map must be R32f");
+    if (!(frame_width >= 1.0f && frame_width <= 65536.0f && frame_height >= 1.0f && frame_height <= 65536.0f))
+        return swr_internal_fail(SWR_EINVAL, "swr_cull_meshlets: frame size outside [1, 65536]");
+    // Texel reads stay inside the map when it is at least half the frame in each dimension (the
+    // frame driver's sizing, Main.cpp:54-56) and has two levels (mip clamps to [1, levels-1]).
+    if (depth_map && ((float)(depth_map->d.width * 2) < frame_width || (float)(depth_map->d.height * 2) < frame_height ||
+                      depth_map->d.mip_levels < 2))
+        return swr_internal_fail(SWR_EINVAL, "swr_cull_meshlets: depth map smaller than half the frame or without mips");
+    cudaStream_t st = swr_internal_stream();
+    CullArgs a = {};
+    a.meshlets = s->meshlets;
+    a.first = first, a.count = count;
+    a.bitmap = bitmap_device;
+    float objToPrev[16], pv[16], objToClip[16], planes[6][4];
+    swr_hostmath::mat4_mul(prev_view, model, objToPrev);
+    swr_hostmath::mat4_mul(proj, view, pv);
+    swr_hostmath::mat4_mul(pv, model, objToClip);
+    swr_hostmath::frustum_planes(objToClip, planes);
+    memcpy(a.planes, planes, sizeof(a.planes));  // planes 0..4 (the reference skips the last, Shading.cpp:806)
+    memcpy(a.objectToPrevView, objToPrev, sizeof(objToPrev));
+    a.objectToWorldScale = swr_hostmath::column0_length(model);
+    a.projFactors[0] = proj[3 * 4 + 2], a.projFactors[1] = proj[0], a.projFactors[2] = proj[1 * 4 + 1];
+    a.frameW = frame_width, a.frameH = frame_height;
+    if (depth_map) {
+        a.depthData = depth_map->d.data;
+        memcpy(a.mipOffsets, depth_map->d.mip_offsets, sizeof(a.mipOffsets));
+        a.mipLevels = depth_map->d.mip_levels;
+        a.rowShift = depth_map->d.row_shift;
+    }
+    unsigned int* cnt = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (visible_count) {
+        e = cudaMallocAsync(&cnt, sizeof(unsigned int), st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, sizeof(unsigned int), st);
+        if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_cull_meshlets");
+        a.visibleCount = cnt;
+    }
+    if (count) {
+        LaunchScope ls("k_cull", st);
+        k_cull<<<(count + 255) / 256, 256, 0, st>>>(a);
+        e = cudaGetLastError();
+    }
+    if (visible_count) {
+        unsigned int h = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&h, cnt, sizeof(h), cudaMemcpyDeviceToHost, st);
+        cudaFreeAsync(cnt, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        *visible_count = h;
+    }
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_cull_meshlets");
+    return SWR_OK;
+}
+
+swr_status swr_downsample_depth(swr_framebuffer fb, swr_texture dest) {
+    if (!fb || !dest) return swr_internal_fail(SWR_EINVAL, "swr_downsample_depth: NULL argument");
+    if (dest->format != SWR_FORMAT_R32F) return swr_internal_fail(SWR_EINVAL, "swr_downsample_depth: destination must be R32f");
+    const uint32_t root = 32 - __builtin_clz(std::max(fb->width, fb->height));
+    if (root < 4) return swr_internal_fail(SWR_EINVAL, "swr_downsample_depth: framebuffer smaller than 16 pixels");
+    cudaStream_t st = swr_internal_stream();
+    const float* depth = (const float*)(fb->layers + fb->layer_stride);
+    uint32_t* tex = (uint32_t*)dest->d.data;
+    auto blocks = [&](uint32_t m, uint32_t& rx, uint32_t& ry, uint32_t& bt) {
+        if (m + 4 <= root) {
+            const uint32_t region = 1u << (m + 4);
+            rx = (fb->width + region - 1) / region, ry = (fb->height + region - 1) / region, bt = 64;
+        } else {
+            rx = ry = 1, bt = 16;
+        }
+    };
+    // Levels the texture does not have use MipOffsets[m] = 0, as the reference's zero-filled table
+    // does (for non-square frames its root tile lands at the start of mip 0). Every written texel
+    // must fall inside the texture's storage.
+    auto mipOff = [&](uint32_t m) { return m < dest->d.mip_levels ? dest->d.mip_offsets[m] : 0u; };
+    for (uint32_t m = 0; m + 3 <= root; m++) {
+        uint32_t rx, ry, bt;
+        blocks(m, rx, ry, bt);
+        const uint32_t side = bt == 64 ? 8 : 4;
+        const int32_t stride = (int32_t)dest->d.row_shift - (int32_t)m;
+        const uint64_t maxX = (uint64_t)rx * side - 1, maxY = (uint64_t)ry * side - 1;
+        if (stride < 0 || mipOff(m) + 7 + (maxX << 3) + (maxY << stride) >= dest->words)
+            return swr_internal_fail(SWR_EINVAL, "swr_downsample_depth: destination too small for this framebuffer");
+    }
+    for (uint32_t m = 0; m + 3 <= root; m++) {
+        uint32_t regionsX, regionsY, blockTexels;
+        blocks(m, regionsX, regionsY, blockTexels);
+        const uint32_t n = regionsX * regionsY * blockTexels;
+        LaunchScope ls("k_hiz_level", st);
+        k_hiz_level<<<(n + 255) / 256, 256, 0, st>>>(depth, fb->width, fb->height, tex, mipOff(m), m ? mipOff(m - 1) : 0,
+                                                      (int32_t)dest->d.row_shift, m, regionsX, n, blockTexels);
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_downsample_depth");
+    return SWR_OK;
+}
+
+swr_status swr_resolve(swr_rasterizer r, swr_framebuffer fb, const swr_shading_context* ctx) {
+    (void)r;
+    if (!fb || !ctx || !ctx->scene) return swr_internal_fail(SWR_EINVAL, "swr_resolve: NULL argument");
+    if (ctx->num_lights && !ctx->lights) return swr_internal_fail(SWR_EINVAL, "swr_resolve: lights is NULL");
+    if (ctx->skybox && ctx->skybox->format != SWR_FORMAT_R11G11B10F)
+        return swr_internal_fail(SWR_EINVAL, "swr_resolve: the skybox must be R11G11B10f");
+    cudaStream_t st = swr_internal_stream();
+    ResolveArgs a = {};
+    a.meshlets = ctx->scene->meshlets;
+    a.numMeshlets = ctx->scene->count;
+    a.materials = ctx->scene->materials;
+    a.numMaterials = ctx->scene->num_materials;
+    a.color = fb->layers;
+    a.depth = (const float*)(fb->layers + fb->layer_stride);
+    a.width = fb->width, a.height = fb->height;
+    memcpy(a.objectToClip, ctx->object_to_clip, sizeof(a.objectToClip));
+    memcpy(a.objectToWorld, ctx->object_to_world, sizeof(a.objectToWorld));
+    if (!swr_hostmath::inverse_screen_proj(ctx->world_to_clip, fb->width, fb->height, a.invProj))
+        return swr_internal_fail(SWR_EINVAL, "swr_resolve: singular world_to_clip");
+    memcpy(a.viewPos, ctx->view_pos, sizeof(a.viewPos));
+    a.exposure = ctx->exposure;
+    if (ctx->skybox) a.sky = ctx->skybox->d, a.hasSky = 1;
+    swr_light* dl = nullptr;
+    cudaError_t e = cudaSuccess;
+    if (ctx->num_lights) {
+        e = cudaMallocAsync(&dl, ctx->num_lights * sizeof(swr_light), st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dl, ctx->lights, ctx->num_lights * sizeof(swr_light), cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_resolve: lights");
+    }
+    a.lights = dl;
+    a.numLights = ctx->num_lights;
+    const uint32_t tiles = (fb->width / 4) * (fb->height / 4);
+    {
+        LaunchScope ls("k_resolve", st);
+        k_resolve<<<(tiles * 16 + 255) / 256, 256, 0, st>>>(a);
+        e = cudaGetLastError();
+    }
+    if (dl) cudaFreeAsync(dl, st);
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_resolve");
+    fb->keys_valid = false;  // layer 0 now holds colour; a later draw rebuilds its keys from depth
+    return SWR_OK;
+}
+
+}  // extern "C"

@@ -48,7 +48,8 @@ class OrcShadingContext(C.Structure):
                 ("lights", C.c_void_p), ("num_lights", C.c_uint32), ("meshlet_offset", C.c_uint32),
                 ("cull_bitmap", C.c_void_p), ("world_to_clip", C.c_float * 16),
                 ("object_to_clip", C.c_float * 16), ("object_to_world", C.c_float * 9),
-                ("skybox", C.c_void_p), ("view_pos", C.c_float * 3), ("exposure", C.c_float)]
+                ("skybox", C.c_void_p), ("view_pos", C.c_float * 3), ("exposure", C.c_float),
+                ("num_meshlets", C.c_uint32)]
 
 
 class OrcRasterFlags(C.Structure):
@@ -157,6 +158,7 @@ class Context:
         s.skybox = C.cast(C.byref(skybox.s), C.c_void_p) if skybox is not None else None
         s.view_pos = (C.c_float * 3)(*[float(v) for v in view_pos])
         s.exposure = exposure
+        s.num_meshlets = len(meshlets)
         self.s = s
 
 

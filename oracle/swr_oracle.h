@@ -70,6 +70,7 @@ typedef struct {
     const orc_texture* skybox;      // R11G11B10 octahedral map or NULL
     float view_pos[3];
     float exposure;
+    uint32_t num_meshlets;          // size of the meshlet pool (bounds surface ids in the resolve)
 } orc_shading_context;
 
 // Rasterizer flags (Rasterizer.h:205-208).

@@ -66,6 +66,13 @@ static inline int32_t ilog2(float x) {
 static inline uint32_t f2u(float f) { uint32_t u; memcpy(&u, &f, 4); return u; }
 static inline float u2f(uint32_t u) { float f; memcpy(&f, &u, 4); return f; }
 
+// simd::ilog2 where a NaN reads as the x86 default NaN 0xFFC00000: every NaN on these paths comes
+// from an invalid operation, which the reference's x86 host answers with that pattern.
+static inline int32_t ilog2_x86(float x) {
+    if (x != x) x = u2f(0xFFC00000u);
+    return ilog2(x);
+}
+
 // AVX-512 rcp14/rsqrt14 (SIMD.h:294-296) or their correctly rounded model.
 float approx_rcp(float x);
 float approx_rsqrt(float x);

@@ -272,7 +272,7 @@ uint32_t orc_cull_meshlets(uint16_t* bitmap, const void* meshlets, uint32_t coun
                 bool projMask = project_sphere(vs.x, vs.y, vs.z, rvs, projFactors, bb);
                 if (projMask) {
                     float bw = (bb[2] - bb[0]) * frame_w, bh = (bb[3] - bb[1]) * frame_h;
-                    int32_t mip = ilog2(vmax(bw, bh));
+                    int32_t mip = ilog2_x86(vmax(bw, bh));
                     mip = std::min(std::max(mip, 1), (int32_t)depth_map->mip_levels - 1);
                     int32_t x0 = std::max(trunc2i(bb[0] * frame_w), 0) >> mip;
                     int32_t y0 = std::max(trunc2i(bb[1] * frame_h), 0) >> mip;

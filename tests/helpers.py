@@ -76,6 +76,56 @@ class GpuRenderer:
         return c.value
 
 
+LIGHT_DTYPE = np.dtype([("type", "<u4"), ("position", "<f4", 3), ("direction", "<f4", 3), ("color", "<f4", 3),
+                        ("intensity", "<f4"), ("radius", "<f4"), ("spot_inner", "<f4"), ("spot_outer", "<f4"),
+                        ("inv_radius_sq", "<f4"), ("spot_scale", "<f4"), ("spot_offset", "<f4")])
+
+
+def default_lights() -> np.ndarray:
+    """The frame driver's fallback light (Main.cpp:192-201): directional, colour 1, 1500 lux."""
+    lights = np.zeros(1, dtype=LIGHT_DTYPE)
+    d = -np.array([0.589494, 0.684509, 0.428906], dtype=np.float32)
+    d = (d * np.float32(1.0 / np.sqrt(np.float64((d * d).sum())))).astype(np.float32)
+    lights["direction"] = d
+    lights["color"] = 1.0
+    lights["intensity"] = 1500.0
+    return lights
+
+
+def gpu_lights(lights: np.ndarray):
+    from glimpsw_gb300 import api
+    out = []
+    for li in lights:
+        s = api.SwrLight()
+        s.type = int(li["type"])
+        s.position[:] = li["position"].tolist()
+        s.direction[:] = li["direction"].tolist()
+        s.color[:] = li["color"].tolist()
+        s.intensity, s.radius = float(li["intensity"]), float(li["radius"])
+        s.spot_inner_angle, s.spot_outer_angle = float(li["spot_inner"]), float(li["spot_outer"])
+        s.inv_radius_sq, s.spot_scale, s.spot_offset = float(li["inv_radius_sq"]), float(li["spot_scale"]), float(li["spot_offset"])
+        out.append(s)
+    return out
+
+
+class TexturePair:
+    """The same texels in an oracle texture and a device texture (mips generated on each side)."""
+
+    def __init__(self, layers, size, fmt=0, max_levels=16, gpu=True):
+        from oracle import oracle as O
+        self.o = O.Texture(size, size, max_levels, len(layers), fmt=fmt)
+        for i, px in enumerate(layers):
+            self.o.set_pixels(px, i)
+        self.o.generate_mips()
+        self.g = None
+        if gpu:
+            from glimpsw_gb300 import api
+            self.g = api.Texture2D(fmt, size, size, max_levels, len(layers))
+            for i, px in enumerate(layers):
+                self.g.set_pixels(px, i)
+            self.g.generate_mips()
+
+
 def assert_visbuffer_equal(gpu_fb, orc_fb):
     g_ids, o_ids = gpu_fb.get_pixels(0), orc_fb.get_pixels(0)
     g_d, o_d = gpu_fb.get_pixels(1), orc_fb.get_pixels(1)
