@@ -2,22 +2,24 @@
 """Benchmark of the GB300 meshlet raster pipeline on the reference's large plain-path scene.
 
 Workload (the headline configuration): 100k meshlets of 64 vertices / 124 triangles (12.4M
-triangles), seeded, scattered in a 200^3 volume with log-uniform scale 0.1-10, 64 materials,
-rendered at 1920x1080 by one camera, unbinned rasterizer semantics (clipping on), as the
-reference's frame driver does (Main.cpp:97-305): clear, meshlet culling, draw in 65536-meshlet
-batches, and the stages of the frame that are available in this build.
+triangles), seeded, scattered in a 200^3 volume with log-uniform scale 0.1-10, 64 materials of two
+2048^2 RGBA8 layers with full mips, an octahedral 1024^2 R11G11B10 sky, 1920x1080. One step is one
+frame of the reference's frame driver (Main.cpp:171-261): clear, per 65536-meshlet batch
+CullMeshlets (frustum + Hi-Z of the previous view) then DrawMeshlets (unbinned semantics, clipping
+on), Resolve, and DownsampleDepth for the next frame. The camera of the timed frame is the
+perturbed second view; its Hi-Z input is built from the first view before timing (ping-pong
+textures keep every timed frame identical).
 
-One "step" = one frame. Timed on the device with CUDA events on the library's stream (set to
-torch's current stream); L2 is flushed between timed steps by a 256 MiB write outside the step's
-events. `e2e` measures the same frame through the public API with the scene uploaded from pinned
-host memory and the id layer read back to host memory inside the timed region.
-
-`--impl reference` times the reference's CPU algorithm (the oracle restatement; the reference
-itself cannot be compiled here) on the host cores for the same workload.
+Timing: CUDA events on the library's stream (torch's current stream), L2 flushed between timed
+steps by a 256 MiB write outside the step's events. `e2e` runs the same frame through the public
+API with the scene uploaded from pinned host memory and the colour image read back to host memory
+inside the timed region. `--impl reference` times the reference's CPU algorithm (the oracle
+restatement; the reference itself cannot be compiled here) on the host cores.
 """
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import subprocess
@@ -30,7 +32,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "1080p frame time (100k meshlets, 12.4M triangles)"
+METRIC = "1080p frame time (100k meshlets, 12.4M triangles, cull+draw+resolve+Hi-Z)"
 UNIT = "ms/frame"
 BATCH = 65536  # Main.cpp:222
 
@@ -44,35 +46,115 @@ def parse():
     p.add_argument("--meshlets", type=int, default=100_000)
     p.add_argument("--width", type=int, default=1920)
     p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--texture-size", type=int, default=2048)
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
 def build_scene(args):
     from glimpsw_gb300 import scenes
-    return scenes.volume_scene(n=args.meshlets, width=args.width, height=args.height, texture_size=2048)
+    return scenes.volume_scene(n=args.meshlets, width=args.width, height=args.height, texture_size=args.texture_size)
+
+
+def default_lights():
+    d = -np.array([0.589494, 0.684509, 0.428906], dtype=np.float32)
+    d = (d * np.float32(1.0 / np.sqrt(np.float64((d * d).sum())))).astype(np.float32)
+    return d
 
 
 def config_dict(args, sc, extra=None):
-    d = {"workload": f"volume scene: {args.meshlets} meshlets x 124 tris @ {args.width}x{args.height}, "
-                     f"unbinned (clipping on), 1 view",
-         "meshlets": args.meshlets, "triangles": int(args.meshlets * 124), "width": args.width,
-         "height": args.height, "materials": int(len(sc.materials)),
+    d = {"workload": f"volume scene: {args.meshlets} meshlets x 124 tris, {len(sc.materials)} materials x 2 layers "
+                     f"{args.texture_size}^2 RGBA8, {args.width}x{args.height}, full frame (cull with Hi-Z, draw "
+                     f"unbinned, resolve, Hi-Z build)",
+         "meshlets": args.meshlets, "triangles": int(args.meshlets * 124), "width": args.width, "height": args.height,
+         "materials": int(len(sc.materials)), "texture_size": args.texture_size,
          "l2": "flushed between timed steps (256 MiB write outside the step events)"}
     if extra:
         d.update(extra)
     return d
 
 
-# ----------------------------------------------------------------------------- CPU baseline
+# ----------------------------------------------------------------------------- textures
+def make_gpu_textures(sc, api):
+    """Seeded value-noise materials generated on the device (identical to scenes.value_noise_rgba)."""
+    import torch
+
+    from glimpsw_gb300 import scenes
+    texs = []
+    for i in range(len(sc.materials)):
+        t = api.Texture2D(api.FORMAT_RGBA8U, sc.texture_size, sc.texture_size, 16, 2)
+        for layer in range(2):
+            px = scenes.value_noise_rgba_torch(sc.texture_size, sc.texture_seed + i, layer=layer)
+            t.set_pixels_device(px, layer)
+            torch.cuda.synchronize()
+        t.generate_mips()
+        texs.append(t)
+    env = api.Texture2D(api.FORMAT_R11G11B10F, sc.env_size, sc.env_size, 16, 1)
+    env.set_pixels(scenes.env_map_r11g11b10(sc.env_size, sc.texture_seed + 999))
+    env.generate_mips()
+    return texs, env
+
+
+# ----------------------------------------------------------------------------- CPU frame
+class OracleFrame:
+    """The same frame on the CPU oracle (test infrastructure, used here only as the timed baseline)."""
+
+    def __init__(self, sc, tex_data, env_data, threads):
+        from oracle import oracle as O
+        from glimpsw_gb300 import scenes
+        self.O, self.sc, self.threads = O, sc, threads
+        v0, v1 = sc.views
+        self.v0, self.v1 = v0, v1
+        self.texs = []
+        for data in tex_data:
+            t = O.Texture(sc.texture_size, sc.texture_size, 16, 2)
+            t.data[:] = data[: t.data.size]
+            self.texs.append(t)
+        self.env = O.Texture(sc.env_size, sc.env_size, 16, 1, fmt=1)
+        self.env.data[:] = env_data[: self.env.data.size]
+        hw, hh = O.hiz_texture_size(v0.width, v0.height)
+        self.hiz_in = O.Texture(hw, hh, 16, 1, fmt=2)
+        self.hiz_out = O.Texture(hw, hh, 16, 1, fmt=2)
+        self.fb = O.Framebuffer(v0.width, v0.height, 3)
+        lights = np.zeros(1, dtype=[("type", "<u4"), ("position", "<f4", 3), ("direction", "<f4", 3), ("color", "<f4", 3),
+                                    ("intensity", "<f4"), ("radius", "<f4"), ("si", "<f4"), ("so", "<f4"), ("irs", "<f4"),
+                                    ("ss", "<f4"), ("sof", "<f4")])
+        lights["direction"], lights["color"], lights["intensity"] = default_lights(), 1.0, 1500.0
+        self.lights = lights
+        self.model = scenes.IDENTITY
+        self.frame(v0, v0, None, self.hiz_in)  # Hi-Z of the previous view
+
+    def frame(self, view, prev, hiz_in, hiz_out):
+        O, sc = self.O, self.sc
+        n = len(sc.meshlets)
+        self.fb.clear(0xFF000000, 0.0)
+        for off in range(0, n, BATCH):
+            cnt = min(BATCH, n - off)
+            bm, _ = O.cull_meshlets(sc.meshlets[off:off + cnt], cnt, view.proj, view.view, self.model, prev.view,
+                                    view.width, view.height, hiz_in)
+            ctx = O.Context(sc.meshlets, sc.materials, view.world_to_clip, meshlet_offset=off, cull_bitmap=bm)
+            O.draw_meshlets(self.fb, ctx, cnt, binning=False, threads=self.threads)
+        ctx = O.Context(sc.meshlets, sc.materials, view.world_to_clip, world_to_clip=view.world_to_clip,
+                        textures=self.texs, lights=self.lights, skybox=self.env, view_pos=view.eye)
+        O.resolve(self.fb, ctx, threads=self.threads)
+        O.downsample_depth(self.fb, hiz_out)
+
+    def timed(self, budget_s, max_frames=50):
+        times = []
+        t_end = time.perf_counter() + budget_s
+        while True:
+            t0 = time.perf_counter()
+            self.frame(self.v1, self.v0, self.hiz_in, self.hiz_out)
+            times.append(time.perf_counter() - t0)
+            if time.perf_counter() > t_end or len(times) >= max_frames:
+                return times
+
+
 def cpu_threads():
     try:
         return len(os.sched_getaffinity(0))
@@ -80,26 +162,23 @@ def cpu_threads():
         return os.cpu_count() or 1
 
 
-def time_cpu_frames(sc, budget_s, threads):
-    """Oracle frames (draw of all meshlets, unbinned semantics) until the budget is used."""
+def oracle_textures_from_host(sc):
+    """Texel storage for the oracle without a GPU: same generator, built on the CPU."""
     from oracle import oracle as O
-    v = sc.views[0]
-    fb = O.Framebuffer(v.width, v.height)
-    ctx = O.Context(sc.meshlets, sc.materials, v.world_to_clip)
-    times = []
-    t_end = time.perf_counter() + budget_s
-    while True:
-        t0 = time.perf_counter()
-        fb.clear(0xFF000000, 0.0)
-        for off in range(0, len(sc.meshlets), BATCH):
-            n = min(BATCH, len(sc.meshlets) - off)
-            ctx2 = O.Context(sc.meshlets, sc.materials, v.world_to_clip, meshlet_offset=off)
-            O.draw_meshlets(fb, ctx2, n, binning=False, threads=threads)
-        times.append(time.perf_counter() - t0)
-        if time.perf_counter() > t_end or len(times) >= 50:
-            break
-    _ = ctx
-    return times
+    from glimpsw_gb300 import scenes
+    data = []
+    for i in range(len(sc.materials)):
+        t = O.Texture(sc.texture_size, sc.texture_size, 16, 2)
+        for layer in range(2):
+            # torch on the CPU (multi-threaded) computes the same texels as scenes.value_noise_rgba
+            px = scenes.value_noise_rgba_torch(sc.texture_size, sc.texture_seed + i, layer=layer, device="cpu")
+            t.set_pixels(px.numpy().view(np.uint32), layer)
+        t.generate_mips()
+        data.append(t.data.copy())
+    env = O.Texture(sc.env_size, sc.env_size, 16, 1, fmt=1)
+    env.set_pixels(scenes.env_map_r11g11b10(sc.env_size, sc.texture_seed + 999))
+    env.generate_mips()
+    return data, env.data.copy()
 
 
 def run_reference(args):
@@ -108,21 +187,21 @@ def run_reference(args):
         return
     sc = build_scene(args)
     threads = cpu_threads()
+    tex_data, env_data = oracle_textures_from_host(sc)
+    of = OracleFrame(sc, tex_data, env_data, threads)
+    of.timed(0.0, 1)  # warm-up frame
     times = []
-    for _ in range(max(1, args.warmup and 1)):
-        time_cpu_frames(sc, 0.0, threads)  # one warm-up frame
     for _ in range(args.steps):
-        times += time_cpu_frames(sc, 0.0, threads)
-        if sum(times) > 120:
+        times += of.timed(0.0, 1)
+        if sum(times) > 150:
             break
     ms = float(np.median(times) * 1e3)
-    line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": len(times), "warmup": 1, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+i32", "data": "synthetic (seeded)",
-            "config": config_dict(args, sc),
+    line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": args.gpus, "steps": len(times),
+            "warmup": 1, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+i32", "data": "synthetic (seeded)", "config": config_dict(args, sc),
             "cpu_baseline": {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{len(times)} full frames (median); oracle restatement of the reference's "
-                                       f"CPU rasterizer, rows split over {threads} threads"},
+                             "sample": f"{len(times)} full frames (median); oracle restatement of the reference's CPU "
+                                       f"pipeline, draw and resolve rows split over {threads} threads"},
             "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -130,10 +209,8 @@ def run_reference(args):
 # ----------------------------------------------------------------------------- clocks
 class ClockSampler:
     def __init__(self, index=0):
-        self.index = index
-        self.samples = []
-        self._stop = threading.Event()
-        self._t = None
+        self.index, self.samples = index, []
+        self._stop, self._t = threading.Event(), None
 
     def _run(self):
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -174,16 +251,15 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-# ----------------------------------------------------------------------------- GPU
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            d = json.load(f)
-        return float(d["hbm_gbs"]), "measured"
+            return float(json.load(f)["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
 
 
+# ----------------------------------------------------------------------------- GPU
 def run_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -191,38 +267,53 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
-    from glimpsw_gb300 import api
+    from glimpsw_gb300 import api, scenes
     api.load_library()
 
     sc = build_scene(args)
-    v = sc.views[0]
+    v0, v1 = sc.views
+    W, H = v0.width, v0.height
     stream = torch.cuda.current_stream()
     api.set_stream(stream.cuda_stream)
 
+    texs, env = make_gpu_textures(sc, api)
     scene = api.Scene()
     scene.upload_meshlets(sc.meshlets)
-    scene.set_materials(sc.materials)
+    scene.set_materials(sc.materials, texs)
     rast = api.Rasterizer()
     rast.EnableBinning = False  # the reference frame driver's setting (Main.cpp:76)
-    fb = api.Framebuffer(v.width, v.height, 3)
+    fb = api.Framebuffer(W, H, 3)
     n = len(sc.meshlets)
-    ctxs = [api.ShadingContext(scene, v.world_to_clip, world_to_clip=v.world_to_clip, meshlet_offset=off)
-            for off in range(0, n, BATCH)]
+    batches = [(off, min(BATCH, n - off)) for off in range(0, n, BATCH)]
+    bitmaps = [torch.zeros((cnt + 15) // 16, dtype=torch.int16, device="cuda") for _, cnt in batches]
+    from oracle.oracle import hiz_texture_size  # sizing rule of the frame driver (Main.cpp:54-56)
+    hw, hh = hiz_texture_size(W, H)
+    hiz = [api.Texture2D(api.FORMAT_R32F, hw, hh, 16, 1) for _ in range(2)]
+    model = scenes.IDENTITY
+    lights = [api.SwrLight()]
+    lights[0].type, lights[0].intensity = 0, 1500.0
+    lights[0].direction[:] = default_lights().tolist()
+    lights[0].color[:] = [1.0, 1.0, 1.0]
 
-    def frame():
+    def frame(view, prev, hiz_in, hiz_out):
         fb.clear(0xFF000000, 0.0)
-        for i, off in enumerate(range(0, n, BATCH)):
-            rast.draw_meshlets(fb, min(BATCH, n - off), ctxs[i])
+        for (off, cnt), bm in zip(batches, bitmaps):
+            api.cull_meshlets(scene, off, cnt, bm, view.proj, view.view, model, prev.view, W, H, hiz_in)
+            rast.draw_meshlets(fb, cnt, api.ShadingContext(scene, view.world_to_clip, meshlet_offset=off, cull_bitmap=bm))
+        ctx = api.ShadingContext(scene, view.world_to_clip, world_to_clip=view.world_to_clip, skybox=env,
+                                 view_pos=view.eye, lights=lights)
+        ctx.resolve(rast, fb)
+        api.downsample_depth(fb, hiz_out)
 
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    frame(v0, v0, None, hiz[0])  # Hi-Z of the previous view
     for _ in range(max(3, args.warmup)):
-        frame()
+        frame(v1, v0, hiz[0], hiz[1])
     torch.cuda.synchronize()
     rast.reset_counters()
-    frame()
+    frame(v1, v0, hiz[0], hiz[1])
     counters = rast.counters()
-    rast.reset_counters()
 
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -233,76 +324,74 @@ def run_ours(args):
         for i in range(args.steps):
             flush.zero_()
             ev[i][0].record(stream)
-            frame()
+            frame(v1, v0, hiz[0], hiz[1])
             ev[i][1].record(stream)
         torch.cuda.synchronize()
     api.profile_enable(False)
     prof = api.profile_collect()
     launches = api.launch_count() - launches0
-    step_ms = [a.elapsed_time(b) for a, b in ev]
-    ms = float(np.mean(step_ms))
+    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
 
-    # per-kernel device time over the timed region
     per = {}
     for name, t in prof:
         c, s = per.get(name, (0, 0.0))
         per[name] = (c + 1, s + t)
-    top = max(per.items(), key=lambda kv: kv[1][1])
-    top_name, (top_count, top_total) = top
-    top_avg_ms = top_total / top_count
-
-    # algorithmic bytes of the draw kernel: positions + indices of every drawn meshlet (1152 B),
-    # the 12-byte meshlet header, and one read+write of the 8-byte vis-buffer key per pixel
-    batches = len(ctxs)
-    draw_bytes = (n * (1152 + 16)) / batches + v.width * v.height * 16 / batches
     peak, peak_kind = peaks()
-    achieved = draw_bytes / (per["k_draw_meshlets"][1] / per["k_draw_meshlets"][0] / 1e3) / 1e9
-    roofline = {"bound": "hbm", "kernel": "k_draw_meshlets", "achieved": achieved, "peak": peak, "unit": "GB/s",
+    ids = fb.get_pixels(1)  # depth layer: sky pixels keep the clear depth 0
+    covered = int((ids != 0).sum())
+    # algorithmic bytes per launch (what each kernel must move at minimum)
+    algo = {
+        "k_draw_meshlets": (n * (1152 + 16)) / len(batches) + W * H * 16 / len(batches),
+        "k_resolve": W * H * (8 + 4) + covered * 60 + covered * 2 * 4 + (W * H - covered) * 4 * 4,
+        "k_raster_big": W * H * 16 / len(batches),
+    }
+    top_name = max((k for k in per if k in algo), key=lambda k: per[k][1])
+    top_avg_s = per[top_name][1] / per[top_name][0] / 1e3
+    achieved = algo[top_name] / top_avg_s / 1e9
+    roofline = {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
-                "algorithmic_bytes_per_launch": draw_bytes}
+                "algorithmic_bytes_per_launch": algo[top_name], "avg_launch_ms": top_avg_s * 1e3}
 
-    # end to end through the public API: pinned host scene upload + frame + id layer readback
+    # end to end through the public API: pinned host scene upload + frame + colour readback
     pinned = torch.empty(sc.meshlets.nbytes, dtype=torch.uint8).pin_memory()
     pinned.numpy()[:] = sc.meshlets.view(np.uint8).reshape(-1)
-    host_ids = torch.empty((v.height, v.width), dtype=torch.int32).pin_memory()
-    import ctypes as C
+    host_img = torch.empty((H, W), dtype=torch.int32).pin_memory()
     e2e_ms = []
     for i in range(args.warmup + args.steps):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         api._check(api._lib.swr_scene_upload_meshlets(scene.h, C.c_void_p(pinned.data_ptr()), 0, n))
-        frame()
-        api._check(api._lib.swr_framebuffer_get_pixels(fb.h, 0, C.c_void_p(host_ids.data_ptr()), v.width))
-        dt = (time.perf_counter() - t0) * 1e3
+        frame(v1, v0, hiz[0], hiz[1])
+        api._check(api._lib.swr_framebuffer_get_pixels(fb.h, 0, C.c_void_p(host_img.data_ptr()), W))
         if i >= args.warmup:
-            e2e_ms.append(dt)
+            e2e_ms.append((time.perf_counter() - t0) * 1e3)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = cpu_threads()
-        times = time_cpu_frames(sc, args.cpu_seconds, threads)
+        of = OracleFrame(sc, [t.get_data() for t in texs], env.get_data(), threads)
+        times = of.timed(args.cpu_seconds)
         cpu = {"value": float(np.median(times) * 1e3), "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{len(times)} full frames of the same workload (median), oracle restatement, "
-                         f"rows split over {threads} threads"}
+               "sample": f"{len(times)} full frames of the same workload (median), oracle restatement, draw and "
+                         f"resolve rows split over {threads} threads"}
 
-    tris_drawn = int(counters[0])
     if rank == 0:
         line = {"metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32+i32", "data": "synthetic (seeded)",
                 "config": config_dict(args, sc, {"parallelism": "replicas only (one GPU renders the frame)"}),
-                "gtri_per_s": tris_drawn / (ms / 1e3) / 1e9,
-                "gpix_per_s": v.width * v.height / (ms / 1e3) / 1e9,
+                "gtri_per_s": int(counters[0]) / (ms / 1e3) / 1e9,
+                "gpix_per_s": W * H / (ms / 1e3) / 1e9,
                 "counters": {"triangles_processed": int(counters[0]), "triangles_rasterized": int(counters[1]),
                              "triangles_clipped": int(counters[2])},
                 "kernels_ms_per_step": {k: s / args.steps for k, (c, s) in sorted(per.items())},
                 "roofline": roofline,
                 "e2e": {"value": float(np.median(e2e_ms)), "unit": UNIT, "h2d_bytes_per_step": int(sc.meshlets.nbytes),
-                        "d2h_bytes_per_step": int(v.width * v.height * 4)},
+                        "d2h_bytes_per_step": int(W * H * 4)},
                 "gpu_launches": int(launches), "clocks": clocks.summary(), "cpu_baseline": cpu}
         print(json.dumps(line), flush=True)
     if world > 1:

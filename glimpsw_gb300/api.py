@@ -87,6 +87,7 @@ _SIGS = {
     "swr_texture_destroy": [C.c_void_p],
     "swr_texture_set_pixels": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32],
     "swr_texture_generate_mips": [C.c_void_p],
+    "swr_texture_set_pixels_device": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32],
     "swr_texture_info": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
     "swr_texture_get_data": [C.c_void_p, C.c_void_p, C.c_size_t],
     "swr_texture_set_data": [C.c_void_p, C.c_void_p, C.c_size_t],
@@ -229,6 +230,10 @@ class Texture2D:
     def set_pixels(self, pixels: np.ndarray, layer: int = 0) -> None:
         pixels = np.ascontiguousarray(pixels, dtype=np.uint32)
         _check(_lib.swr_texture_set_pixels(self.h, pixels.ctypes.data, pixels.shape[1], layer))
+
+    def set_pixels_device(self, pixels, layer: int = 0) -> None:
+        """Row-major texels already on the device (e.g. a torch int32 tensor of shape (h, w))."""
+        _check(_lib.swr_texture_set_pixels_device(self.h, _ptr(pixels), self.width, layer))
 
     def generate_mips(self) -> None:
         _check(_lib.swr_texture_generate_mips(self.h))

@@ -164,6 +164,18 @@ swr_status swr_texture_set_pixels(swr_texture t, const uint32_t* pixels, uint32_
     return SWR_OK;
 }
 
+swr_status swr_texture_set_pixels_device(swr_texture t, const uint32_t* pixels_device, uint32_t stride, uint32_t layer) {
+    if (!t || !pixels_device || layer >= t->d.num_layers || stride != t->d.width)
+        return swr_internal_fail(SWR_EINVAL, "swr_texture_set_pixels_device: bad argument (stride must equal the width)");
+    cudaStream_t st = swr_internal_stream();
+    LaunchScope ls("k_set_pixels", st);
+    k_set_pixels<<<grid_for(t->d.width * t->d.height), 256, 0, st>>>(
+        pixels_device, (uint32_t*)t->d.data + (size_t)layer * t->d.layer_stride, t->d.width, t->d.height, t->d.row_shift);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_texture_set_pixels_device");
+    return SWR_OK;
+}
+
 swr_status swr_texture_generate_mips(swr_texture t) {
     if (!t) return swr_internal_fail(SWR_EINVAL, "swr_texture_generate_mips: NULL texture");
     cudaStream_t st = swr_internal_stream();

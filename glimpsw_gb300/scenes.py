@@ -211,12 +211,8 @@ def make_view(width, height, eye, target, fov=60.0, near=0.1, depth_only=False) 
 # ---------------------------------------------------------------------------------- textures
 def value_noise_rgba(size: int, seed: int, cells: int = 32, layer: int = 0) -> np.ndarray:
     """Seeded RGBA8 value noise (bilinear over a cells x cells lattice, wrapping), uint32[size, size]."""
-    rng = np.random.default_rng(seed * 7919 + layer)
-    lat = rng.integers(0, 256, size=(cells, cells, 4), dtype=np.int64)
-    if layer == 1:
-        # layer 1 = tangent-space normal XY (centred near 128), metallic, roughness (Scene.h:8-10)
-        lat[..., 0] = 128 + (lat[..., 0] - 128) // 3
-        lat[..., 1] = 128 + (lat[..., 1] - 128) // 3
+    # layer 1 = tangent-space normal XY (centred near 128), metallic, roughness (Scene.h:8-10)
+    lat = _noise_lattice(seed, cells, layer)
     step = size // cells
     t = (np.arange(size) % step) * 256 // step                       # 8-bit fraction
     i0 = np.arange(size) // step
@@ -232,6 +228,39 @@ def value_noise_rgba(size: int, seed: int, cells: int = 32, layer: int = 0) -> n
     if layer == 0:
         v[..., 3] = 255
     return v[..., 0] | (v[..., 1] << 8) | (v[..., 2] << 16) | (v[..., 3] << 24)
+
+
+def _noise_lattice(seed: int, cells: int, layer: int) -> np.ndarray:
+    rng = np.random.default_rng(seed * 7919 + layer)
+    lat = rng.integers(0, 256, size=(cells, cells, 4), dtype=np.int64)
+    if layer == 1:
+        lat[..., 0] = 128 + (lat[..., 0] - 128) // 3
+        lat[..., 1] = 128 + (lat[..., 1] - 128) // 3
+    return lat
+
+
+def value_noise_rgba_torch(size: int, seed: int, cells: int = 32, layer: int = 0, device="cuda"):
+    """value_noise_rgba computed on the device with torch (same integer arithmetic, same texels);
+    returns an int32 tensor of shape (size, size) holding the packed RGBA8 words."""
+    import torch
+    lat = torch.from_numpy(_noise_lattice(seed, cells, layer)).to(device)
+    step = size // cells
+    ar = torch.arange(size, device=device)
+    t = (ar % step) * 256 // step
+    i0 = ar // step
+    i1 = (i0 + 1) % cells
+    ty, tx = t[:, None, None], t[None, :, None]
+    a = lat[i0[:, None], i0[None, :]]
+    b = lat[i0[:, None], i1[None, :]]
+    c = lat[i1[:, None], i0[None, :]]
+    d = lat[i1[:, None], i1[None, :]]
+    top = a * (256 - tx) + b * tx
+    bot = c * (256 - tx) + d * tx
+    v = (top * (256 - ty) + bot * ty) >> 16
+    if layer == 0:
+        v[..., 3] = 255
+    packed = v[..., 0] | (v[..., 1] << 8) | (v[..., 2] << 16) | (v[..., 3] << 24)
+    return (packed - ((packed >> 31) << 32)).to(torch.int32)
 
 
 def env_map_r11g11b10(size: int, seed: int) -> np.ndarray:

@@ -178,6 +178,8 @@ swr_status swr_texture_create(uint32_t format, uint32_t width, uint32_t height, 
 swr_status swr_texture_destroy(swr_texture t);
 /* SetPixels(pixels, stride, layer, 0): row-major host texels into mip 0 of a layer. */
 swr_status swr_texture_set_pixels(swr_texture t, const uint32_t* pixels, uint32_t stride, uint32_t layer);
+/* The same from row-major texels already in device memory (stream-ordered, no host sync). */
+swr_status swr_texture_set_pixels_device(swr_texture t, const uint32_t* pixels_device, uint32_t stride, uint32_t layer);
 swr_status swr_texture_generate_mips(swr_texture t);                                     /* GenerateMips */
 /* Raw storage (Data[], MipOffsets[16], levels) for inspection; words = layer_stride*layers. */
 swr_status swr_texture_info(swr_texture t, uint32_t* mip_levels, uint32_t* layer_stride, uint32_t mip_offsets[16]);

@@ -188,8 +188,11 @@ def downsample_depth(fb: Framebuffer, dest: Texture):
     lib().orc_downsample_depth(C.byref(fb.s), C.byref(dest.s))
 
 
-def resolve(fb: Framebuffer, ctx: Context):
-    lib().orc_resolve(C.byref(fb.s), C.byref(ctx.s))
+def resolve(fb: Framebuffer, ctx: Context, threads: int = 1):
+    if threads > 1:
+        lib().orc_resolve_mt(C.byref(fb.s), C.byref(ctx.s), C.c_uint32(threads))
+    else:
+        lib().orc_resolve(C.byref(fb.s), C.byref(ctx.s))
 
 
 def set_approx_mode(mode: int) -> bool:

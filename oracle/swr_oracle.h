@@ -125,6 +125,8 @@ void orc_downsample_depth(const orc_framebuffer* fb, orc_texture* dest);
 
 // ShadingContext::Resolve (Shading.cpp:658-690), light-sprite overlay excluded.
 void orc_resolve(orc_framebuffer* fb, const orc_shading_context* ctx);
+void orc_resolve_rows(orc_framebuffer* fb, const orc_shading_context* ctx, uint32_t row_begin, uint32_t row_end);
+void orc_resolve_mt(orc_framebuffer* fb, const orc_shading_context* ctx, uint32_t num_threads);
 
 #ifdef __cplusplus
 }

@@ -12,6 +12,8 @@
 #include "../include/swr/hostmath.h"
 
 #include <algorithm>
+#include <thread>
+#include <vector>
 
 namespace orc {
 namespace {
@@ -396,7 +398,7 @@ using namespace orc;
 
 // ShadingContext::Resolve (Shading.cpp:658-690). The light-sprite overlay (691-731) is not part
 // of the restatement. The number of meshlets of the scene bounds the surface ids it accepts.
-extern "C" void orc_resolve(orc_framebuffer* fb, const orc_shading_context* sc) {
+extern "C" void orc_resolve_rows(orc_framebuffer* fb, const orc_shading_context* sc, uint32_t row_begin, uint32_t row_end) {
     float invProj[16] = {};
     if (!swr_hostmath::inverse_screen_proj(sc->world_to_clip, fb->width, fb->height, invProj)) {
         fprintf(stderr, "orc_resolve: singular world-to-clip matrix\n");
@@ -409,7 +411,7 @@ extern "C" void orc_resolve(orc_framebuffer* fb, const orc_shading_context* sc) 
     const float* depthLayer = (const float*)(fb->data + fb->layer_stride);
     const F3 viewPos = { sc->view_pos[0], sc->view_pos[1], sc->view_pos[2] };
 
-    for (uint32_t y0 = 0; y0 < fb->height; y0 += 4) {
+    for (uint32_t y0 = row_begin & ~3u; y0 < std::min(row_end, fb->height); y0 += 4) {
         for (uint32_t x0 = 0; x0 < fb->width; x0 += 4) {
             uint32_t tileOffset = ((x0 & ~3u) << 2) + (y0 & ~3u) * fb->width;
             uint32_t ids[L];
@@ -448,4 +450,19 @@ extern "C" void orc_resolve(orc_framebuffer* fb, const orc_shading_context* sc) 
             }
         }
     }
+}
+
+extern "C" void orc_resolve(orc_framebuffer* fb, const orc_shading_context* sc) { orc_resolve_rows(fb, sc, 0, fb->height); }
+
+// Tiles are independent, so rows of 4x4 tiles split over threads give the same image.
+extern "C" void orc_resolve_mt(orc_framebuffer* fb, const orc_shading_context* sc, uint32_t num_threads) {
+    if (num_threads <= 1) { orc_resolve(fb, sc); return; }
+    std::vector<std::thread> threads;
+    uint32_t rows = ((fb->height + num_threads - 1) / num_threads + 3) & ~3u;
+    for (uint32_t t = 0; t < num_threads; t++) {
+        uint32_t r0 = t * rows, r1 = std::min(fb->height, r0 + rows);
+        if (r0 >= r1) break;
+        threads.emplace_back([=]() { orc_resolve_rows(fb, sc, r0, r1); });
+    }
+    for (auto& th : threads) th.join();
 }
