@@ -258,10 +258,18 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs 
     TriRec* tris = sTri[warp];
     unsigned long long nProcessed = 0, nRaster = 0, nClipped = 0;
 
+    // Meshlets are fetched kFetch at a time: one contended atomic per kFetch meshlets.
+    constexpr uint32_t kFetch = 4;
+    uint32_t fetchBase = 0, fetchLeft = 0;
     while (true) {
-        uint32_t m = 0;
-        if (lane == 0) m = (uint32_t)atomicAdd(&a.s.control[0], 1ull);
-        m = __shfl_sync(0xFFFFFFFFu, m, 0);
+        if (fetchLeft == 0) {
+            uint32_t b = 0;
+            if (lane == 0) b = (uint32_t)atomicAdd(&a.s.control[0], (unsigned long long)kFetch);
+            fetchBase = __shfl_sync(0xFFFFFFFFu, b, 0);
+            fetchLeft = kFetch;
+        }
+        const uint32_t m = fetchBase++;
+        fetchLeft--;
         if (m >= a.count) break;
         if (a.cullBitmap != nullptr && !((a.cullBitmap[m >> 4] >> (m & 15)) & 1)) continue;  // Shading.cpp:282-289
 
