@@ -5,10 +5,11 @@ Workload (the headline configuration): 100k meshlets of 64 vertices / 124 triang
 triangles), seeded, scattered in a 200^3 volume with log-uniform scale 0.1-10, 64 materials of two
 2048^2 RGBA8 layers with full mips, an octahedral 1024^2 R11G11B10 sky, 1920x1080. One step is one
 frame of the reference's frame driver (Main.cpp:171-261): clear, per 65536-meshlet batch
-CullMeshlets (frustum + Hi-Z of the previous view) then DrawMeshlets (unbinned semantics, clipping
-on), Resolve, and DownsampleDepth for the next frame. The camera of the timed frame is the
-perturbed second view; its Hi-Z input is built from the first view before timing (ping-pong
-textures keep every timed frame identical).
+CullMeshlets then DrawMeshlets (unbinned semantics, clipping on), Resolve, and DownsampleDepth for
+the next frame. The headline frame has no previous depth (frustum culling only, every triangle
+of the visible meshlets is set up); `hiz_frame` reports the following frame, whose perturbed
+camera is culled against that Hi-Z (in this dense scene the occlusion test removes almost all
+meshlets).
 
 Timing: CUDA events on the library's stream (torch's current stream), L2 flushed between timed
 steps by a 256 MiB write outside the step's events. `e2e` runs the same frame through the public
