@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--texture-size", type=int, default=2048)
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="budget of the CPU baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-multiview", action="store_true")
+    p.add_argument("--multiview-meshlets", type=int, default=200_000)
     return p.parse_args()
 
 
@@ -260,6 +262,65 @@ def peaks():
         return 6800.0, "fallback"
 
 
+# ----------------------------------------------------------------------------- multi-view
+def multiview_section(args, api, stream):
+    """64 views (6 depth-only cube faces at 1024^2 + 58 cameras of log-uniform resolution) of a
+    200k-meshlet grid: one batched graph launch (autotuned chunk size / warps per block) against
+    64 per-view sequences of clear + frustum cull + draw through the regular entry points."""
+    import torch
+
+    from glimpsw_gb300 import autotune, scenes
+    sc = scenes.multiview_scene(n=args.multiview_meshlets)
+    scene = api.Scene()
+    scene.upload_meshlets(sc.meshlets)
+    scene.set_materials(sc.materials)
+    rast = api.Rasterizer()
+    rast.EnableBinning = False
+    n = len(sc.meshlets)
+    fbs = [api.Framebuffer(v.width, v.height) for v in sc.views]
+    views = [(fb, v.proj, v.view, scenes.IDENTITY, v.depth_only) for fb, v in zip(fbs, sc.views)]
+    batch = api.Batch(rast, scene, views)
+    gpu = torch.cuda.get_device_name()
+    best, timings = autotune.tune(batch, key=autotune.workload_key(gpu, views, n), repeats=3)
+    bms = [torch.zeros((n + 15) // 16, dtype=torch.int16, device="cuda") for _ in sc.views]
+    ctxs = [api.ShadingContext(scene, v.world_to_clip, cull_bitmap=bm) for v, bm in zip(sc.views, bms)]
+    visible = [api.cull_meshlets(scene, 0, n, bm, v.proj, v.view, scenes.IDENTITY, v.view, v.width, v.height, None,
+                                 want_count=True) for v, bm in zip(sc.views, bms)]
+
+    def per_view():
+        for fb, v, bm, ctx in zip(fbs, sc.views, bms, ctxs):
+            fb.clear(0xFF000000, 0.0)
+            api.cull_meshlets(scene, 0, n, bm, v.proj, v.view, scenes.IDENTITY, v.view, v.width, v.height, None)
+            rast.draw_meshlets(fb, n, ctx)
+
+    def timed(fn, steps):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return float(np.median(ms))
+
+    batched_ms = timed(batch.render, args.steps)
+    per_view_ms = timed(per_view, args.steps)
+    batch.reset_counters()
+    batch.render()
+    c = batch.counters()
+    return {"views": len(sc.views), "meshlets": n, "pixels": int(sum(v.width * v.height for v in sc.views)),
+            "visible_meshlets_per_view": {"min": int(min(visible)), "max": int(max(visible)),
+                                          "total": int(sum(visible))},
+            "batched_ms": batched_ms, "per_view_ms": per_view_ms, "speedup": per_view_ms / batched_ms,
+            "autotuned": {"chunk_px": best[0] * 4, "warps_per_block": best[1],
+                          "candidates_ms": {f"{cc * 4}px/{w}w": round(t, 4) for (cc, w), t in timings.items()}},
+            "triangles_processed": int(c[0]), "gtri_per_s": float(c[0]) / (batched_ms / 1e3) / 1e9}
+
+
 # ----------------------------------------------------------------------------- GPU
 def run_ours(args):
     import torch
@@ -387,6 +448,11 @@ def run_ours(args):
         if i >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
 
+    multiview = None
+    if not args.no_multiview:
+        del pinned, host_img
+        multiview = multiview_section(args, api, stream)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = cpu_threads()
@@ -412,7 +478,8 @@ def run_ours(args):
                 "roofline": roofline,
                 "e2e": {"value": float(np.median(e2e_ms)), "unit": UNIT, "h2d_bytes_per_step": int(sc.meshlets.nbytes),
                         "d2h_bytes_per_step": int(W * H * 4)},
-                "gpu_launches": int(launches), "clocks": clocks.summary(), "cpu_baseline": cpu}
+                "gpu_launches": int(launches), "clocks": clocks.summary(), "cpu_baseline": cpu,
+                "multiview": multiview}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

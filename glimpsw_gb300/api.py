@@ -95,7 +95,19 @@ _SIGS = {
                           C.c_void_p, C.c_float, C.c_float, C.c_void_p, C.c_void_p],
     "swr_downsample_depth": [C.c_void_p, C.c_void_p],
     "swr_resolve": [C.c_void_p, C.c_void_p, C.c_void_p],
+    "swr_batch_create": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p],
+    "swr_batch_set_views": [C.c_void_p, C.c_void_p, C.c_uint32],
+    "swr_batch_set_tuning": [C.c_void_p, C.c_uint32, C.c_uint32],
+    "swr_batch_render": [C.c_void_p],
+    "swr_batch_get_counters": [C.c_void_p, C.c_void_p],
+    "swr_batch_reset_counters": [C.c_void_p],
+    "swr_batch_destroy": [C.c_void_p],
 }
+
+
+class SwrViewDesc(C.Structure):
+    _fields_ = [("fb", C.c_void_p), ("proj", C.c_float * 16), ("view", C.c_float * 16), ("model", C.c_float * 16),
+                ("depth_only", C.c_uint32)]
 _RESTYPES = {"swr_last_error": C.c_char_p, "swr_get_stream": C.c_void_p, "swr_launch_count": C.c_uint64}
 
 
@@ -325,6 +337,58 @@ def cull_meshlets(scene: Scene, first: int, count: int, bitmap_device, proj, vie
 
 def downsample_depth(fb: Framebuffer, dest: Texture2D) -> None:
     _check(_lib.swr_downsample_depth(fb.h, dest.h))
+
+
+class Batch:
+    """Batched multi-view rendering (swr_batch_*): many framebuffers, one CUDA graph per frame.
+
+    views: list of (Framebuffer, proj, view, model, depth_only)."""
+
+    def __init__(self, rast: "Rasterizer", scene: Scene, views, first: int = 0, count: int | None = None,
+                 frustum_cull: bool = True):
+        L = load_library()
+        if count is None:
+            c = C.c_uint32()
+            _check(L.swr_scene_meshlet_count(scene.h, C.byref(c)))
+            count = c.value - first
+        self._views = list(views)
+        arr = self._descs(self._views)
+        h = C.c_void_p()
+        _check(L.swr_batch_create(rast.h, scene.h, first, count, arr, len(self._views), int(frustum_cull), C.byref(h)))
+        self.h = h
+        self.count, self.rast, self.scene = count, rast, scene
+
+    @staticmethod
+    def _descs(views):
+        arr = (SwrViewDesc * len(views))()
+        for i, (fb, proj, view, model, depth_only) in enumerate(views):
+            arr[i].fb = fb.h.value
+            arr[i].proj, arr[i].view, arr[i].model = _f16(proj), _f16(view), _f16(model)
+            arr[i].depth_only = int(depth_only)
+        return arr
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.swr_batch_destroy(self.h)
+            self.h = None
+
+    def set_views(self, views) -> None:
+        self._views = list(views)
+        _check(_lib.swr_batch_set_views(self.h, self._descs(self._views), len(self._views)))
+
+    def set_tuning(self, chunk_tiles: int = 0, warps_per_block: int = 0) -> None:
+        _check(_lib.swr_batch_set_tuning(self.h, chunk_tiles, warps_per_block))
+
+    def render(self) -> None:
+        _check(_lib.swr_batch_render(self.h))
+
+    def counters(self) -> np.ndarray:
+        out = np.zeros(4, dtype=np.uint64)
+        _check(_lib.swr_batch_get_counters(self.h, out.ctypes.data))
+        return out
+
+    def reset_counters(self) -> None:
+        _check(_lib.swr_batch_reset_counters(self.h))
 
 
 class Rasterizer:

@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libswr_gb300.so")
-SOURCES = ["swr_api.cu", "swr_raster.cu", "swr_texture.cu", "swr_shade.cu", "swr_noalloc.cu"]
+SOURCES = ["swr_api.cu", "swr_raster.cu", "swr_texture.cu", "swr_shade.cu", "swr_batch.cu", "swr_noalloc.cu"]
 HEADERS = ["swr_device.cuh", "swr_internal.h"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -129,6 +129,13 @@ swr::LaunchScope::~LaunchScope() {
     if (rec >= 0) cudaEventRecord(t_prof[rec].stop, st);
 }
 
+bool swr_internal_set_profiling(bool on) {
+    bool prev = t_profiling;
+    t_profiling = on;
+    return prev;
+}
+void swr_internal_count_launches(unsigned long long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
 swr_status swr_internal_fail(swr_status code, const char* msg) { return fail(code, "%s", msg); }
 swr_status swr_internal_cuda_fail(cudaError_t e, const char* what) { return cuda_fail(e, what); }
 cudaStream_t swr_internal_stream() { return t_stream; }

@@ -1,0 +1,321 @@
+// Batched multi-view rendering: many views of different resolutions and meshlet ranges drawn by one
+// persistent launch of the mesh stage, the whole frame (clear, frustum culling, draw, chunk raster,
+// finalize) captured once into a CUDA graph and replayed. The reference renders one view per
+// DrawMeshlets call (Main.cpp:216-245); each view of a batch gives exactly the vis-buffer of that
+// call sequence (clear, CullMeshlets without depth map, DrawMeshlets), since keys stay per view.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/swr/hostmath.h"
+#include "swr_device.cuh"
+#include "swr_internal.h"
+
+namespace swr {
+namespace {
+
+struct BatchView {              // device table for the batched clear / cull / finalize kernels
+    float planes[5][4];         // CullMeshlets frustum planes 0..4 (Shading.cpp:806)
+    uint32_t* layer0;
+    uint32_t* layer1;
+    unsigned long long* keys;
+    uint16_t* bitmap;
+    uint32_t pixels;            // width * height
+    uint32_t depthOnly;
+    uint32_t pad[2];
+};
+
+// Framebuffer::Clear(color, depth) for every view; keys restart from the cleared depth.
+__global__ void k_clear_views(const BatchView* __restrict__ views, uint32_t color, uint32_t depthBits) {
+    const BatchView& v = views[blockIdx.y];
+    const unsigned long long key = ((unsigned long long)float_order(__uint_as_float(depthBits)) << 32) | kKeyEmptyLow;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < v.pixels; i += gridDim.x * blockDim.x) {
+        v.layer0[i] = color;
+        v.layer1[i] = depthBits;
+        v.keys[i] = key;
+    }
+}
+
+// CullMeshlets without a depth map (Shading.cpp:797-809, 865): frustum planes 0..4, one meshlet per
+// thread, the view in blockIdx.y; a warp's ballot gives two 16-bit masks.
+__global__ void k_cull_views(const BatchView* __restrict__ views, const uint8_t* __restrict__ meshlets, uint32_t first,
+                             uint32_t count) {
+    const BatchView& v = views[blockIdx.y];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    bool visible = i < count;
+    if (visible) {
+        const float4 s = *(const float4*)(meshlets + (size_t)(first + i) * kMeshletSize);
+        for (int k = 0; k < 5; k++) {
+            float dist = fadd(ffma(s.x, v.planes[k][0], ffma(s.y, v.planes[k][1], fmul(s.z, v.planes[k][2]))), v.planes[k][3]);
+            visible = visible && (dist > -s.w);
+        }
+    }
+    const unsigned m = __ballot_sync(0xFFFFFFFFu, visible);
+    const uint32_t w0 = i & ~31u;
+    if ((threadIdx.x & 31) == 0 && w0 < count) {
+        v.bitmap[w0 / 16] = (uint16_t)(m & 0xFFFF);
+        if (w0 + 16 < count) v.bitmap[w0 / 16 + 1] = (uint16_t)(m >> 16);
+    }
+}
+
+// Keys to the reference's layers for every view; depth-only views keep only the depth layer.
+__global__ void k_finalize_views(const BatchView* __restrict__ views) {
+    const BatchView& v = views[blockIdx.y];
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < v.pixels; i += gridDim.x * blockDim.x) {
+        const unsigned long long k = v.keys[i];
+        const uint32_t low = (uint32_t)k;
+        if (low == kKeyEmptyLow) continue;
+        v.layer1[i] = __float_as_uint(float_unorder((uint32_t)(k >> 32)));
+        if (!v.depthOnly) v.layer0[i] = rank_surface_id(0xFFFFFFFEu - low);
+    }
+}
+
+}  // namespace
+}  // namespace swr
+
+using namespace swr;
+
+struct swr_batch_t {
+    swr_rasterizer rast;
+    swr_scene scene;
+    uint32_t first, count, numViews;
+    int frustumCull;
+    uint32_t maxPixels;
+    std::vector<swr_framebuffer> fbs;
+    ViewParams* dViews = nullptr;
+    BatchView* dBatch = nullptr;
+    uint32_t* dViewStart = nullptr;
+    uint16_t* dBitmaps = nullptr;
+    DrawScratch scratch = {};
+    uint32_t chunkTiles = 0, warpsPerBlock = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long kernelNodes = 0;
+};
+
+namespace {
+
+int sm_count() {
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    return n > 0 ? n : 148;
+}
+
+swr_status upload_views(swr_batch b, const swr_view_desc* views) {
+    std::vector<ViewParams> vp(b->numViews);
+    std::vector<BatchView> bv(b->numViews);
+    const uint32_t words = (b->count + 15) / 16;
+    for (uint32_t i = 0; i < b->numViews; i++) {
+        const swr_view_desc& d = views[i];
+        swr_framebuffer fb = b->fbs[i];
+        float pv[16], objToClip[16], planes[6][4];
+        swr_hostmath::mat4_mul(d.proj, d.view, pv);
+        swr_hostmath::mat4_mul(pv, d.model, objToClip);
+        swr_hostmath::frustum_planes(objToClip, planes);
+        ViewParams& v = vp[i];
+        memset(&v, 0, sizeof(v));
+        memcpy(v.m, objToClip, sizeof(v.m));
+        v.halfW = (int32_t)fb->width / 2, v.halfH = (int32_t)fb->height / 2;
+        v.width = fb->width, v.height = fb->height;
+        // binned or unbinned semantics follow the rasterizer's flags, as swr_draw_meshlets does
+        v.bx = (float)SWR_MAX_RENDER_SIZE / (float)fb->width;
+        v.by = (float)SWR_MAX_RENDER_SIZE / (float)fb->height;
+        if (!b->rast->enable_binning && !b->rast->enable_guardband) v.bx = v.by = 1.0f;
+        v.meshletOffset = b->first;
+        v.count = b->count;
+        v.keys = fb->keys;
+        v.cullBitmap = b->frustumCull ? b->dBitmaps + (size_t)i * words : nullptr;
+        BatchView& w = bv[i];
+        memset(&w, 0, sizeof(w));
+        memcpy(w.planes, planes, sizeof(w.planes));
+        w.layer0 = fb->layers;
+        w.layer1 = fb->layers + fb->layer_stride;
+        w.keys = fb->keys;
+        w.bitmap = b->dBitmaps + (size_t)i * words;
+        w.pixels = fb->width * fb->height;
+        w.depthOnly = d.depth_only != 0;
+    }
+    cudaStream_t st = swr_internal_stream();
+    cudaError_t e = cudaMemcpyAsync(b->dViews, vp.data(), vp.size() * sizeof(ViewParams), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b->dBatch, bv.data(), bv.size() * sizeof(BatchView), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // the host staging vectors die here
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_batch: view upload");
+    return SWR_OK;
+}
+
+// The frame, recorded once on a private stream into a graph (event tracing is paused while
+// capturing; the graph's kernels are counted at every replay).
+swr_status capture(swr_batch b) {
+    cudaStream_t cs;
+    cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_batch: stream");
+    const bool prof = swr_internal_set_profiling(false);
+    e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        const uint32_t nv = b->numViews;
+        const int blocksX = (int)std::min<uint32_t>((b->maxPixels + 255) / 256, 1024u);
+        k_clear_views<<<dim3(blocksX, nv), 256, 0, cs>>>(b->dBatch, 0xFF000000u, 0u);
+        if (b->frustumCull && b->count)
+            k_cull_views<<<dim3((b->count + 255) / 256, nv), 256, 0, cs>>>(b->dBatch, b->scene->meshlets, b->first, b->count);
+        cudaMemsetAsync(b->scratch.control, 0, 3 * sizeof(unsigned long long), cs);
+        DrawArgs a = {};
+        a.meshlets = b->scene->meshlets;
+        a.materials = b->scene->materials;
+        a.numMaterials = b->scene->num_materials;
+        a.clipMode = (!b->rast->enable_binning && b->rast->enable_clipping) ? 1 : 0;
+        a.countClipped = (b->rast->enable_binning || b->rast->enable_clipping) ? 1 : 0;
+        a.s = b->scratch;
+        a.views = b->dViews;
+        a.viewStart = b->dViewStart;
+        a.numViews = nv;
+        a.chunkTiles = b->chunkTiles;
+        a.warpsPerBlock = b->warpsPerBlock;
+        launch_draw(a, cs, sm_count());
+        k_finalize_views<<<dim3(blocksX, nv), 256, 0, cs>>>(b->dBatch);
+        e = cudaStreamEndCapture(cs, &b->graph);
+    }
+    swr_internal_set_profiling(prof);
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+    if (e == cudaSuccess) {
+        size_t n = 0;
+        cudaGraphGetNodes(b->graph, nullptr, &n);
+        std::vector<cudaGraphNode_t> nodes(n);
+        cudaGraphGetNodes(b->graph, nodes.data(), &n);
+        b->kernelNodes = 0;
+        for (cudaGraphNode_t node : nodes) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(node, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) b->kernelNodes++;
+        }
+    }
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_batch: graph capture");
+    return SWR_OK;
+}
+
+void drop_graph(swr_batch b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr, b->graph = nullptr;
+}
+
+}  // namespace
+
+extern "C" {
+
+swr_status swr_batch_create(swr_rasterizer r, swr_scene s, uint32_t first, uint32_t count, const swr_view_desc* views,
+                            uint32_t num_views, int frustum_cull, swr_batch* out) {
+    if (!r || !s || !views || !out || num_views == 0) return swr_internal_fail(SWR_EINVAL, "swr_batch_create: bad argument");
+    if ((uint64_t)first + count > s->count) return swr_internal_fail(SWR_EINVAL, "swr_batch_create: range outside the scene");
+    if (num_views > 4096) return swr_internal_fail(SWR_EINVAL, "swr_batch_create: at most 4096 views");
+    for (uint32_t i = 0; i < num_views; i++)
+        if (!views[i].fb) return swr_internal_fail(SWR_EINVAL, "swr_batch_create: view without framebuffer");
+    if ((uint64_t)count * num_views >= (1ull << 32)) return swr_internal_fail(SWR_EINVAL, "swr_batch_create: too many work items");
+    swr_batch b = new (std::nothrow) swr_batch_t();
+    if (!b) return swr_internal_fail(SWR_ENOMEM, "swr_batch_create: host allocation failed");
+    b->rast = r, b->scene = s, b->first = first, b->count = count, b->numViews = num_views, b->frustumCull = frustum_cull != 0;
+    uint64_t totalTris = 0;
+    for (uint32_t i = 0; i < num_views; i++) {
+        b->fbs.push_back(views[i].fb);
+        b->maxPixels = std::max(b->maxPixels, views[i].fb->width * views[i].fb->height);
+        totalTris += (uint64_t)count * 32;
+    }
+    const uint32_t words = (count + 15) / 16;
+    std::vector<uint32_t> start(num_views + 1);
+    for (uint32_t i = 0; i <= num_views; i++) start[i] = i * count;
+    cudaError_t e = cudaMalloc(&b->dViews, num_views * sizeof(ViewParams));
+    if (e == cudaSuccess) e = cudaMalloc(&b->dBatch, num_views * sizeof(BatchView));
+    if (e == cudaSuccess) e = cudaMalloc(&b->dViewStart, (num_views + 1) * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&b->dBitmaps, (size_t)num_views * words * sizeof(uint16_t) + 16);
+    if (e == cudaSuccess) e = cudaMemcpy(b->dViewStart, start.data(), start.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    // the batch's own queue: a quarter of the triangles of every view; overflow is rasterized in place
+    b->scratch.bigCapacity = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(totalTris, 1u << 18), 1u << 26);
+    if (e == cudaSuccess) e = cudaMalloc(&b->scratch.control, 16 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(b->scratch.control, 0, 16 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&b->scratch.big, (size_t)b->scratch.bigCapacity * sizeof(TriRec));
+    if (e == cudaSuccess) e = cudaMalloc(&b->scratch.bigBase, (size_t)b->scratch.bigCapacity * sizeof(unsigned long long));
+    if (e != cudaSuccess) {
+        swr_batch_destroy(b);
+        return swr_internal_cuda_fail(e, "swr_batch_create");
+    }
+    swr_status st = upload_views(b, views);
+    if (st != SWR_OK) {
+        swr_batch_destroy(b);
+        return st;
+    }
+    *out = b;
+    return SWR_OK;
+}
+
+swr_status swr_batch_set_views(swr_batch b, const swr_view_desc* views, uint32_t num_views) {
+    if (!b || !views || num_views != b->numViews) return swr_internal_fail(SWR_EINVAL, "swr_batch_set_views: bad argument");
+    for (uint32_t i = 0; i < num_views; i++)
+        if (views[i].fb != b->fbs[i]) return swr_internal_fail(SWR_EINVAL, "swr_batch_set_views: framebuffers must not change");
+    return upload_views(b, views);
+}
+
+swr_status swr_batch_set_tuning(swr_batch b, uint32_t chunk_tiles, uint32_t warps_per_block) {
+    if (!b) return swr_internal_fail(SWR_EINVAL, "swr_batch_set_tuning: NULL batch");
+    if (chunk_tiles && chunk_tiles != 2 && chunk_tiles != 4 && chunk_tiles != 8 && chunk_tiles != 16)
+        return swr_internal_fail(SWR_EINVAL, "swr_batch_set_tuning: chunk_tiles must be 2, 4, 8 or 16 (8-64 px bins)");
+    if (warps_per_block && warps_per_block != 4 && warps_per_block != 8 && warps_per_block != 16)
+        return swr_internal_fail(SWR_EINVAL, "swr_batch_set_tuning: warps_per_block must be 4, 8 or 16");
+    if (chunk_tiles != b->chunkTiles || warps_per_block != b->warpsPerBlock) drop_graph(b);
+    b->chunkTiles = chunk_tiles, b->warpsPerBlock = warps_per_block;
+    return SWR_OK;
+}
+
+swr_status swr_batch_render(swr_batch b) {
+    if (!b) return swr_internal_fail(SWR_EINVAL, "swr_batch_render: NULL batch");
+    if (!b->exec) {
+        swr_status st = capture(b);
+        if (st != SWR_OK) return st;
+    }
+    cudaStream_t st = swr_internal_stream();
+    cudaError_t e;
+    {
+        LaunchScope ls("swr_batch_graph", st);
+        e = cudaGraphLaunch(b->exec, st);
+    }
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_batch_render");
+    if (b->kernelNodes > 1) swr_internal_count_launches(b->kernelNodes - 1);
+    for (swr_framebuffer fb : b->fbs) fb->keys_valid = true;
+    return SWR_OK;
+}
+
+swr_status swr_batch_get_counters(swr_batch b, uint64_t out[SWR_NUM_COUNTERS]) {
+    if (!b || !out) return swr_internal_fail(SWR_EINVAL, "swr_batch_get_counters: bad argument");
+    unsigned long long c[16];
+    cudaStream_t st = swr_internal_stream();
+    cudaError_t e = cudaMemcpyAsync(c, b->scratch.control, sizeof(c), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_batch_get_counters");
+    out[0] = c[3], out[1] = c[4], out[2] = c[5], out[3] = c[6];
+    return SWR_OK;
+}
+
+swr_status swr_batch_reset_counters(swr_batch b) {
+    if (!b) return swr_internal_fail(SWR_EINVAL, "swr_batch_reset_counters: NULL batch");
+    cudaError_t e = cudaMemsetAsync(b->scratch.control + 3, 0, 4 * sizeof(unsigned long long), swr_internal_stream());
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_batch_reset_counters");
+    return SWR_OK;
+}
+
+swr_status swr_batch_destroy(swr_batch b) {
+    if (!b) return SWR_OK;
+    drop_graph(b);
+    cudaFree(b->dViews);
+    cudaFree(b->dBatch);
+    cudaFree(b->dViewStart);
+    cudaFree(b->dBitmaps);
+    cudaFree(b->scratch.control);
+    cudaFree(b->scratch.big);
+    cudaFree(b->scratch.bigBase);
+    delete b;
+    return SWR_OK;
+}
+
+}  // extern "C"

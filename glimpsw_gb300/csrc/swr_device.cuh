@@ -60,7 +60,8 @@ __device__ __forceinline__ uint32_t srai16_4(uint32_t v) {
 // Total order on floats as unsigned integers (monotone for all non-NaN values, -0 == +0).
 __device__ __forceinline__ uint32_t float_order(float f) {
     uint32_t b = __float_as_uint(f);
-    return (b & 0x80000000u) ? ((b == 0x80000000u) ? 0x80000000u : ~b) : (b | 0x80000000u);
+    b = (b == 0x80000000u) ? 0u : b;                      // -0 orders like +0
+    return b ^ ((uint32_t)((int32_t)b >> 31) | 0x80000000u);  // positive: set sign; negative: invert
 }
 __device__ __forceinline__ float float_unorder(uint32_t o) {
     return __uint_as_float((o & 0x80000000u) ? (o & 0x7FFFFFFFu) : ~o);

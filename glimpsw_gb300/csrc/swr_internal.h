@@ -51,10 +51,24 @@ struct DrawScratch {
 
 enum : unsigned long long { kStatusBigOverflow = 1ull, kStatusClipOverflow = 2ull };
 
+// One view of a draw: its transform, viewport, vis-buffer keys and meshlet range.
+struct ViewParams {
+    float m[16];
+    int32_t halfW, halfH;
+    uint32_t width, height;
+    float bx, by;
+    uint32_t meshletOffset, count;
+    unsigned long long* keys;
+    const uint16_t* cullBitmap;
+    uint32_t pad[4];
+};
+static_assert(sizeof(ViewParams) == 128, "ViewParams");
+
 struct DrawArgs {
     const uint8_t* meshlets;
     const DevMaterial* materials;
     uint32_t numMaterials;
+    // single view (views == nullptr)
     uint32_t meshletOffset;
     uint32_t count;
     const uint16_t* cullBitmap;
@@ -66,6 +80,13 @@ struct DrawArgs {
     int countClipped; // count non-trivial triangles in TrianglesClipped
     unsigned long long* keys;
     DrawScratch s;
+    // batched views: work item i of [0, viewStart[numViews]) is meshlet i - viewStart[v] of view v
+    const ViewParams* views;
+    const uint32_t* viewStart;
+    uint32_t numViews;
+    // tuning: chunk edge in 4x4 tiles (0 = 8) and warps per block (0 = 8)
+    uint32_t chunkTiles;
+    uint32_t warpsPerBlock;
 };
 
 void launch_draw(const DrawArgs& a, cudaStream_t st, int numSMs);
@@ -82,6 +103,10 @@ void launch_detile(const uint32_t* src, uint32_t* dst, uint32_t width, uint32_t 
 swr_status swr_internal_fail(swr_status code, const char* msg);
 swr_status swr_internal_cuda_fail(cudaError_t e, const char* what);
 cudaStream_t swr_internal_stream();
+// Profiling on/off for this thread (returns the previous state) and extra launches to count
+// (kernels replayed inside a CUDA graph).
+bool swr_internal_set_profiling(bool on);
+void swr_internal_count_launches(unsigned long long n);
 
 namespace swr {
 // Kernel tracing: every launch is counted; while profiling is enabled each launch is bracketed

@@ -121,6 +121,22 @@ __device__ __forceinline__ void shade_fragment(const TriRec& r, uint32_t px, uin
     if (key > *(volatile unsigned long long*)p) atomicMax(p, key);
 }
 
+// The same for pixel (tx + l % 4, ty + l / 4) of the 4x4 tile at the 4-aligned (tx, ty), l = lane % 16:
+// the tiled key offset is then the tile's base plus l.
+__device__ __forceinline__ void shade_tile_pixel(const TriRec& r, uint32_t tx, uint32_t ty, uint32_t l,
+                                                 unsigned long long* keys, uint32_t width) {
+    const uint32_t px = tx + (l & 3), py = ty + (l >> 2);
+    const int32_t e0 = (int32_t)((uint32_t)r.E0 + (uint32_t)r.A12 * px + (uint32_t)r.B12 * py);
+    const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
+    const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
+    if ((e0 | e1 | e2) < 0) return;
+    const float depth = ffma(__int2float_rn(e1), r.Z10, ffma(__int2float_rn(e2), r.Z20, r.Z0));
+    if (depth != depth) return;
+    const unsigned long long key = ((unsigned long long)float_order(depth) << 32) | r.lowword;
+    unsigned long long* p = keys + (tx << 2) + ty * width + l;
+    if (key > *(volatile unsigned long long*)p) atomicMax(p, key);
+}
+
 // One lane rasterizes a whole triangle (fallback of the rare clipped triangle that finds the
 // queue full; slow but exact).
 __device__ __noinline__ void raster_serial(const TriRec& r, unsigned long long* keys, uint32_t width) {
@@ -129,12 +145,13 @@ __device__ __noinline__ void raster_serial(const TriRec& r, unsigned long long* 
         for (uint32_t x = minX; x < maxX; x++) shade_fragment(r, x, y, keys, width);
 }
 
-// Appends a triangle to the chunk queue; false when the queue is full (the caller rasterizes it).
-__device__ __forceinline__ bool enqueue_big(const TriRec& r, const DrawArgs& a) {
+// Appends a triangle (its view index in r.pad) to the chunk queue; false when the queue is full
+// (the caller rasterizes it).
+__device__ __forceinline__ bool enqueue_big(const TriRec& r, const DrawArgs& a, uint32_t chunk) {
     int tilesX = ((r.bbMax & 0xFFFF) - (r.bbMin & 0xFFFF)) >> 2;
     int tilesY = ((r.bbMax >> 16) - (r.bbMin >> 16)) >> 2;
-    unsigned long long chunks = (unsigned long long)((tilesX + kChunkTiles - 1) / kChunkTiles) *
-                                (unsigned long long)((tilesY + kChunkTiles - 1) / kChunkTiles);
+    unsigned long long chunks = (unsigned long long)((tilesX + chunk - 1) / chunk) *
+                                (unsigned long long)((tilesY + chunk - 1) / chunk);
     unsigned long long old = atomicAdd(&a.s.control[1], (1ull << 40) | chunks);
     unsigned long long slot = old >> 40;
     if (slot < a.s.bigCapacity) {
@@ -164,7 +181,7 @@ __device__ __forceinline__ bool tile_empty(const TriRec& r, uint32_t px, uint32_
 __device__ __forceinline__ void raster_region(const TriRec& r, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
                                               unsigned long long* keys, uint32_t width, int lane) {
     const int T = tilesX * tilesY;
-    const uint32_t fx = lane & 3, fy = (lane >> 2) & 3, half = lane >> 4;
+    const uint32_t half = lane >> 4;
     for (int tb = 0; tb < T; tb += 32) {
         const int t = tb + lane;
         bool live = false;
@@ -183,7 +200,7 @@ __device__ __forceinline__ void raster_region(const TriRec& r, uint32_t x0, uint
             const int src = half ? s1 : s0;
             const uint32_t qx = __shfl_sync(0xFFFFFFFFu, tpx, src & 31);
             const uint32_t qy = __shfl_sync(0xFFFFFFFFu, tpy, src & 31);
-            if (src >= 0) shade_fragment(r, qx + fx, qy + fy, keys, width);
+            if (src >= 0) shade_tile_pixel(r, qx, qy, lane & 15, keys, width);
         }
     }
 }
@@ -192,14 +209,15 @@ __device__ __forceinline__ void raster_region(const TriRec& r, uint32_t x0, uint
 // lanes of a packet are independent (each prim restarts its new-vertex slots). Fan outputs are
 // set up with TrianglePacket::Setup and queued with rank (packet, clipped, lane, fan index).
 __device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t outcodes, const DrawArgs& a,
-                                            int cullMode, uint32_t gMeshlet, uint32_t prim, unsigned long long& nRaster) {
+                                            const ViewParams& vp, uint32_t viewIndex, uint32_t chunk, int cullMode,
+                                            uint32_t gMeshlet, uint32_t prim, unsigned long long& nRaster) {
     float V[4][16];  // x, y, z, w of the polygon's vertices (barycentric rows are not needed here)
     V[0][0] = v0.x, V[1][0] = v0.y, V[2][0] = v0.z, V[3][0] = v0.w;
     V[0][1] = v1.x, V[1][1] = v1.y, V[2][1] = v1.z, V[3][1] = v1.w;
     V[0][2] = v2.x, V[1][2] = v2.y, V[2][2] = v2.z, V[3][2] = v2.w;
     uint8_t idx[16] = { 0, 1, 2 };
     uint32_t vertCount = 3, nextIdx = 3;
-    const float guard[2] = { a.bx, a.by };
+    const float guard[2] = { vp.bx, vp.by };
 
     for (uint32_t planeId = 0; planeId < 6; planeId++) {
         if (!((outcodes >> planeId) & 1)) continue;
@@ -238,27 +256,54 @@ __device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t out
         Vtx a2 = { V[0][i2], V[1][i2], V[2][i2], V[3][i2] };
         Setup t;
         uint32_t bbMin, bbMax;
-        if (!tri_setup(a0, a1, a2, a.halfW, a.halfH, cullMode, t, bbMin, bbMax)) continue;
+        if (!tri_setup(a0, a1, a2, vp.halfW, vp.halfH, cullMode, t, bbMin, bbMax)) continue;
         TriRec r;
-        edge_setup(t, a.halfW, a.halfH, bbMin, bbMax, make_rank(gMeshlet, prim, 1, vi), r);
-        if (!enqueue_big(r, a)) raster_serial(r, a.keys, a.width);
+        edge_setup(t, vp.halfW, vp.halfH, bbMin, bbMax, make_rank(gMeshlet, prim, 1, vi), r);
+        r.pad = viewIndex;
+        if (!enqueue_big(r, a, chunk)) raster_serial(r, vp.keys, vp.width);
         nRaster++;
     }
 }
 
 // ------------------------------------------------------------------ kernels
-__global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs a) {
-    __shared__ float4 sPos[kWarpsPerBlock][64];
-    __shared__ uint32_t sIdx[kWarpsPerBlock][96];
-    __shared__ TriRec sTri[kWarpsPerBlock][32];
+// Per-warp shared memory: transformed vertices, index bytes, triangle records and the view.
+struct WarpSmem {
+    float4 pos[64];
+    uint32_t idx[96];
+    TriRec tris[32];
+    ViewParams view;
+};
 
+// Mesh stage. A work item is one meshlet of one view: a single-view draw numbers its meshlets
+// 0..count-1; a batched draw concatenates the meshlet ranges of its views (viewStart is their
+// prefix), so one launch serves views of any size.
+__global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
+    extern __shared__ __align__(16) unsigned char smemRaw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    float4* pos = sPos[warp];
-    const uint8_t* idxBytes = (const uint8_t*)sIdx[warp];
-    TriRec* tris = sTri[warp];
+    WarpSmem& S = ((WarpSmem*)smemRaw)[warp];
+    float4* pos = S.pos;
+    const uint8_t* idxBytes = (const uint8_t*)S.idx;
+    TriRec* tris = S.tris;
+    const ViewParams& vp = S.view;
+    const uint32_t chunk = a.chunkTiles ? a.chunkTiles : kChunkTiles;
+    const bool multi = a.views != nullptr;
+    const uint32_t totalItems = multi ? a.viewStart[a.numViews] : a.count;
+    uint32_t curView = 0xFFFFFFFFu;
+    if (!multi) {
+        if (lane == 0) {
+            ViewParams v = {};
+            for (int k = 0; k < 16; k++) v.m[k] = a.m[k];
+            v.halfW = a.halfW, v.halfH = a.halfH, v.width = a.width, v.height = a.height;
+            v.bx = a.bx, v.by = a.by, v.meshletOffset = a.meshletOffset, v.count = a.count;
+            v.keys = a.keys, v.cullBitmap = a.cullBitmap;
+            S.view = v;
+        }
+        curView = 0;
+        __syncwarp();
+    }
     unsigned long long nProcessed = 0, nRaster = 0, nClipped = 0;
 
-    // Meshlets are fetched kFetch at a time: one contended atomic per kFetch meshlets.
+    // Work items are fetched kFetch at a time: one contended atomic per kFetch items.
     constexpr uint32_t kFetch = 4;
     uint32_t fetchBase = 0, fetchLeft = 0;
     while (true) {
@@ -268,12 +313,28 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs 
             fetchBase = __shfl_sync(0xFFFFFFFFu, b, 0);
             fetchLeft = kFetch;
         }
-        const uint32_t m = fetchBase++;
+        const uint32_t item = fetchBase++;
         fetchLeft--;
-        if (m >= a.count) break;
-        if (a.cullBitmap != nullptr && !((a.cullBitmap[m >> 4] >> (m & 15)) & 1)) continue;  // Shading.cpp:282-289
+        if (item >= totalItems) break;
+        uint32_t m = item, view = 0;
+        if (multi) {
+            uint32_t lo = 0, hi = a.numViews - 1;  // largest view with viewStart <= item
+            while (lo < hi) {
+                uint32_t mid = (lo + hi + 1) >> 1;
+                if (a.viewStart[mid] <= item) lo = mid; else hi = mid - 1;
+            }
+            view = lo;
+            m = item - a.viewStart[lo];
+            if (view != curView) {
+                __syncwarp();
+                ((uint32_t*)&S.view)[lane] = ((const uint32_t*)&a.views[view])[lane];
+                __syncwarp();
+                curView = view;
+            }
+        }
+        if (vp.cullBitmap != nullptr && !((vp.cullBitmap[m >> 4] >> (m & 15)) & 1)) continue;  // Shading.cpp:282-289
 
-        const uint32_t g = a.meshletOffset + m;
+        const uint32_t g = vp.meshletOffset + m;
         const uint8_t* mp = a.meshlets + (size_t)g * kMeshletSize;
         const uint32_t hdr = *(const uint32_t*)(mp + kOffNumVertices);
         const uint32_t matId = *(const uint32_t*)(mp + kOffMaterialId);
@@ -291,15 +352,15 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs 
             float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
             if (v < nvr) {
                 float x = P[v], y = P[64 + v], z = P[128 + v];
-                c.x = ffma(x, a.m[0], ffma(y, a.m[4], ffma(z, a.m[8], a.m[12])));
-                c.y = ffma(x, a.m[1], ffma(y, a.m[5], ffma(z, a.m[9], a.m[13])));
-                c.z = ffma(x, a.m[2], ffma(y, a.m[6], ffma(z, a.m[10], a.m[14])));
-                c.w = ffma(x, a.m[3], ffma(y, a.m[7], ffma(z, a.m[11], a.m[15])));
+                c.x = ffma(x, vp.m[0], ffma(y, vp.m[4], ffma(z, vp.m[8], vp.m[12])));
+                c.y = ffma(x, vp.m[1], ffma(y, vp.m[5], ffma(z, vp.m[9], vp.m[13])));
+                c.z = ffma(x, vp.m[2], ffma(y, vp.m[6], ffma(z, vp.m[10], vp.m[14])));
+                c.w = ffma(x, vp.m[3], ffma(y, vp.m[7], ffma(z, vp.m[11], vp.m[15])));
             }
             pos[v] = c;
         }
         const uint32_t* I = (const uint32_t*)(mp + kOffIndices);
-        for (uint32_t k = lane; k < 96; k += 32) sIdx[warp][k] = I[k];
+        for (uint32_t k = lane; k < 96; k += 32) S.idx[k] = I[k];
         __syncwarp();
 
         for (uint32_t base = 0; base < nt; base += 32) {
@@ -325,7 +386,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs 
                 oc |= (q.z > q.w) ? 32u : 0u;
                 partial |= oc;
                 combined &= oc;
-                trivial = trivial && (fabsf(q.x) < fmul(q.w, a.bx) && fabsf(q.y) < fmul(q.w, a.by));
+                trivial = trivial && (fabsf(q.x) < fmul(q.w, vp.bx) && fabsf(q.y) < fmul(q.w, vp.by));
             }
             if (partial & 0x30u) trivial = false;
             const bool accept = valid && combined == 0;
@@ -338,9 +399,9 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs 
             if (acc) {
                 Setup t;
                 uint32_t bbMin, bbMax;
-                if (tri_setup(v0, v1, v2, a.halfW, a.halfH, cullMode, t, bbMin, bbMax)) {
+                if (tri_setup(v0, v1, v2, vp.halfW, vp.halfH, cullMode, t, bbMin, bbMax)) {
                     TriRec r;
-                    edge_setup(t, a.halfW, a.halfH, bbMin, bbMax, make_rank(g, p, 0, 0), r);
+                    edge_setup(t, vp.halfW, vp.halfH, bbMin, bbMax, make_rank(g, p, 0, 0), r);
                     nRaster++;
                     const int tilesX = ((bbMax & 0xFFFF) - (bbMin & 0xFFFF)) >> 2;
                     const int tilesY = ((bbMax >> 16) - (bbMin >> 16)) >> 2;
@@ -349,13 +410,16 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs 
                         r.pad = (uint32_t)tilesX | ((uint32_t)((256 + tilesX - 1) / tilesX) << 8);
                         tris[lane] = r;
                         myTiles = tilesX * tilesY;
-                    } else if (!enqueue_big(r, a)) {
-                        tris[lane] = r;
-                        overflow = true;
+                    } else {
+                        r.pad = view;
+                        if (!enqueue_big(r, a, chunk)) {
+                            tris[lane] = r;
+                            overflow = true;
+                        }
                     }
                 }
             }
-            if (nontriv && a.clipMode) clip_and_queue(v0, v1, v2, partial, a, cullMode, g, p, nRaster);
+            if (nontriv && a.clipMode) clip_and_queue(v0, v1, v2, partial, a, vp, view, chunk, cullMode, g, p, nRaster);
             __syncwarp();
 
             // Small triangles: the warp walks the concatenated tile lists of all of them, two
@@ -368,7 +432,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs 
             }
             const int excl = incl - myTiles;
             const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-            const uint32_t fx = lane & 3, fy = (lane >> 2) & 3, half = lane >> 4;
+            const uint32_t half = lane >> 4;
             for (int b = 0; b < total; b += 2) {
                 const unsigned m0 = __ballot_sync(0xFFFFFFFFu, incl > b);
                 const unsigned m1 = __ballot_sync(0xFFFFFFFFu, incl > b + 1);
@@ -379,7 +443,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs 
                     const int tile = b + (int)half - ownerExcl;
                     const int tilesX = r.pad & 0xFF, magic = r.pad >> 8;
                     const int ty = (tile * magic) >> 8, tx = tile - ty * tilesX;
-                    shade_fragment(r, (r.bbMin & 0xFFFF) + tx * 4 + fx, (r.bbMin >> 16) + ty * 4 + fy, a.keys, a.width);
+                    shade_tile_pixel(r, (r.bbMin & 0xFFFF) + tx * 4, (r.bbMin >> 16) + ty * 4, lane & 15, vp.keys, vp.width);
                 }
             }
             // Triangles the full queue turned away are rasterized here by the whole warp.
@@ -390,7 +454,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs 
                 const TriRec r = tris[src];
                 const uint32_t x0 = r.bbMin & 0xFFFF, y0 = r.bbMin >> 16;
                 raster_region(r, x0, y0, (int)(((r.bbMax & 0xFFFF) - x0) >> 2), (int)(((r.bbMax >> 16) - y0) >> 2),
-                              a.keys, a.width, lane);
+                              vp.keys, vp.width, lane);
             }
             __syncwarp();
         }
@@ -405,9 +469,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32) k_draw_meshlets(DrawArgs 
     }
 }
 
+// Chunk stage: warps take chunk-sized pieces (chunk x chunk tiles) of queued triangles; a queued
+// triangle carries its view in pad (batched draws) or belongs to the single view.
 __global__ void __launch_bounds__(256) k_raster_big(const TriRec* __restrict__ big, const unsigned long long* __restrict__ bigBase,
                                                     const unsigned long long* control, uint32_t capacity,
-                                                    unsigned long long* keys, uint32_t width) {
+                                                    unsigned long long* keys, uint32_t width,
+                                                    const ViewParams* __restrict__ views, uint32_t chunk) {
     const unsigned long long q = control[1];
     const uint32_t n = (uint32_t)min((unsigned long long)capacity, q >> 40);
     if (n == 0) return;
@@ -415,8 +482,8 @@ __global__ void __launch_bounds__(256) k_raster_big(const TriRec* __restrict__ b
     const TriRec& last = big[n - 1];
     const int lastTX = (int)(((last.bbMax & 0xFFFF) - (last.bbMin & 0xFFFF)) >> 2);
     const int lastTY = (int)(((last.bbMax >> 16) - (last.bbMin >> 16)) >> 2);
-    const unsigned long long total = bigBase[n - 1] + (unsigned long long)((lastTX + kChunkTiles - 1) / kChunkTiles) *
-                                                          ((lastTY + kChunkTiles - 1) / kChunkTiles);
+    const unsigned long long total = bigBase[n - 1] + (unsigned long long)((lastTX + chunk - 1) / chunk) *
+                                                          ((lastTY + chunk - 1) / chunk);
     const unsigned long long nWarps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
     for (unsigned long long w = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < total; w += nWarps) {
         // largest slot with bigBase[slot] <= w
@@ -426,14 +493,17 @@ __global__ void __launch_bounds__(256) k_raster_big(const TriRec* __restrict__ b
             if (bigBase[mid] <= w) lo = mid; else hi = mid - 1;
         }
         const TriRec r = big[lo];
+        unsigned long long* vkeys = keys;
+        uint32_t vwidth = width;
+        if (views) vkeys = views[r.pad].keys, vwidth = views[r.pad].width;
         const uint32_t c = (uint32_t)(w - bigBase[lo]);
         const uint32_t minX = r.bbMin & 0xFFFF, minY = r.bbMin >> 16, maxX = r.bbMax & 0xFFFF, maxY = r.bbMax >> 16;
-        const uint32_t chunksX = (((maxX - minX) >> 2) + kChunkTiles - 1) / kChunkTiles;
+        const uint32_t chunksX = (((maxX - minX) >> 2) + chunk - 1) / chunk;
         const uint32_t cy = c / chunksX, cx = c - cy * chunksX;
-        const uint32_t x0 = minX + cx * (kChunkTiles * 4), y0 = minY + cy * (kChunkTiles * 4);
-        const uint32_t x1 = min(x0 + kChunkTiles * 4, maxX), y1 = min(y0 + kChunkTiles * 4, maxY);
+        const uint32_t x0 = minX + cx * (chunk * 4), y0 = minY + cy * (chunk * 4);
+        const uint32_t x1 = min(x0 + chunk * 4, maxX), y1 = min(y0 + chunk * 4, maxY);
         // Empty tiles of the chunk are rejected by their corner samples inside raster_region.
-        raster_region(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), keys, width, lane);
+        raster_region(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys, vwidth, lane);
     }
 }
 
@@ -490,13 +560,23 @@ static int grid_for(uint32_t n, int perThread, int block) {
 }
 
 void launch_draw(const DrawArgs& a, cudaStream_t st, int numSMs) {
+    const uint32_t warps = a.warpsPerBlock ? a.warpsPerBlock : kWarpsPerBlock;
+    const size_t smem = warps * sizeof(WarpSmem);
+    static size_t s_smemSet = 0;
+    if (smem > s_smemSet && smem > 48 * 1024) {
+        cudaFuncSetAttribute(k_draw_meshlets, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        s_smemSet = smem;
+    }
+    const uint32_t chunk = a.chunkTiles ? a.chunkTiles : kChunkTiles;
     {
+        // 64 registers a thread (launch bounds) leave room for 32 resident warps per SM
         LaunchScope ls("k_draw_meshlets", st);
-        k_draw_meshlets<<<numSMs * 4, kWarpsPerBlock * 32, 0, st>>>(a);
+        k_draw_meshlets<<<numSMs * (32 / warps), warps * 32, smem, st>>>(a);
     }
     {
         LaunchScope ls("k_raster_big", st);
-        k_raster_big<<<numSMs * 8, 256, 0, st>>>(a.s.big, a.s.bigBase, a.s.control, a.s.bigCapacity, a.keys, a.width);
+        k_raster_big<<<numSMs * 8, 256, 0, st>>>(a.s.big, a.s.bigBase, a.s.control, a.s.bigCapacity, a.keys, a.width,
+                                                 a.views, chunk);
     }
 }
 

@@ -320,6 +320,44 @@ def grid_scene(n_side: int = 32, width: int = 1280, height: int = 720, seed: int
     return Scene(m, mats, texture_size, 1, [view], texture_seed=seed, name=f"grid{n}@{width}x{height}")
 
 
+def _round4(v: float) -> int:
+    return max(4, int(round(v / 4.0)) * 4)
+
+
+def multiview_scene(n: int = 200_000, n_cameras: int = 58, seed: int = 3, cube_size: int = 1024,
+                    min_res=(256, 256), max_res=(2560, 1440)) -> Scene:
+    """Batched multi-view workload: n meshlets of the grid construction (spacing 1, radius 1,
+    random yaw) seen by 6 depth-only cube-face views (cube_size^2, 90 degrees) from a point above the
+    grid's centre plus n_cameras cameras at random positions and heights whose resolutions are
+    drawn log-uniformly between min_res and max_res (rounded to multiples of 4)."""
+    rng = np.random.default_rng(seed)
+    side = int(math.ceil(math.sqrt(n)))
+    g = np.arange(side) - (side - 1) / 2.0
+    gx, gz = np.meshgrid(g, g)
+    centers = np.stack([gx.ravel(), np.zeros(gx.size), gz.ravel()], axis=1)[:n]
+    m = build_meshlets(centers, np.ones(n), rng.uniform(0, 2 * math.pi, n), np.zeros(n, np.int64), rng)
+    mats = np.zeros(1, dtype=MATERIAL_DTYPE)
+    mats["alpha_cutoff"] = 255
+    views = []
+    eye = np.array([0.0, 3.0, 0.0])
+    faces = [((1, 0, 0), (0, 1, 0)), ((-1, 0, 0), (0, 1, 0)), ((0, 1, 0), (0, 0, 1)), ((0, -1, 0), (0, 0, 1)),
+             ((0, 0, 1), (0, 1, 0)), ((0, 0, -1), (0, 1, 0))]
+    for d, up in faces:
+        v = View(cube_size, cube_size, look_at(eye, eye + np.array(d), up), proj_reversed_z(90.0, 1.0, 0.1),
+                 eye.astype(np.float32), depth_only=True)
+        views.append(v)
+    half = side / 2.0
+    for _ in range(n_cameras):
+        w = _round4(math.exp(rng.uniform(math.log(min_res[0]), math.log(max_res[0]))))
+        h = _round4(math.exp(rng.uniform(math.log(min_res[1]), math.log(max_res[1]))))
+        height = math.exp(rng.uniform(math.log(1.5), math.log(80.0)))
+        e = np.array([rng.uniform(-half, half), height, rng.uniform(-half, half)])
+        yaw, pitch = rng.uniform(0, 2 * math.pi), math.radians(rng.uniform(-70, -8))
+        d = np.array([math.cos(pitch) * math.cos(yaw), math.sin(pitch), math.cos(pitch) * math.sin(yaw)])
+        views.append(make_view(w, h, eye=e, target=e + d))
+    return Scene(m, mats, 0, 1, views, name=f"multiview{n}x{len(views)}")
+
+
 def volume_scene(n: int = 100_000, width: int = 1920, height: int = 1080, n_materials: int = 64,
                  seed: int = 2, texture_size: int = 2048, extent: float = 100.0,
                  env_size: int = 1024) -> Scene:

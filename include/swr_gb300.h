@@ -145,6 +145,32 @@ swr_status swr_draw_meshlets_noalloc(const void* meshlets, uint32_t meshlet_offs
                                      uint32_t* surface_ids, float* depth, uint32_t width, uint32_t height,
                                      int enable_binning, int enable_clipping, int enable_guardband);
 
+/* ---- Batched multi-view rendering (no reference counterpart: the reference issues one
+ * DrawMeshlets per view, Main.cpp:216-245) ----
+ * A batch renders the meshlets [first, first+count) of a scene into many framebuffers of any
+ * sizes. Each view's result equals, bit for bit, swr_framebuffer_clear(fb, 0xFF000000, 0) +
+ * swr_cull_meshlets (frustum only, when frustum_cull) + swr_draw_meshlets with the rasterizer's
+ * flags. The frame runs as one CUDA graph (batched clear, batched cull, one persistent mesh-stage
+ * launch over every (view, meshlet), the chunk rasterizer, batched finalize), captured at the first
+ * render and replayed on the calling thread's stream. */
+typedef struct swr_batch_t* swr_batch;
+typedef struct {
+    swr_framebuffer fb;
+    float proj[16], view[16], model[16];   /* object_to_clip = proj * view * model */
+    uint32_t depth_only;                   /* keep only the depth layer (shadow-map style views) */
+} swr_view_desc;
+swr_status swr_batch_create(swr_rasterizer r, swr_scene s, uint32_t first, uint32_t count, const swr_view_desc* views,
+                            uint32_t num_views, int frustum_cull, swr_batch* out);
+/* New matrices for the same framebuffers (takes effect at the next render; no re-capture). */
+swr_status swr_batch_set_views(swr_batch b, const swr_view_desc* views, uint32_t num_views);
+/* Chunk (bin) edge in 4x4 tiles: 2, 4, 8, 16 (8-64 pixels); warps per mesh-stage block: 4, 8, 16;
+ * 0 = default (8, 8). Changing them re-captures the graph at the next render. */
+swr_status swr_batch_set_tuning(swr_batch b, uint32_t chunk_tiles, uint32_t warps_per_block);
+swr_status swr_batch_render(swr_batch b);
+swr_status swr_batch_get_counters(swr_batch b, uint64_t out[SWR_NUM_COUNTERS]);
+swr_status swr_batch_reset_counters(swr_batch b);
+swr_status swr_batch_destroy(swr_batch b);
+
 /* ---- Framebuffer (Rasterizer.h:10-78, ImageHelpers.cpp:109-147) ---- */
 /* CreateFramebuffer(width, height, numLayers): width/height multiples of 4, at most 2896. */
 swr_status swr_framebuffer_create(uint32_t width, uint32_t height, uint32_t num_layers, swr_framebuffer* out);
