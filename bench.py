@@ -52,6 +52,11 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-multiview", action="store_true")
     p.add_argument("--multiview-meshlets", type=int, default=200_000)
+    p.add_argument("--no-neural", action="store_true")
+    p.add_argument("--neural-steps", type=int, default=20_000)
+    p.add_argument("--neural-batch", type=int, default=65536)
+    p.add_argument("--neural-level-weighting", type=int, default=1, choices=[0, 1, 2],
+                   help="training texture level l drawn with weight 2^(w*(5-l)): 2 by texel count, 1 by edge, 0 uniform")
     return p.parse_args()
 
 
@@ -92,7 +97,7 @@ def make_gpu_textures(sc, api):
     for i in range(len(sc.materials)):
         t = api.Texture2D(api.FORMAT_RGBA8U, sc.texture_size, sc.texture_size, 16, 2)
         for layer in range(2):
-            px = scenes.value_noise_rgba_torch(sc.texture_size, sc.texture_seed + i, layer=layer)
+            px = scenes.value_noise_rgba_torch(sc.texture_size, sc.texture_seed + i, layer=layer, detail=sc.texture_detail)
             t.set_pixels_device(px, layer)
             torch.cuda.synchronize()
         t.generate_mips()
@@ -174,7 +179,8 @@ def oracle_textures_from_host(sc):
         t = O.Texture(sc.texture_size, sc.texture_size, 16, 2)
         for layer in range(2):
             # torch on the CPU (multi-threaded) computes the same texels as scenes.value_noise_rgba
-            px = scenes.value_noise_rgba_torch(sc.texture_size, sc.texture_seed + i, layer=layer, device="cpu")
+            px = scenes.value_noise_rgba_torch(sc.texture_size, sc.texture_seed + i, layer=layer, device="cpu",
+                                               detail=sc.texture_detail)
             t.set_pixels(px.numpy().view(np.uint32), layer)
         t.generate_mips()
         data.append(t.data.copy())
@@ -321,6 +327,106 @@ def multiview_section(args, api, stream):
             "triangles_processed": int(c[0]), "gtri_per_s": float(c[0]) / (batched_ms / 1e3) / 1e9}
 
 
+# ----------------------------------------------------------------------------- learned decoder
+def neural_section(args, api, stream, sc, texs, env, scene, rast, lights):
+    """Learned texture decoder over the scene's 64 materials: trained on the device (Adam, lr 1e-3,
+    `neural_steps` steps of `neural_batch` texels spread over 8 materials per step), then the scene
+    is resolved at 2560x1440 with the plain sampler and with the decoder (texture levels 0-3 decoded,
+    coarser levels sampled), from the headline camera and from a camera inside the volume where
+    more pixels use the decoded levels. Reports training time and loss, both resolves' device time,
+    PSNR / max-abs of the neural frame against the plain frame, decoded texels and memory."""
+    import torch
+
+    from glimpsw_gb300 import scenes
+    model = api.NeuralMaterials(texs, latent_levels=4, seed=1)
+    mps, lw = 8, args.neural_level_weighting
+    loss0 = model.train(1, batch=args.neural_batch, materials_per_step=mps, want_loss=True, level_weighting=lw)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    model.train(max(args.neural_steps - 2, 0), batch=args.neural_batch, materials_per_step=mps, level_weighting=lw)
+    b.record(stream)
+    loss1 = model.train(1, batch=args.neural_batch, materials_per_step=mps, want_loss=True, level_weighting=lw)
+    train_ms = a.elapsed_time(b)
+    api.profile_enable(True)
+    api.profile_collect()
+    model.train(4, batch=args.neural_batch, materials_per_step=mps, level_weighting=lw)
+    step_kernels = {}
+    for k, t in api.profile_collect():
+        step_kernels[k] = step_kernels.get(k, 0.0) + t / 4
+    api.profile_enable(False)
+    W, H = 2560, 1440
+    n = len(sc.meshlets)
+    batches = [(off, min(BATCH, n - off)) for off in range(0, n, BATCH)]
+    bms = [torch.zeros((cnt + 15) // 16, dtype=torch.int16, device="cuda") for _, cnt in batches]
+    fbs = [api.Framebuffer(W, H, 3), api.Framebuffer(W, H, 3)]
+    eye = sc.views[0].eye
+    cams = {"headline_camera": scenes.make_view(W, H, eye=eye, target=(0.0, 0.0, 0.0)),
+            "interior_camera": scenes.make_view(W, H, eye=(3.0, 2.0, -20.0), target=(0.0, 0.0, 40.0))}
+
+    def render(fb, view):
+        fb.clear(0xFF000000, 0.0)
+        for (off, cnt), bm in zip(batches, bms):
+            api.cull_meshlets(scene, off, cnt, bm, view.proj, view.view, scenes.IDENTITY, view.view, W, H, None)
+            rast.draw_meshlets(fb, cnt, api.ShadingContext(scene, view.world_to_clip, meshlet_offset=off, cull_bitmap=bm))
+
+    out = {"training": {"steps": args.neural_steps, "batch": args.neural_batch, "materials_per_step": mps,
+                        "level_weighting": lw,
+                        "lr": 1e-3, "loss_first_step": loss0, "loss_last_step": loss1, "train_ms": train_ms,
+                        "ms_per_step": train_ms / max(args.neural_steps - 2, 1),
+                        "step_kernels_ms": {k: round(v, 4) for k, v in step_kernels.items()},
+                        "samples_per_s": (args.neural_steps - 2) * args.neural_batch / (train_ms / 1e3)}}
+    mem = model.memory()
+    neural_bytes = mem["latent_bytes"] + mem["weight_bytes"] + mem["fallback_bytes"]
+    out["memory"] = {**mem, "neural_total_bytes": neural_bytes, "ratio_plain_over_neural": mem["plain_bytes"] / neural_bytes}
+    for name, view in cams.items():
+        ctx = api.ShadingContext(scene, view.world_to_clip, world_to_clip=view.world_to_clip, skybox=env,
+                                 view_pos=view.eye, lights=lights)
+        ms = {"plain": [], "neural": []}
+        for i in range(args.warmup + args.steps):
+            for kind, fb in zip(("plain", "neural"), fbs):
+                render(fb, view)
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                if kind == "plain":
+                    ctx.resolve(rast, fb)
+                else:
+                    ctx.resolve_neural(rast, fb, model)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                if i >= args.warmup:
+                    ms[kind].append(e0.elapsed_time(e1))
+        render(fbs[1], view)
+        depth = fbs[1].get_pixels(1)
+        covered = int((depth != 0).sum())
+        requests, tiles, per_level = ctx.resolve_neural(rast, fbs[1], model, want_stats=True)
+        render(fbs[0], view)
+        ctx.resolve(rast, fbs[0])
+        pa = fbs[0].get_pixels(0).view(np.uint8).reshape(H, W, 4)[..., :3].astype(np.float64) / 255.0
+        pb = fbs[1].get_pixels(0).view(np.uint8).reshape(H, W, 4)[..., :3].astype(np.float64) / 255.0
+        diff = np.abs(pa - pb)
+        mse = float((diff ** 2).mean())
+        cov = (depth != 0)
+        mse_cov = float((diff[cov] ** 2).mean()) if covered else 0.0
+        out[name] = {"plain_resolve_ms": float(np.median(ms["plain"])), "neural_resolve_ms": float(np.median(ms["neural"])),
+                     "psnr_db": 10 * np.log10(1.0 / mse) if mse > 0 else float("inf"),
+                     "psnr_covered_pixels_db": 10 * np.log10(1.0 / mse_cov) if mse_cov > 0 else float("inf"),
+                     "max_abs_255": int(round(diff.max() * 255)), "pixels_differing": int((diff.max(axis=2) > 0).sum()),
+                     "covered_pixels": covered, "decoded_texels": int(requests), "decode_tiles": int(tiles),
+                     "decoded_texels_per_level": [int(v) for v in per_level],
+                     "plain_gpix_per_s": W * H / (np.median(ms["plain"]) / 1e3) / 1e9,
+                     "neural_gpix_per_s": W * H / (np.median(ms["neural"]) / 1e3) / 1e9}
+    api.profile_enable(True)
+    render(fbs[1], cams["interior_camera"])
+    ctx = api.ShadingContext(scene, cams["interior_camera"].world_to_clip, world_to_clip=cams["interior_camera"].world_to_clip,
+                             skybox=env, view_pos=cams["interior_camera"].eye, lights=lights)
+    api.profile_collect()
+    ctx.resolve_neural(rast, fbs[1], model)
+    out["interior_camera"]["neural_kernels_ms"] = {k: round(t, 4) for k, t in api.profile_collect()}
+    api.profile_enable(False)
+    return out
+
+
 # ----------------------------------------------------------------------------- GPU
 def run_ours(args):
     import torch
@@ -448,9 +554,12 @@ def run_ours(args):
         if i >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
 
+    del pinned, host_img
+    neural = None
+    if not args.no_neural:
+        neural = neural_section(args, api, stream, sc, texs, env, scene, rast, lights)
     multiview = None
     if not args.no_multiview:
-        del pinned, host_img
         multiview = multiview_section(args, api, stream)
 
     cpu = None
@@ -479,7 +588,7 @@ def run_ours(args):
                 "e2e": {"value": float(np.median(e2e_ms)), "unit": UNIT, "h2d_bytes_per_step": int(sc.meshlets.nbytes),
                         "d2h_bytes_per_step": int(W * H * 4)},
                 "gpu_launches": int(launches), "clocks": clocks.summary(), "cpu_baseline": cpu,
-                "multiview": multiview}
+                "multiview": multiview, "neural": neural}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

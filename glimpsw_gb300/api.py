@@ -102,6 +102,17 @@ _SIGS = {
     "swr_batch_get_counters": [C.c_void_p, C.c_void_p],
     "swr_batch_reset_counters": [C.c_void_p],
     "swr_batch_destroy": [C.c_void_p],
+    "swr_neural_create": [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64, C.c_void_p],
+    "swr_neural_destroy": [C.c_void_p],
+    "swr_neural_get_info": [C.c_void_p, C.c_void_p],
+    "swr_neural_train": [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_float, C.c_void_p],
+    "swr_neural_gradients": [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p],
+    "swr_neural_get_params": [C.c_void_p, C.c_uint32, C.c_void_p],
+    "swr_neural_set_params": [C.c_void_p, C.c_uint32, C.c_void_p],
+    "swr_neural_get_latents": [C.c_void_p, C.c_uint32, C.c_void_p],
+    "swr_neural_set_latents": [C.c_void_p, C.c_uint32, C.c_void_p],
+    "swr_neural_decode": [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p],
+    "swr_resolve_neural": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
 }
 
 
@@ -323,6 +334,14 @@ class ShadingContext:
     def resolve(self, rast: "Rasterizer", fb: Framebuffer) -> None:
         _check(_lib.swr_resolve(rast.h, fb.h, C.byref(self.s)))
 
+    def resolve_neural(self, rast: "Rasterizer", fb: Framebuffer, model: "NeuralMaterials",
+                       want_stats: bool = False):
+        """resolve() with the texture levels the model covers decoded by its network; returns
+        (texels decoded, 128-texel tiles) when want_stats (synchronises)."""
+        st = SwrNeuralStats()
+        _check(_lib.swr_resolve_neural(rast.h, fb.h, C.byref(self.s), model.h, C.byref(st) if want_stats else None))
+        return (st.requests, st.tiles, list(st.level_texels)) if want_stats else None
+
 
 def cull_meshlets(scene: Scene, first: int, count: int, bitmap_device, proj, view, model, prev_view,
                   frame_w: float, frame_h: float, depth_map: Texture2D | None = None, want_count: bool = False):
@@ -448,3 +467,97 @@ class Rasterizer:
 
     def reset_counters(self) -> None:
         _check(_lib.swr_rasterizer_reset_counters(self.h))
+
+
+# ---------------------------------------------------------------- learned texture decoder
+NEURAL_PARAMS = 5704
+
+
+class SwrNeuralInfo(C.Structure):
+    _fields_ = [("num_materials", C.c_uint32), ("latent_levels", C.c_uint32), ("texels_per_material", C.c_uint32),
+                ("level_offset", C.c_uint32 * 4), ("level_width", C.c_uint32 * 4), ("level_height", C.c_uint32 * 4),
+                ("latent_bytes", C.c_uint64), ("weight_bytes", C.c_uint64), ("fallback_bytes", C.c_uint64),
+                ("plain_bytes", C.c_uint64)]
+
+
+class SwrNeuralStats(C.Structure):
+    _fields_ = [("requests", C.c_uint32), ("tiles", C.c_uint32), ("level_texels", C.c_uint32 * 6)]
+
+
+def pack_texel(level, x, y):
+    """Packed texel address used by the decoder entry points: level<<28 | y<<14 | x."""
+    return (np.asarray(level, dtype=np.uint32) << 28) | (np.asarray(y, dtype=np.uint32) << 14) | np.asarray(x, dtype=np.uint32)
+
+
+class NeuralMaterials:
+    """Learned texture decoder over a set of material textures (no counterpart in the reference):
+    per material an FP16 latent pyramid (8 channels; latent level k has texture level k+2's size)
+    and an 11->64->64->8 GELU MLP (latents, bias, level-0/1 flags) decoding texture levels
+    0..latent_levels+1, trained on the device by tensor-core kernels."""
+
+    def __init__(self, textures: list, latent_levels: int = 4, seed: int = 1):
+        L = load_library()
+        arr = (C.c_void_p * len(textures))(*[t.h.value if t is not None else None for t in textures])
+        h = C.c_void_p()
+        _check(L.swr_neural_create(arr, len(textures), latent_levels, C.c_uint64(seed), C.byref(h)))
+        self.h = h
+        self._textures = list(textures)
+        info = SwrNeuralInfo()
+        _check(L.swr_neural_get_info(h, C.byref(info)))
+        self.info = info
+        self.num_materials = info.num_materials
+        self.latent_levels = info.latent_levels
+        self.texels_per_material = info.texels_per_material
+        self.level_offset = list(info.level_offset)[:latent_levels]
+        self.level_size = [(info.level_width[l], info.level_height[l]) for l in range(latent_levels)]
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.swr_neural_destroy(self.h)
+            self.h = None
+
+    def memory(self) -> dict:
+        i = self.info
+        return {"latent_bytes": i.latent_bytes, "weight_bytes": i.weight_bytes, "fallback_bytes": i.fallback_bytes,
+                "plain_bytes": i.plain_bytes}
+
+    def train(self, steps: int, batch: int = 65536, materials_per_step: int = 8, lr: float = 1e-3,
+              want_loss: bool = False, level_weighting: int = 1):
+        """level_weighting w: texture level l drawn with weight 2^(w * (latent_levels+1-l)); 2 = by
+        texel count, 1 = by edge length, 0 = uniform."""
+        loss = C.c_float(0.0)
+        _check(_lib.swr_neural_train(self.h, steps, batch, materials_per_step, level_weighting, C.c_float(lr),
+                                     C.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
+
+    def gradients(self, material: int, samples_device, count: int, want_latent: bool = True):
+        """(param_grad[5704], latent_grad[texels, 8] or None, summed squared error) for explicit samples."""
+        pg = np.zeros(NEURAL_PARAMS, dtype=np.float32)
+        lg = np.zeros((self.texels_per_material, 8), dtype=np.float32) if want_latent else None
+        loss = C.c_float(0.0)
+        _check(_lib.swr_neural_gradients(self.h, material, _ptr(samples_device), count, pg.ctypes.data,
+                                         lg.ctypes.data if lg is not None else None, C.byref(loss)))
+        return pg, lg, loss.value
+
+    def get_params(self, material: int) -> np.ndarray:
+        p = np.zeros(NEURAL_PARAMS, dtype=np.float32)
+        _check(_lib.swr_neural_get_params(self.h, material, p.ctypes.data))
+        return p
+
+    def set_params(self, material: int, params: np.ndarray) -> None:
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        assert p.size == NEURAL_PARAMS
+        _check(_lib.swr_neural_set_params(self.h, material, p.ctypes.data))
+
+    def get_latents(self, material: int) -> np.ndarray:
+        p = np.zeros((self.texels_per_material, 8), dtype=np.float32)
+        _check(_lib.swr_neural_get_latents(self.h, material, p.ctypes.data))
+        return p
+
+    def set_latents(self, material: int, latents: np.ndarray) -> None:
+        p = np.ascontiguousarray(latents, dtype=np.float32)
+        assert p.size == self.texels_per_material * 8
+        _check(_lib.swr_neural_set_latents(self.h, material, p.ctypes.data))
+
+    def decode(self, material: int, texels_device, count: int, out_device) -> None:
+        _check(_lib.swr_neural_decode(self.h, material, _ptr(texels_device), count, _ptr(out_device)))

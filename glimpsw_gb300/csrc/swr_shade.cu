@@ -15,11 +15,13 @@
 #include <algorithm>
 #include <cfloat>
 #include <cstring>
+#include <string>
 #include <vector>
 
 #include "../../include/swr/hostmath.h"
 #include "swr_device.cuh"
 #include "swr_internal.h"
+#include "swr_neural.h"
 
 namespace swr {
 namespace {
@@ -182,6 +184,18 @@ struct ResolveArgs {
     int hasSky;
 };
 
+// Neural resolve: the emit pass records, per pixel, the texels of the levels the model decodes
+// (4 slots: the nearest texel, or the bilinear quad's 00 10 01 11 texels; ~0 = none) and counts
+// them per material; the shade pass reads the decoded texels from the same slots.
+enum { kResolvePlain = 0, kResolveEmit = 1, kResolveNeural = 2 };
+struct NeuralResolve {
+    const DevTexture* tex;             // model textures (data == nullptr: not decoded)
+    uint32_t numMaterials, decodedLevels;  // texture levels below decodedLevels are decoded
+    unsigned long long* pixelReq;      // [pixel * 4 + k] material<<32 | level<<28 | ty<<14 | tx
+    uint32_t* counts;                  // [material]
+    const uint2* decoded;              // [pixel * 4 + k] layer-0 RGBA8, layer-1 RGBA8
+};
+
 __device__ __forceinline__ uint32_t lerp16(uint32_t a, uint32_t b, uint32_t t) {
     uint32_t r = 0;
 #pragma unroll
@@ -207,26 +221,48 @@ __device__ __forceinline__ F3 unmap_oct(float u, float v) {
     return normalize3(n);
 }
 
-// SampleLevel<SurfaceSampler> for one lane once the tile's filter is known (Texture.h:412-459).
-__device__ uint32_t sample_rgba8(const DevTexture& t, float u, float v, int layer, int32_t mipIn, bool nearest) {
-    int32_t ix = round2i(u * t.scale_lerp_u) & t.mask_lerp_u;
-    int32_t iy = round2i(v * t.scale_lerp_v) & t.mask_lerp_v;
-    int32_t m = min(max(mipIn, 0), (int32_t)t.mip_levels - 1);
-    int32_t stride = (int32_t)t.row_shift - m;
-    ix >>= m, iy >>= m;
-    const uint32_t* base = t.data + (size_t)layer * t.layer_stride + t.mip_offsets[m & 15];
-    if (nearest) return base[texel_offset(ix >> 8, iy >> 8, stride)];
-    int32_t xf = max(ix - 127, 0), yf = max(iy - 127, 0);
-    int32_t tx = xf >> 8, ty = yf >> 8;
-    bool inX = ((tx + 1) << m) < (int32_t)t.width, inY = ((ty + 1) << m) < (int32_t)t.height;
-    uint32_t i00 = texel_offset(tx, ty, stride), i01 = texel_offset(tx, ty + (inY ? 1 : 0), stride);
-    uint32_t d00 = base[i00], d10 = base[i00 + 8], d01 = base[i01], d11 = base[i01 + 8];
-    uint32_t fx = (uint32_t)(xf & 255) << 7, fy = (uint32_t)(yf & 255) << 7;
-    fx = (fx << 16) | fx, fy = (fy << 16) | fy;
-    if (!inX) fx = 0;
+// Bilinear blend of four RGBA8 texels with 1.15 fixed-point weights (the 16-bit lane lerps of
+// SampleLevel<SurfaceSampler>, Texture.h:440-456).
+__device__ __forceinline__ uint32_t filter_rgba8(uint32_t d00, uint32_t d10, uint32_t d01, uint32_t d11, uint32_t fx, uint32_t fy) {
     uint32_t rb1 = lerp16(d00 & 0x00FF00FF, d10 & 0x00FF00FF, fx), ga1 = lerp16((d00 >> 8) & 0x00FF00FF, (d10 >> 8) & 0x00FF00FF, fx);
     uint32_t rb2 = lerp16(d01 & 0x00FF00FF, d11 & 0x00FF00FF, fx), ga2 = lerp16((d01 >> 8) & 0x00FF00FF, (d11 >> 8) & 0x00FF00FF, fx);
     return lerp16(rb1, rb2, fy) | (lerp16(ga1, ga2, fy) << 8);
+}
+
+// The texel coordinates one lane's SampleLevel<SurfaceSampler> reads (Texture.h:412-459): level m,
+// the nearest texel (tx, ty), or for bilinear the top-left texel, whether its right / lower
+// neighbours are inside the level, and the packed 1.15 weights.
+struct TexelQuad {
+    int32_t m, stride, tx, ty;
+    bool inX, inY;
+    uint32_t fx, fy;
+};
+__device__ __forceinline__ TexelQuad texel_quad(const DevTexture& t, float u, float v, int32_t mipIn, bool nearest) {
+    TexelQuad q;
+    int32_t ix = round2i(u * t.scale_lerp_u) & t.mask_lerp_u;
+    int32_t iy = round2i(v * t.scale_lerp_v) & t.mask_lerp_v;
+    q.m = min(max(mipIn, 0), (int32_t)t.mip_levels - 1);
+    q.stride = (int32_t)t.row_shift - q.m;
+    ix >>= q.m, iy >>= q.m;
+    if (nearest) {
+        q.tx = ix >> 8, q.ty = iy >> 8, q.inX = q.inY = false, q.fx = q.fy = 0;
+        return q;
+    }
+    int32_t xf = max(ix - 127, 0), yf = max(iy - 127, 0);
+    q.tx = xf >> 8, q.ty = yf >> 8;
+    q.inX = ((q.tx + 1) << q.m) < (int32_t)t.width, q.inY = ((q.ty + 1) << q.m) < (int32_t)t.height;
+    uint32_t fx = (uint32_t)(xf & 255) << 7, fy = (uint32_t)(yf & 255) << 7;
+    q.fx = q.inX ? ((fx << 16) | fx) : 0u, q.fy = (fy << 16) | fy;
+    return q;
+}
+
+// SampleLevel<SurfaceSampler> for one lane once the tile's filter is known (Texture.h:412-459).
+__device__ uint32_t sample_rgba8(const DevTexture& t, float u, float v, int layer, int32_t mipIn, bool nearest) {
+    const TexelQuad q = texel_quad(t, u, v, mipIn, nearest);
+    const uint32_t* base = t.data + (size_t)layer * t.layer_stride + t.mip_offsets[q.m & 15];
+    if (nearest) return base[texel_offset(q.tx, q.ty, q.stride)];
+    uint32_t i00 = texel_offset(q.tx, q.ty, q.stride), i01 = texel_offset(q.tx, q.ty + (q.inY ? 1 : 0), q.stride);
+    return filter_rgba8(base[i00], base[i00 + 8], base[i01], base[i01 + 8], q.fx, q.fy);
 }
 
 // SampleOctLevel<EnvSampler>(dir, 1) on an R11G11B10 map (Texture.h:467-480; level 1 has no fraction).
@@ -254,7 +290,8 @@ __device__ F3 sample_env(const DevTexture& t, F3 dir) {
     return { ra.x + (rb.x - ra.x) * fy, ra.y + (rb.y - ra.y) * fy, ra.z + (rb.z - ra.z) * fy };
 }
 
-__global__ void __launch_bounds__(256) k_resolve(ResolveArgs a) {
+template <int kMode>
+__global__ void __launch_bounds__(256) k_resolve(ResolveArgs a, NeuralResolve nr) {
     const uint32_t lane = threadIdx.x & 31, l = lane & 15, half = lane >> 4;
     const unsigned hm = 0xFFFFu << (16 * half);
     const uint32_t tilesX = a.width >> 2, numTiles = tilesX * (a.height >> 2);
@@ -279,6 +316,14 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a) {
     const unsigned skyBits = (__ballot_sync(hm, isSky) >> (16 * half)) & 0xFFFF;
 
     F3 color = { 0.f, 0.f, 0.f };
+    unsigned long long req[4] = { ~0ull, ~0ull, ~0ull, ~0ull };
+    if constexpr (kMode == kResolveEmit) {
+        if (skyBits == 0xFFFF) {
+            uint4* dst = (uint4*)(nr.pixelReq + (size_t)off * 4);
+            dst[0] = dst[1] = make_uint4(~0u, ~0u, ~0u, ~0u);
+            return;
+        }
+    }
     if (skyBits != 0xFFFF) {
         // ---- ResolveSurface (Shading.cpp:471-579): waterfall over the tile's surface ids
         F3 pos[3] = {};
@@ -359,9 +404,53 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a) {
             const int32_t mip = ilog2_x86(vmax(ddx2, ddy2)) >> 1;
             const bool nearest = __ballot_sync(hm, mip > 0) & hm;
             if ((iter >> l) & 1) {
-                albedo = sample_rgba8(tex, texU, texV, 0, mip, nearest);
-                if (tex.num_layers >= 2) nmr = sample_rgba8(tex, texU, texV, 1, mip, nearest);
+                if constexpr (kMode == kResolvePlain) {
+                    albedo = sample_rgba8(tex, texU, texV, 0, mip, nearest);
+                    if (tex.num_layers >= 2) nmr = sample_rgba8(tex, texU, texV, 1, mip, nearest);
+                } else {
+                    const TexelQuad q = texel_quad(tex, texU, texV, mip, nearest);
+                    // decoded when the model covers the level and its texture has this texture's size
+                    const bool dec = mid < nr.numMaterials && q.m < (int32_t)nr.decodedLevels && nr.tex[mid].data != nullptr &&
+                                     nr.tex[mid].width == tex.width && nr.tex[mid].height == tex.height;
+                    if constexpr (kMode == kResolveEmit) {
+                        uint32_t nq = 0;
+                        if (dec) {
+                            const unsigned long long b = ((unsigned long long)mid << 32) | ((uint32_t)q.m << 28);
+                            const uint32_t x0 = (uint32_t)q.tx, y0 = (uint32_t)q.ty;
+                            req[0] = b | (y0 << 14) | x0, nq = 1;
+                            if (!nearest) {
+                                if (q.inX) req[1] = b | (y0 << 14) | (x0 + 1), nq++;
+                                if (q.inY) req[2] = b | ((y0 + 1) << 14) | x0, nq++;
+                                if (q.inX && q.inY) req[3] = b | ((y0 + 1) << 14) | (x0 + 1), nq++;
+                            }
+                        }
+                        const unsigned grp = iter << (16 * half);
+                        const uint32_t total = __reduce_add_sync(grp, nq);
+                        if (total && (int)lane == __ffs(grp) - 1) atomicAdd(&nr.counts[mid], total);
+                    } else if (dec) {
+                        const uint2* d = nr.decoded + (size_t)off * 4;
+                        const uint2 d00 = d[0];
+                        uint2 r0 = d00;
+                        if (!nearest) {
+                            const uint2 d10 = q.inX ? d[1] : d00, d01 = q.inY ? d[2] : d00;
+                            const uint2 d11 = q.inY ? (q.inX ? d[3] : d01) : d10;
+                            r0.x = filter_rgba8(d00.x, d10.x, d01.x, d11.x, q.fx, q.fy);
+                            r0.y = filter_rgba8(d00.y, d10.y, d01.y, d11.y, q.fx, q.fy);
+                        }
+                        albedo = r0.x;
+                        if (tex.num_layers >= 2) nmr = r0.y;
+                    } else {
+                        albedo = sample_rgba8(tex, texU, texV, 0, mip, nearest);
+                        if (tex.num_layers >= 2) nmr = sample_rgba8(tex, texU, texV, 1, mip, nearest);
+                    }
+                }
             }
+        }
+        if constexpr (kMode == kResolveEmit) {
+            uint4* dst = (uint4*)(nr.pixelReq + (size_t)off * 4);
+            dst[0] = make_uint4((uint32_t)req[0], (uint32_t)(req[0] >> 32), (uint32_t)req[1], (uint32_t)(req[1] >> 32));
+            dst[1] = make_uint4((uint32_t)req[2], (uint32_t)(req[2] >> 32), (uint32_t)req[3], (uint32_t)(req[3] >> 32));
+            return;
         }
         F3 nrm[3], tan[3];
 #pragma unroll
@@ -467,6 +556,42 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a) {
 }  // namespace swr
 
 using namespace swr;
+
+namespace {
+// ShadingContext::Resolve's per-frame constants (Shading.cpp:658-690); the lights are copied to a
+// stream-ordered device allocation that the caller frees after the launch.
+swr_status build_resolve_args(swr_framebuffer fb, const swr_shading_context* ctx, ResolveArgs& a, const char* fn) {
+    if (!fb || !ctx || !ctx->scene) return swr_internal_fail(SWR_EINVAL, (std::string(fn) + ": NULL argument").c_str());
+    if (ctx->num_lights && !ctx->lights) return swr_internal_fail(SWR_EINVAL, (std::string(fn) + ": lights is NULL").c_str());
+    if (ctx->skybox && ctx->skybox->format != SWR_FORMAT_R11G11B10F)
+        return swr_internal_fail(SWR_EINVAL, (std::string(fn) + ": the skybox must be R11G11B10f").c_str());
+    cudaStream_t st = swr_internal_stream();
+    a = {};
+    a.meshlets = ctx->scene->meshlets;
+    a.numMeshlets = ctx->scene->count;
+    a.materials = ctx->scene->materials;
+    a.numMaterials = ctx->scene->num_materials;
+    a.color = fb->layers;
+    a.depth = (const float*)(fb->layers + fb->layer_stride);
+    a.width = fb->width, a.height = fb->height;
+    memcpy(a.objectToClip, ctx->object_to_clip, sizeof(a.objectToClip));
+    memcpy(a.objectToWorld, ctx->object_to_world, sizeof(a.objectToWorld));
+    if (!swr_hostmath::inverse_screen_proj(ctx->world_to_clip, fb->width, fb->height, a.invProj))
+        return swr_internal_fail(SWR_EINVAL, (std::string(fn) + ": singular world_to_clip").c_str());
+    memcpy(a.viewPos, ctx->view_pos, sizeof(a.viewPos));
+    a.exposure = ctx->exposure;
+    if (ctx->skybox) a.sky = ctx->skybox->d, a.hasSky = 1;
+    if (ctx->num_lights) {
+        swr_light* dl = nullptr;
+        cudaError_t e = cudaMallocAsync(&dl, ctx->num_lights * sizeof(swr_light), st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dl, ctx->lights, ctx->num_lights * sizeof(swr_light), cudaMemcpyHostToDevice, st);
+        if (e != cudaSuccess) return swr_internal_cuda_fail(e, fn);
+        a.lights = dl;
+    }
+    a.numLights = ctx->num_lights;
+    return SWR_OK;
+}
+}  // namespace
 
 extern "C" {
 
@@ -574,44 +699,109 @@ swr_status swr_downsample_depth(swr_framebuffer fb, swr_texture dest) {
 
 swr_status swr_resolve(swr_rasterizer r, swr_framebuffer fb, const swr_shading_context* ctx) {
     (void)r;
-    if (!fb || !ctx || !ctx->scene) return swr_internal_fail(SWR_EINVAL, "swr_resolve: NULL argument");
-    if (ctx->num_lights && !ctx->lights) return swr_internal_fail(SWR_EINVAL, "swr_resolve: lights is NULL");
-    if (ctx->skybox && ctx->skybox->format != SWR_FORMAT_R11G11B10F)
-        return swr_internal_fail(SWR_EINVAL, "swr_resolve: the skybox must be R11G11B10f");
-    cudaStream_t st = swr_internal_stream();
     ResolveArgs a = {};
-    a.meshlets = ctx->scene->meshlets;
-    a.numMeshlets = ctx->scene->count;
-    a.materials = ctx->scene->materials;
-    a.numMaterials = ctx->scene->num_materials;
-    a.color = fb->layers;
-    a.depth = (const float*)(fb->layers + fb->layer_stride);
-    a.width = fb->width, a.height = fb->height;
-    memcpy(a.objectToClip, ctx->object_to_clip, sizeof(a.objectToClip));
-    memcpy(a.objectToWorld, ctx->object_to_world, sizeof(a.objectToWorld));
-    if (!swr_hostmath::inverse_screen_proj(ctx->world_to_clip, fb->width, fb->height, a.invProj))
-        return swr_internal_fail(SWR_EINVAL, "swr_resolve: singular world_to_clip");
-    memcpy(a.viewPos, ctx->view_pos, sizeof(a.viewPos));
-    a.exposure = ctx->exposure;
-    if (ctx->skybox) a.sky = ctx->skybox->d, a.hasSky = 1;
-    swr_light* dl = nullptr;
-    cudaError_t e = cudaSuccess;
-    if (ctx->num_lights) {
-        e = cudaMallocAsync(&dl, ctx->num_lights * sizeof(swr_light), st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(dl, ctx->lights, ctx->num_lights * sizeof(swr_light), cudaMemcpyHostToDevice, st);
-        if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_resolve: lights");
-    }
-    a.lights = dl;
-    a.numLights = ctx->num_lights;
+    swr_status s = build_resolve_args(fb, ctx, a, "swr_resolve");
+    if (s != SWR_OK) return s;
+    cudaStream_t st = swr_internal_stream();
     const uint32_t tiles = (fb->width / 4) * (fb->height / 4);
+    cudaError_t e;
     {
         LaunchScope ls("k_resolve", st);
-        k_resolve<<<(tiles * 16 + 255) / 256, 256, 0, st>>>(a);
+        k_resolve<kResolvePlain><<<(tiles * 16 + 255) / 256, 256, 0, st>>>(a, NeuralResolve{});
         e = cudaGetLastError();
     }
-    if (dl) cudaFreeAsync(dl, st);
+    if (a.lights) cudaFreeAsync((void*)a.lights, st);
     if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_resolve");
     fb->keys_valid = false;  // layer 0 now holds colour; a later draw rebuilds its keys from depth
+    return SWR_OK;
+}
+
+swr_status swr_resolve_neural(swr_rasterizer r, swr_framebuffer fb, const swr_shading_context* ctx, swr_neural n,
+                              swr_neural_stats* stats) {
+    (void)r;
+    if (!n) return swr_internal_fail(SWR_EINVAL, "swr_resolve_neural: NULL model");
+    ResolveArgs a = {};
+    swr_status s = build_resolve_args(fb, ctx, a, "swr_resolve_neural");
+    if (s != SWR_OK) return s;
+    cudaStream_t st = swr_internal_stream();
+    const uint32_t M = n->d.numMaterials;
+    const size_t slots = (size_t)fb->width * fb->height * 4;
+    cudaError_t e = cudaSuccess;
+    if (n->scratchSlots < slots) {
+        if (n->pixelReq) cudaFree(n->pixelReq);
+        if (n->sorted) cudaFree(n->sorted);
+        if (n->decoded) cudaFree(n->decoded);
+        n->pixelReq = n->sorted = nullptr, n->decoded = nullptr, n->scratchSlots = 0;
+        e = cudaMalloc(&n->pixelReq, slots * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMalloc(&n->sorted, slots * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMalloc(&n->decoded, slots * sizeof(uint2));
+        if (e != cudaSuccess) {
+            if (a.lights) cudaFreeAsync((void*)a.lights, st);
+            return swr_internal_cuda_fail(e, "swr_resolve_neural: scratch");
+        }
+        n->scratchSlots = slots;
+    }
+    neural_sync_half(n, st);
+    uint32_t* counts = n->counters;
+    uint32_t* cursor = counts + (M + 1);
+    uint32_t* reqOffset = cursor + (M + 1);
+    uint32_t* tileOffset = reqOffset + (M + 1);
+    uint32_t* levelCount = tileOffset + (M + 1);
+    NeuralResolve nr = {};
+    nr.tex = n->d.tex, nr.numMaterials = M, nr.decodedLevels = n->d.levels + 2;
+    nr.pixelReq = n->pixelReq, nr.counts = counts, nr.decoded = n->decoded;
+    const uint32_t tiles = (fb->width / 4) * (fb->height / 4), blocks = (tiles * 16 + 255) / 256;
+    e = cudaMemsetAsync(counts, 0, 2 * (M + 1) * sizeof(uint32_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(levelCount, 0, kNeuralMaxDecoded * sizeof(uint32_t), st);
+    if (e == cudaSuccess) {
+        LaunchScope ls("k_resolve_emit", st);
+        k_resolve<kResolveEmit><<<blocks, 256, 0, st>>>(a, nr);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        LaunchScope ls("k_neural_offsets", st);
+        launch_neural_offsets(counts, reqOffset, tileOffset, M, st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        LaunchScope ls("k_neural_scatter", st);
+        launch_neural_scatter(n->pixelReq, (uint32_t)slots, reqOffset, cursor, n->sorted, levelCount, st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        NeuralDecodeArgs d = {};
+        d.n = n->d;
+        d.sorted = n->sorted, d.reqOffset = reqOffset, d.tileOffset = tileOffset;
+        d.out = n->decoded;
+        d.status = n->status;
+        LaunchScope ls("k_neural_decode", st);
+        launch_neural_decode(d, neural_decode_blocks_per_sm() * neural_num_sms(), st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) {
+        LaunchScope ls("k_resolve_neural", st);
+        k_resolve<kResolveNeural><<<blocks, 256, 0, st>>>(a, nr);
+        e = cudaGetLastError();
+    }
+    if (a.lights) cudaFreeAsync((void*)a.lights, st);
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_resolve_neural");
+    fb->keys_valid = false;
+    if (stats) {
+        uint32_t v[2] = {};
+        e = cudaMemcpyAsync(&v[0], reqOffset + M, 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&v[1], tileOffset + M, 4, cudaMemcpyDeviceToHost, st);
+        uint32_t status = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&status, n->status, 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(stats->level_texels, levelCount, kNeuralMaxDecoded * 4, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_resolve_neural: stats");
+        stats->requests = v[0], stats->tiles = v[1];
+        if (status) {
+            cudaMemsetAsync(n->status, 0, 4, st);
+            return swr_internal_fail(SWR_ETIMEOUT, "swr_resolve_neural: a tensor-core wait timed out");
+        }
+    }
     return SWR_OK;
 }
 

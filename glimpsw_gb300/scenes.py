@@ -209,10 +209,9 @@ def make_view(width, height, eye, target, fov=60.0, near=0.1, depth_only=False) 
 
 
 # ---------------------------------------------------------------------------------- textures
-def value_noise_rgba(size: int, seed: int, cells: int = 32, layer: int = 0) -> np.ndarray:
-    """Seeded RGBA8 value noise (bilinear over a cells x cells lattice, wrapping), uint32[size, size]."""
-    # layer 1 = tangent-space normal XY (centred near 128), metallic, roughness (Scene.h:8-10)
-    lat = _noise_lattice(seed, cells, layer)
+def _lattice_rgba(size: int, lat: np.ndarray) -> np.ndarray:
+    """Bilinear interpolation (8-bit fractions) of a wrapping cells x cells x 4 lattice, int64[size, size, 4]."""
+    cells = lat.shape[0]
     step = size // cells
     t = (np.arange(size) % step) * 256 // step                       # 8-bit fraction
     i0 = np.arange(size) // step
@@ -224,7 +223,17 @@ def value_noise_rgba(size: int, seed: int, cells: int = 32, layer: int = 0) -> n
     d = lat[i1[:, None], i1[None, :]]
     top = a * (256 - tx) + b * tx
     bot = c * (256 - tx) + d * tx
-    v = ((top * (256 - ty) + bot * ty) >> 16).astype(np.uint32)
+    return (top * (256 - ty) + bot * ty) >> 16
+
+
+def value_noise_rgba(size: int, seed: int, cells: int = 32, layer: int = 0, detail: bool = False) -> np.ndarray:
+    """Seeded RGBA8 value noise (bilinear over a cells x cells lattice, wrapping), uint32[size, size].
+    With detail, a second octave with 8-texel cells is blended in at 1/4 weight."""
+    # layer 1 = tangent-space normal XY (centred near 128), metallic, roughness (Scene.h:8-10)
+    v = _lattice_rgba(size, _noise_lattice(seed, cells, layer))
+    if detail:
+        v = (3 * v + _lattice_rgba(size, _noise_lattice(seed + 104729, size // 8, layer))) >> 2
+    v = v.astype(np.uint32)
     if layer == 0:
         v[..., 3] = 255
     return v[..., 0] | (v[..., 1] << 8) | (v[..., 2] << 16) | (v[..., 3] << 24)
@@ -236,27 +245,40 @@ def _noise_lattice(seed: int, cells: int, layer: int) -> np.ndarray:
     if layer == 1:
         lat[..., 0] = 128 + (lat[..., 0] - 128) // 3
         lat[..., 1] = 128 + (lat[..., 1] - 128) // 3
+        # roughness in [ROUGHNESS_MIN, 255]: no mirror-like texels (their one-LSB changes swing the
+        # GGX lobe by 2x and dominate any image comparison)
+        lat[..., 3] = ROUGHNESS_MIN + lat[..., 3] * (255 - ROUGHNESS_MIN) // 255
     return lat
 
 
-def value_noise_rgba_torch(size: int, seed: int, cells: int = 32, layer: int = 0, device="cuda"):
+ROUGHNESS_MIN = 51  # 0.2
+
+
+def value_noise_rgba_torch(size: int, seed: int, cells: int = 32, layer: int = 0, device="cuda", detail: bool = False):
     """value_noise_rgba computed on the device with torch (same integer arithmetic, same texels);
     returns an int32 tensor of shape (size, size) holding the packed RGBA8 words."""
     import torch
-    lat = torch.from_numpy(_noise_lattice(seed, cells, layer)).to(device)
-    step = size // cells
-    ar = torch.arange(size, device=device)
-    t = (ar % step) * 256 // step
-    i0 = ar // step
-    i1 = (i0 + 1) % cells
-    ty, tx = t[:, None, None], t[None, :, None]
-    a = lat[i0[:, None], i0[None, :]]
-    b = lat[i0[:, None], i1[None, :]]
-    c = lat[i1[:, None], i0[None, :]]
-    d = lat[i1[:, None], i1[None, :]]
-    top = a * (256 - tx) + b * tx
-    bot = c * (256 - tx) + d * tx
-    v = (top * (256 - ty) + bot * ty) >> 16
+
+    def lattice(lat_np):
+        lat = torch.from_numpy(lat_np).to(device)
+        c = lat.shape[0]
+        step = size // c
+        ar = torch.arange(size, device=device)
+        t = (ar % step) * 256 // step
+        i0 = ar // step
+        i1 = (i0 + 1) % c
+        ty, tx = t[:, None, None], t[None, :, None]
+        a = lat[i0[:, None], i0[None, :]]
+        b = lat[i0[:, None], i1[None, :]]
+        cc = lat[i1[:, None], i0[None, :]]
+        d = lat[i1[:, None], i1[None, :]]
+        top = a * (256 - tx) + b * tx
+        bot = cc * (256 - tx) + d * tx
+        return (top * (256 - ty) + bot * ty) >> 16
+
+    v = lattice(_noise_lattice(seed, cells, layer))
+    if detail:
+        v = (3 * v + lattice(_noise_lattice(seed + 104729, size // 8, layer))) >> 2
     if layer == 0:
         v[..., 3] = 255
     packed = v[..., 0] | (v[..., 1] << 8) | (v[..., 2] << 16) | (v[..., 3] << 24)
@@ -294,13 +316,15 @@ class Scene:
     texture_seed: int = 0
     env_size: int = 0
     name: str = ""
+    texture_detail: bool = False              # second noise octave with 8-texel cells
+
 
     @property
     def num_meshlets(self) -> int:
         return len(self.meshlets)
 
     def texture_pixels(self, i: int, layer: int) -> np.ndarray:
-        return value_noise_rgba(self.texture_size, self.texture_seed + i, layer=layer)
+        return value_noise_rgba(self.texture_size, self.texture_seed + i, layer=layer, detail=self.texture_detail)
 
 
 def grid_scene(n_side: int = 32, width: int = 1280, height: int = 720, seed: int = 1,
@@ -376,5 +400,5 @@ def volume_scene(n: int = 100_000, width: int = 1920, height: int = 1080, n_mate
     eye = np.array([0.0, 0.0, -1.3 * extent])
     v0 = make_view(width, height, eye=eye, target=(0.0, 0.0, 0.0))
     v1 = make_view(width, height, eye=eye + np.array([0.4, 0.2, 0.6]), target=(1.0, 0.5, 0.0))
-    return Scene(m, mats, texture_size, 2, [v0, v1], texture_seed=seed * 1000, env_size=env_size,
+    return Scene(m, mats, texture_size, 2, [v0, v1], texture_seed=seed * 1000, env_size=env_size, texture_detail=True,
                  name=f"volume{n}@{width}x{height}")

@@ -227,6 +227,67 @@ swr_status swr_downsample_depth(swr_framebuffer fb, swr_texture dest);
  * into RGBA8 colour written over layer 0. The light-sprite overlay (691-731) is not drawn. */
 swr_status swr_resolve(swr_rasterizer r, swr_framebuffer fb, const swr_shading_context* ctx);
 
+/* ---- Learned texture decoder (no counterpart in the reference) ----
+ * One model holds, per material, an FP16 latent pyramid of 8 channels (latent level k has the size
+ * of texture level k+2, k < latent_levels) and an MLP of 11 inputs (8 latent channels, bias, two
+ * level flags) -> 64 -> 64 -> 8 (GELU; 5384 parameters) decoding a texel's albedo RGB, normal XY,
+ * metallic, roughness and AO. Texture levels 2..latent_levels+1 decode from their latent level's
+ * texel, levels 1 and 0 from latent level 0 magnified 2x / 4x. It is trained on the device (BF16
+ * tensor cores, FP32 accumulation, Adam) towards the plain sampler's texels, and
+ * swr_resolve_neural decodes the texture levels it covers instead of sampling them; coarser
+ * levels keep the plain sampler. Textures: RGBA8, 1 or 2 layers, width and height multiples of
+ * 4 << (latent_levels-1), at least latent_levels+2 mips. The textures must outlive the model. */
+typedef struct swr_neural_t* swr_neural;
+enum { SWR_NEURAL_PARAMS = 5704 };   /* padded FP32 parameter block per material (see swr_neural_get_params) */
+typedef struct {
+    uint32_t num_materials, latent_levels;
+    uint32_t texels_per_material;     /* latent texels over all levels */
+    uint32_t level_offset[4], level_width[4], level_height[4];
+    uint64_t latent_bytes;            /* FP16 latents of all materials */
+    uint64_t weight_bytes;            /* inference weights of all materials (BF16 + FP32 biases) */
+    uint64_t fallback_bytes;          /* texture levels >= latent_levels+2 kept for the plain sampler */
+    uint64_t plain_bytes;             /* all levels of the plain textures */
+} swr_neural_info;
+typedef struct {
+    uint32_t requests;                /* texels decoded by the network */
+    uint32_t tiles;                   /* 128-texel tensor-core tiles */
+    uint32_t level_texels[6];         /* decoded texels per texture level */
+} swr_neural_stats;
+
+/* textures[i] is the texture of material i (NULL: the material has none and is never decoded). */
+swr_status swr_neural_create(const swr_texture* textures, uint32_t num_materials, uint32_t latent_levels, uint64_t seed,
+                             swr_neural* out);
+swr_status swr_neural_destroy(swr_neural n);
+swr_status swr_neural_get_info(swr_neural n, swr_neural_info* info);
+/* `steps` Adam steps (lr, beta1 0.9, beta2 0.999, eps 1e-8). Each step draws batch samples spread
+ * evenly over materials_per_step materials taken round-robin; a sample is a texel and its target
+ * the plain texel. Texture level l is drawn with weight 2^(level_weighting * (latent_levels+1-l)):
+ * 2 = proportional to the level's texel count, 1 = to its edge, 0 = uniform. batch /
+ * materials_per_step must be a multiple of 128. mean_loss (optional, synchronises) receives the
+ * mean squared error per output of the last step. */
+swr_status swr_neural_train(swr_neural n, uint32_t steps, uint32_t batch, uint32_t materials_per_step,
+                            uint32_t level_weighting, float learning_rate, float* mean_loss);
+/* Gradients for explicit samples of one material without updating anything: samples_device holds
+ * count (multiple of 128) packed texels level<<28 | y<<14 | x. param_grad (host, SWR_NEURAL_PARAMS)
+ * receives the parameter gradient of the loss sum over 128-sample tiles of mean squared error,
+ * latent_grad (host, texels_per_material*8, may be NULL) the latent gradient, loss (may be NULL)
+ * the summed squared error. */
+swr_status swr_neural_gradients(swr_neural n, uint32_t material, const uint32_t* samples_device, uint32_t count,
+                                float* param_grad, float* latent_grad, float* loss);
+/* FP32 parameters / latents (texels_per_material*8 floats, [texel][channel]) of one material. */
+swr_status swr_neural_get_params(swr_neural n, uint32_t material, float* params);
+swr_status swr_neural_set_params(swr_neural n, uint32_t material, const float* params);
+swr_status swr_neural_get_latents(swr_neural n, uint32_t material, float* latents);
+swr_status swr_neural_set_latents(swr_neural n, uint32_t material, const float* latents);
+/* Decodes count texels (packed as for swr_neural_gradients) of one material into out_device
+ * (2 words per texel: layer-0 RGBA8 with AO in alpha, layer-1 RGBA8). */
+swr_status swr_neural_decode(swr_neural n, uint32_t material, const uint32_t* texels_device, uint32_t count,
+                             uint32_t* out_device);
+/* swr_resolve with the texture levels below latent_levels decoded by the model (the scene's
+ * material i must use the model's texture i); stats may be NULL (else the stream is synchronised). */
+swr_status swr_resolve_neural(swr_rasterizer r, swr_framebuffer fb, const swr_shading_context* ctx, swr_neural n,
+                              swr_neural_stats* stats);
+
 #ifdef __cplusplus
 }
 #endif
