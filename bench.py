@@ -57,6 +57,11 @@ def parse():
     p.add_argument("--neural-batch", type=int, default=65536)
     p.add_argument("--neural-level-weighting", type=int, default=1, choices=[0, 1, 2],
                    help="training texture level l drawn with weight 2^(w*(5-l)): 2 by texel count, 1 by edge, 0 uniform")
+    p.add_argument("--materials", type=int, default=64)
+    p.add_argument("--neural-width", type=int, default=2560)
+    p.add_argument("--neural-height", type=int, default=1440)
+    p.add_argument("--only", default="all", choices=["all", "neural"],
+                   help="neural: only the learned-decoder section (for profiling runs; prints that section)")
     return p.parse_args()
 
 
@@ -66,7 +71,8 @@ def dist_env():
 
 def build_scene(args):
     from glimpsw_gb300 import scenes
-    return scenes.volume_scene(n=args.meshlets, width=args.width, height=args.height, texture_size=args.texture_size)
+    return scenes.volume_scene(n=args.meshlets, width=args.width, height=args.height, texture_size=args.texture_size,
+                               n_materials=args.materials)
 
 
 def default_lights():
@@ -328,6 +334,44 @@ def multiview_section(args, api, stream):
 
 
 # ----------------------------------------------------------------------------- learned decoder
+def texel_accuracy(api, model, texs, materials=4, n=65536, seed=7):
+    """Decoded texels against the plain texels they replace, per channel group, over n random texels
+    of each decoded level (levels weighted by edge length) of the first `materials` materials; the
+    AO channel (no source texels) is compared with its constant target 1."""
+    import torch
+    rng = np.random.default_rng(seed)
+    levels = np.arange(model.latent_levels + 2)
+    w = 2.0 ** -levels.astype(np.float64)
+    got, ref = [], []
+    for mat in range(min(materials, len(texs))):
+        t = texs[mat]
+        data = t.get_data()
+        row_shift = int(np.log2(max(t.width, 8)))
+        lvl = rng.choice(levels, n, p=w / w.sum())
+        x, y = rng.integers(0, t.width >> lvl), rng.integers(0, t.height >> lvl)
+        off = np.asarray(t.mip_offsets, np.int64)[lvl] + ((y & 7) | (x << 3) | ((y & ~7) << (row_shift - lvl)))
+        a0, a1 = data[off].astype(np.int64), data[t.layer_stride + off].astype(np.int64)
+        ref.append(np.stack([a0 & 255, (a0 >> 8) & 255, (a0 >> 16) & 255, a1 & 255, (a1 >> 8) & 255, (a1 >> 16) & 255,
+                             a1 >> 24, np.full(n, 255)], axis=1))
+        packed = api.pack_texel(lvl, x, y).astype(np.uint32)
+        out = torch.zeros(2 * n, dtype=torch.int32, device="cuda")
+        model.decode(mat, torch.from_numpy(packed.view(np.int32)).cuda(), n, out)
+        d = out.cpu().numpy().view(np.uint32).reshape(-1, 2).astype(np.int64)
+        got.append(np.stack([d[:, 0] & 255, (d[:, 0] >> 8) & 255, (d[:, 0] >> 16) & 255, d[:, 1] & 255,
+                             (d[:, 1] >> 8) & 255, (d[:, 1] >> 16) & 255, d[:, 1] >> 24, d[:, 0] >> 24], axis=1))
+    got, ref = np.concatenate(got), np.concatenate(ref)
+
+    def psnr(cols):
+        mse = float(((got[:, cols] - ref[:, cols]) ** 2).mean()) / 255.0 ** 2
+        return 10 * np.log10(1.0 / mse) if mse > 0 else float("inf")
+    err = np.abs(got - ref)
+    return {"texels": int(len(got)), "albedo_psnr_db": psnr([0, 1, 2]), "normal_xy_psnr_db": psnr([3, 4]),
+            "metal_rough_psnr_db": psnr([5, 6]), "max_abs_255": {"albedo": int(err[:, :3].max()),
+                                                                  "normal_xy": int(err[:, 3:5].max()),
+                                                                  "metal_rough": int(err[:, 5:7].max())},
+            "ao": {"target": 255, "mean": float(got[:, 7].mean()), "max_abs_255": int(err[:, 7].max())}}
+
+
 def neural_section(args, api, stream, sc, texs, env, scene, rast, lights):
     """Learned texture decoder over the scene's 64 materials: trained on the device (Adam, lr 1e-3,
     `neural_steps` steps of `neural_batch` texels spread over 8 materials per step), then the scene
@@ -355,7 +399,8 @@ def neural_section(args, api, stream, sc, texs, env, scene, rast, lights):
     for k, t in api.profile_collect():
         step_kernels[k] = step_kernels.get(k, 0.0) + t / 4
     api.profile_enable(False)
-    W, H = 2560, 1440
+    texel = texel_accuracy(api, model, texs)
+    W, H = args.neural_width, args.neural_height
     n = len(sc.meshlets)
     batches = [(off, min(BATCH, n - off)) for off in range(0, n, BATCH)]
     bms = [torch.zeros((cnt + 15) // 16, dtype=torch.int16, device="cuda") for _, cnt in batches]
@@ -379,6 +424,7 @@ def neural_section(args, api, stream, sc, texs, env, scene, rast, lights):
     mem = model.memory()
     neural_bytes = mem["latent_bytes"] + mem["weight_bytes"] + mem["fallback_bytes"]
     out["memory"] = {**mem, "neural_total_bytes": neural_bytes, "ratio_plain_over_neural": mem["plain_bytes"] / neural_bytes}
+    out["texel_accuracy"] = texel
     for name, view in cams.items():
         ctx = api.ShadingContext(scene, view.world_to_clip, world_to_clip=view.world_to_clip, skybox=env,
                                  view_pos=view.eye, lights=lights)
@@ -454,14 +500,18 @@ def run_ours(args):
     n = len(sc.meshlets)
     batches = [(off, min(BATCH, n - off)) for off in range(0, n, BATCH)]
     bitmaps = [torch.zeros((cnt + 15) // 16, dtype=torch.int16, device="cuda") for _, cnt in batches]
-    from oracle.oracle import hiz_texture_size  # sizing rule of the frame driver (Main.cpp:54-56)
-    hw, hh = hiz_texture_size(W, H)
+    hw, hh = api.hiz_texture_size(W, H)
     hiz = [api.Texture2D(api.FORMAT_R32F, hw, hh, 16, 1) for _ in range(2)]
     model = scenes.IDENTITY
     lights = [api.SwrLight()]
     lights[0].type, lights[0].intensity = 0, 1500.0
     lights[0].direction[:] = default_lights().tolist()
     lights[0].color[:] = [1.0, 1.0, 1.0]
+    if args.only == "neural":  # the learned-decoder section alone (profiling runs)
+        out = neural_section(args, api, stream, sc, texs, env, scene, rast, lights)
+        if rank == 0:
+            print(json.dumps({"neural": out, "config": config_dict(args, sc)}), flush=True)
+        return
 
     def frame(view, prev, hiz_in, hiz_out):
         fb.clear(0xFF000000, 0.0)

@@ -358,6 +358,14 @@ def downsample_depth(fb: Framebuffer, dest: Texture2D) -> None:
     _check(_lib.swr_downsample_depth(fb.h, dest.h))
 
 
+def hiz_texture_size(width: int, height: int) -> tuple[int, int]:
+    """Hi-Z texture size the reference frame driver allocates for a frame (Main.cpp:54-56): each
+    dimension is the power of two at or above half the frame's."""
+    def half(v):
+        return 1 << ((v - 1) // 2).bit_length()
+    return half(width), half(height)
+
+
 class Batch:
     """Batched multi-view rendering (swr_batch_*): many framebuffers, one CUDA graph per frame.
 

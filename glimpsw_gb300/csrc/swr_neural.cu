@@ -480,6 +480,21 @@ __global__ void k_neural_image(const float* params, uint8_t* image) {
         image_store(image + (size_t)mat * kNeuralImage, i, params[(size_t)mat * kNeuralParams + i]);
 }
 
+// One Adam update: m, v moments; w -= lr m / (1 - b1^t) / (sqrt(v / (1 - b2^t)) + eps), written as
+// w -= lrm m / (sqrt(v) s2 + eps) with lrm = lr / (1 - b1^t) and s2 = 1 / sqrt(1 - b2^t) from the host,
+// square root and quotient on the SFU (sqrt.approx, div.approx: a few ulp, irrelevant to Adam).
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float y;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ void adam_update(float g, float& m, float& v, float& w, float b1, float b2, float lrm, float s2,
+                                            float eps) {
+    m = fmaf(b1, m, (1.0f - b1) * g);
+    v = fmaf(b2, v, (1.0f - b2) * g * g);
+    w -= __fdividef(lrm * m, fmaf(sqrt_approx(v), s2, eps));
+}
+
 // Adam on the parameters of the step's materials (sum of the CTAs' partial gradients in a fixed
 // order), then the new BF16 image.
 __global__ void k_neural_adam_params(const __grid_constant__ NeuralAdamArgs a) {
@@ -488,7 +503,6 @@ __global__ void k_neural_adam_params(const __grid_constant__ NeuralAdamArgs a) {
     float* m = a.m + (size_t)mat * kNeuralParams;
     float* v = a.v + (size_t)mat * kNeuralParams;
     const float* part = a.partial + (size_t)slot * a.ctasPerMaterial * kNeuralParams;
-    const float bc1 = a.bc1[slot], bc2 = a.bc2[slot];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;  // one parameter per thread
     if (i < kNeuralParams) {
         float g = 0.f;
@@ -501,32 +515,32 @@ __global__ void k_neural_adam_params(const __grid_constant__ NeuralAdamArgs a) {
             for (int k = 0; k < 8; k++) g += q[k];
         }
         for (; c < a.ctasPerMaterial; c++) g += part[(size_t)c * kNeuralParams + i];
-        const float mi = a.beta1 * m[i] + (1.0f - a.beta1) * g;
-        const float vi = a.beta2 * v[i] + (1.0f - a.beta2) * g * g;
-        m[i] = mi, v[i] = vi;
-        const float w = p[i] - a.lr * (mi / bc1) / (sqrtf(vi / bc2) + a.eps);
-        p[i] = w;
+        float mi = m[i], vi = v[i], w = p[i];
+        adam_update(g, mi, vi, w, a.beta1, a.beta2, a.lrm[slot], a.s2[slot], a.eps);
+        m[i] = mi, v[i] = vi, p[i] = w;
         image_store(a.image + (size_t)mat * kNeuralImage, i, w);
     }
 }
 
-// Adam on the latents of the step's materials; clears the gradient.
-__global__ void k_neural_adam_latent(const __grid_constant__ NeuralAdamArgs a) {
+// Adam on the latents of the step's materials, one float4 per thread; clears the gradient.
+__global__ void __launch_bounds__(256) k_neural_adam_latent(const __grid_constant__ NeuralAdamArgs a) {
     const uint32_t slot = blockIdx.y, mat = a.materials[slot];
     const size_t n4 = (size_t)a.texelsPerMaterial * 2, base = (size_t)mat * n4;
-    const float bc1 = a.bc1[slot], bc2 = a.bc2[slot];
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n4; i += (size_t)gridDim.x * blockDim.x) {
-        float4 g = ((float4*)a.latentGrad)[base + i];
-        ((float4*)a.latentGrad)[base + i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        float4 m = ((float4*)a.latentM)[base + i], v = ((float4*)a.latentV)[base + i], p = ((float4*)a.latent)[base + i];
-        auto upd = [&](float gi, float& mi, float& vi, float& pi) {
-            mi = a.beta1 * mi + (1.0f - a.beta1) * gi;
-            vi = a.beta2 * vi + (1.0f - a.beta2) * gi * gi;
-            pi = pi - a.lr * (mi / bc1) / (sqrtf(vi / bc2) + a.eps);
-        };
-        upd(g.x, m.x, v.x, p.x), upd(g.y, m.y, v.y, p.y), upd(g.z, m.z, v.z, p.z), upd(g.w, m.w, v.w, p.w);
-        ((float4*)a.latentM)[base + i] = m, ((float4*)a.latentV)[base + i] = v, ((float4*)a.latent)[base + i] = p;
-    }
+    const size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if (i >= n4) return;
+    float4* G = (float4*)a.latentGrad + base + i;
+    float4* M = (float4*)a.latentM + base + i;
+    float4* V = (float4*)a.latentV + base + i;
+    float4* P = (float4*)a.latent + base + i;
+    const float4 g = *G;
+    float4 m = *M, v = *V, p = *P;
+    *G = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float lrm = a.lrm[slot], s2 = a.s2[slot];
+    adam_update(g.x, m.x, v.x, p.x, a.beta1, a.beta2, lrm, s2, a.eps);
+    adam_update(g.y, m.y, v.y, p.y, a.beta1, a.beta2, lrm, s2, a.eps);
+    adam_update(g.z, m.z, v.z, p.z, a.beta1, a.beta2, lrm, s2, a.eps);
+    adam_update(g.w, m.w, v.w, p.w, a.beta1, a.beta2, lrm, s2, a.eps);
+    *M = m, *V = v, *P = p;
 }
 
 // Latent level l texel (x, y) starts as texture level l + 2 texel (x, y): channels R G B (layer
@@ -699,30 +713,45 @@ __global__ void __launch_bounds__(1024) k_neural_offsets(const uint32_t* counts,
     if (t == n - 1) reqOffset[n] = sr[t], tileOffset[n] = st[t];
 }
 
-// Groups the per-pixel requests (material<<32 | level<<28 | ty<<14 | tx, or ~0) by material.
-__global__ void k_neural_scatter(const unsigned long long* pixelReq, uint32_t slots, const uint32_t* reqOffset, uint32_t* cursor,
-                                 unsigned long long* sorted, uint32_t* levelCount) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31;
-    const unsigned long long r = i < slots ? pixelReq[i] : ~0ull;
-    const bool valid = r != ~0ull;
-    const unsigned act = __ballot_sync(0xFFFFFFFFu, valid);
-    {  // requests per decoded level (statistics)
-        const uint32_t lvl = valid ? (uint32_t)(r >> 28) & 15u : 15u;
+// Groups the per-pixel requests (material<<32 | level<<28 | ty<<14 | tx, or ~0) by material. A
+// block takes kScatterSlots consecutive slots: shared-memory counters rank each request among the
+// block's requests of its material, then one global atomic per (block, material) reserves the
+// block's run in that material's list (the per-material cursors see few, uncontended atomics).
+constexpr uint32_t kScatterThreads = 256, kScatterPerThread = 4, kScatterSlots = kScatterThreads * kScatterPerThread;
+__global__ void __launch_bounds__(kScatterThreads) k_neural_scatter(const unsigned long long* pixelReq, uint32_t slots,
+                                                                    const uint32_t* reqOffset, uint32_t* cursor,
+                                                                    unsigned long long* sorted, uint32_t* levelCount,
+                                                                    uint32_t numMaterials) {
+    extern __shared__ uint32_t sMat[];  // [numMaterials] counts, then [numMaterials] run starts
+    __shared__ uint32_t sLevel[kNeuralMaxDecoded];
+    uint32_t* sCount = sMat;
+    uint32_t* sBase = sMat + numMaterials;
+    for (uint32_t m = threadIdx.x; m < numMaterials; m += kScatterThreads) sCount[m] = 0;
+    if (threadIdx.x < kNeuralMaxDecoded) sLevel[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t first = blockIdx.x * kScatterSlots + threadIdx.x;
+    unsigned long long r[kScatterPerThread];
+    uint32_t rank[kScatterPerThread];
 #pragma unroll
-        for (uint32_t l = 0; l < kNeuralMaxDecoded; l++) {
-            const unsigned b = __ballot_sync(0xFFFFFFFFu, lvl == l);
-            if (lane == 0 && b) atomicAdd(&levelCount[l], (uint32_t)__popc(b));
+    for (uint32_t k = 0; k < kScatterPerThread; k++) {  // slot first + k * 256: coalesced loads
+        const uint32_t i = first + k * kScatterThreads;
+        r[k] = i < slots ? pixelReq[i] : ~0ull;
+        if (r[k] != ~0ull) {
+            rank[k] = atomicAdd(&sCount[(uint32_t)(r[k] >> 32)], 1u);
+            atomicAdd(&sLevel[((uint32_t)r[k] >> 28) & 15u], 1u);
         }
     }
-    if (!valid) return;
-    const uint32_t m = (uint32_t)(r >> 32);
-    const unsigned peers = __match_any_sync(act, m);
-    const int leader = __ffs(peers) - 1;
-    uint32_t base = 0;
-    if ((int)lane == leader) base = atomicAdd(&cursor[m], (uint32_t)__popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    const uint32_t rank = __popc(peers & ((1u << lane) - 1u));
-    sorted[reqOffset[m] + base + rank] = ((unsigned long long)i << 32) | (uint32_t)r;
+    __syncthreads();
+    for (uint32_t m = threadIdx.x; m < numMaterials; m += kScatterThreads)
+        if (sCount[m]) sBase[m] = reqOffset[m] + atomicAdd(&cursor[m], sCount[m]);
+    if (threadIdx.x < kNeuralMaxDecoded && sLevel[threadIdx.x]) atomicAdd(&levelCount[threadIdx.x], sLevel[threadIdx.x]);
+    __syncthreads();
+#pragma unroll
+    for (uint32_t k = 0; k < kScatterPerThread; k++) {
+        if (r[k] == ~0ull) continue;
+        const uint32_t i = first + k * kScatterThreads;
+        sorted[sBase[(uint32_t)(r[k] >> 32)] + rank[k]] = ((unsigned long long)i << 32) | (uint32_t)r[k];
+    }
 }
 
 }  // namespace
@@ -738,7 +767,7 @@ void launch_neural_train(const NeuralTrainArgs& a, uint32_t blocks, cudaStream_t
 void launch_neural_adam(const NeuralAdamArgs& a, cudaStream_t st) {
     k_neural_adam_params<<<dim3((kNeuralParams + 127) / 128, a.numSlots), 128, 0, st>>>(a);
     const uint32_t n4 = a.texelsPerMaterial * 2;
-    k_neural_adam_latent<<<dim3(std::min<uint32_t>((n4 + 255) / 256, 1024), a.numSlots), 256, 0, st>>>(a);
+    k_neural_adam_latent<<<dim3((n4 + 255) / 256, a.numSlots), 256, 0, st>>>(a);
 }
 uint32_t neural_decode_blocks_per_sm() {
     static int per = 0;
@@ -772,8 +801,9 @@ void launch_neural_offsets(const uint32_t* counts, uint32_t* reqOffset, uint32_t
     k_neural_offsets<<<1, 1024, 0, st>>>(counts, reqOffset, tileOffset, numMaterials);
 }
 void launch_neural_scatter(const unsigned long long* pixelReq, uint32_t slots, const uint32_t* reqOffset, uint32_t* cursor,
-                           unsigned long long* sorted, uint32_t* levelCount, cudaStream_t st) {
-    k_neural_scatter<<<(slots + 255) / 256, 256, 0, st>>>(pixelReq, slots, reqOffset, cursor, sorted, levelCount);
+                           unsigned long long* sorted, uint32_t* levelCount, uint32_t numMaterials, cudaStream_t st) {
+    k_neural_scatter<<<(slots + kScatterSlots - 1) / kScatterSlots, kScatterThreads, 2 * numMaterials * sizeof(uint32_t), st>>>(
+        pixelReq, slots, reqOffset, cursor, sorted, levelCount, numMaterials);
 }
 
 }  // namespace swr

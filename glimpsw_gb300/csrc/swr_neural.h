@@ -70,8 +70,8 @@ struct NeuralAdamArgs {
     uint32_t ctasPerMaterial, numSlots;
     float lr, beta1, beta2, eps;
     uint32_t materials[kNeuralMaxStepMaterials];
-    float bc1[kNeuralMaxStepMaterials];   // 1 - beta1^t per slot
-    float bc2[kNeuralMaxStepMaterials];   // 1 - beta2^t per slot
+    float lrm[kNeuralMaxStepMaterials];   // lr / (1 - beta1^t) per slot (t: the material's step count)
+    float s2[kNeuralMaxStepMaterials];    // 1 / sqrt(1 - beta2^t) per slot
 };
 
 struct NeuralDecodeArgs {
@@ -93,7 +93,8 @@ void launch_neural_export(const float* latent, uint16_t* half, size_t count, cud
 void launch_neural_offsets(const uint32_t* counts, uint32_t* reqOffset, uint32_t* tileOffset, uint32_t numMaterials,
                            cudaStream_t st);
 void launch_neural_scatter(const unsigned long long* pixelReq, uint32_t slots, const uint32_t* reqOffset,
-                           uint32_t* cursor, unsigned long long* sorted, uint32_t* levelCount, cudaStream_t st);
+                           uint32_t* cursor, unsigned long long* sorted, uint32_t* levelCount, uint32_t numMaterials,
+                           cudaStream_t st);
 
 }  // namespace swr
 

@@ -279,8 +279,8 @@ swr_status swr_neural_train(swr_neural n, uint32_t steps, uint32_t batch, uint32
             const uint32_t m = trainable[(n->trainCalls * (uint64_t)G + i) % trainable.size()];
             a.materials[i] = d.materials[i] = m;
             const uint32_t tstep = ++n->steps[m];
-            d.bc1[i] = (float)(1.0 - std::pow(0.9, (double)tstep));
-            d.bc2[i] = (float)(1.0 - std::pow(0.999, (double)tstep));
+            d.lrm[i] = (float)((double)learning_rate / (1.0 - std::pow(0.9, (double)tstep)));
+            d.s2[i] = (float)(1.0 / std::sqrt(1.0 - std::pow(0.999, (double)tstep)));
         }
         a.step = n->trainCalls++;
         if (k + 1 == steps && mean_loss) e = cudaMemsetAsync(n->loss, 0, 8, st);

@@ -765,7 +765,7 @@ swr_status swr_resolve_neural(swr_rasterizer r, swr_framebuffer fb, const swr_sh
     }
     if (e == cudaSuccess) {
         LaunchScope ls("k_neural_scatter", st);
-        launch_neural_scatter(n->pixelReq, (uint32_t)slots, reqOffset, cursor, n->sorted, levelCount, st);
+        launch_neural_scatter(n->pixelReq, (uint32_t)slots, reqOffset, cursor, n->sorted, levelCount, M, st);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) {
