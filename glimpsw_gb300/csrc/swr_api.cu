@@ -255,6 +255,7 @@ swr_status swr_framebuffer_create(uint32_t width, uint32_t height, uint32_t num_
     fb->num_layers = num_layers;
     cudaError_t e = cudaMalloc(&fb->layers, ((size_t)fb->layer_stride * num_layers + 64) * 4);
     if (e == cudaSuccess) e = cudaMalloc(&fb->keys, (size_t)fb->layer_stride * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&fb->tileMin, (size_t)fb->layer_stride / 16 * 4);
     if (e == cudaSuccess) e = cudaMemsetAsync(fb->layers, 0, ((size_t)fb->layer_stride * num_layers + 64) * 4, t_stream);
     if (e != cudaSuccess) {
         swr_framebuffer_destroy(fb);
@@ -269,6 +270,7 @@ swr_status swr_framebuffer_destroy(swr_framebuffer fb) {
     if (!fb) return SWR_OK;
     cudaFree(fb->layers);
     cudaFree(fb->keys);
+    cudaFree(fb->tileMin);
     delete fb;
     return SWR_OK;
 }
@@ -277,7 +279,8 @@ swr_status swr_framebuffer_clear(swr_framebuffer fb, uint32_t color, float depth
     if (!fb) return fail(SWR_EINVAL, "swr_framebuffer_clear: NULL framebuffer");
     uint32_t d;
     memcpy(&d, &depth, 4);
-    launch_clear(fb->layers, fb->layers + fb->layer_stride, fb->keys, fb->width * fb->height, color, d, t_stream);
+    launch_clear(fb->layers, fb->layers + fb->layer_stride, fb->keys, fb->tileMin, fb->width * fb->height, color, d,
+                 t_stream);
     SWR_CHECK_LAUNCH("swr_framebuffer_clear");
     fb->keys_valid = true;
     return SWR_OK;
@@ -426,7 +429,7 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
     if (st == SWR_OK) st = size_queue(r, count);
     if (st != SWR_OK) return st;
     if (!fb->keys_valid) {
-        launch_init_keys(fb->layers + fb->layer_stride, fb->keys, fb->width * fb->height, t_stream);
+        launch_init_keys(fb->layers + fb->layer_stride, fb->keys, fb->tileMin, fb->width * fb->height, t_stream);
         SWR_CHECK_LAUNCH("swr_draw_meshlets: init keys");
         fb->keys_valid = true;
     }
@@ -447,6 +450,7 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
     a.clipMode = (!r->enable_binning && r->enable_clipping) ? 1 : 0;
     a.countClipped = (r->enable_binning || r->enable_clipping) ? 1 : 0;
     a.keys = fb->keys;
+    a.tileMin = fb->tileMin;
     a.s = r->scratch;
     SWR_CUDA(cudaMemsetAsync(r->scratch.control, 0, 3 * sizeof(unsigned long long), t_stream));
     launch_draw(a, t_stream, num_sms());

@@ -25,17 +25,20 @@ struct BatchView {              // device table for the batched clear / cull / f
     uint16_t* bitmap;
     uint32_t pixels;            // width * height
     uint32_t depthOnly;
-    uint32_t pad[2];
+    uint32_t* tileMin;          // per 4x4 tile depth bound
 };
 
-// Framebuffer::Clear(color, depth) for every view; keys restart from the cleared depth.
+// Framebuffer::Clear(color, depth) for every view; keys and tile depth bounds restart from the
+// cleared depth.
 __global__ void k_clear_views(const BatchView* __restrict__ views, uint32_t color, uint32_t depthBits) {
     const BatchView& v = views[blockIdx.y];
-    const unsigned long long key = ((unsigned long long)float_order(__uint_as_float(depthBits)) << 32) | kKeyEmptyLow;
+    const uint32_t hi = float_order(__uint_as_float(depthBits));
+    const unsigned long long key = ((unsigned long long)hi << 32) | kKeyEmptyLow;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < v.pixels; i += gridDim.x * blockDim.x) {
         v.layer0[i] = color;
         v.layer1[i] = depthBits;
         v.keys[i] = key;
+        if ((i & 15) == 0) v.tileMin[i >> 4] = hi;
     }
 }
 
@@ -128,6 +131,7 @@ swr_status upload_views(swr_batch b, const swr_view_desc* views) {
         v.meshletOffset = b->first;
         v.count = b->count;
         v.keys = fb->keys;
+        v.tileMin = fb->tileMin;
         v.cullBitmap = b->frustumCull ? b->dBitmaps + (size_t)i * words : nullptr;
         BatchView& w = bv[i];
         memset(&w, 0, sizeof(w));
@@ -135,6 +139,7 @@ swr_status upload_views(swr_batch b, const swr_view_desc* views) {
         w.layer0 = fb->layers;
         w.layer1 = fb->layers + fb->layer_stride;
         w.keys = fb->keys;
+        w.tileMin = fb->tileMin;
         w.bitmap = b->dBitmaps + (size_t)i * words;
         w.pixels = fb->width * fb->height;
         w.depthOnly = d.depth_only != 0;

@@ -60,7 +60,8 @@ struct ViewParams {
     uint32_t meshletOffset, count;
     unsigned long long* keys;
     const uint16_t* cullBitmap;
-    uint32_t pad[4];
+    uint32_t* tileMin;      // per 4x4 tile: lower bound of its keys' depth words (nullptr: no tile culling)
+    uint32_t pad[2];
 };
 static_assert(sizeof(ViewParams) == 128, "ViewParams");
 
@@ -79,6 +80,7 @@ struct DrawArgs {
     int clipMode;     // 1: clip non-trivial triangles (Mode B), 0: drop them
     int countClipped; // count non-trivial triangles in TrianglesClipped
     unsigned long long* keys;
+    uint32_t* tileMin;  // per 4x4 tile depth lower bound (nullptr: no tile culling)
     DrawScratch s;
     // batched views: work item i of [0, viewStart[numViews]) is meshlet i - viewStart[v] of view v
     const ViewParams* views;
@@ -90,9 +92,9 @@ struct DrawArgs {
 };
 
 void launch_draw(const DrawArgs& a, cudaStream_t st, int numSMs);
-void launch_init_keys(const uint32_t* depthLayer, unsigned long long* keys, uint32_t n, cudaStream_t st);
-void launch_clear(uint32_t* layer0, uint32_t* layer1, unsigned long long* keys, uint32_t n, uint32_t color,
-                  uint32_t depthBits, cudaStream_t st);
+void launch_init_keys(const uint32_t* depthLayer, unsigned long long* keys, uint32_t* tileMin, uint32_t n, cudaStream_t st);
+void launch_clear(uint32_t* layer0, uint32_t* layer1, unsigned long long* keys, uint32_t* tileMin, uint32_t n,
+                  uint32_t color, uint32_t depthBits, cudaStream_t st);
 void launch_fill(uint32_t* dst, uint32_t n, uint32_t value, cudaStream_t st);
 void launch_finalize(const unsigned long long* keys, uint32_t* layer0, uint32_t* layer1, uint32_t n, cudaStream_t st);
 void launch_detile(const uint32_t* src, uint32_t* dst, uint32_t width, uint32_t height, cudaStream_t st);
@@ -123,7 +125,8 @@ struct swr_framebuffer_t {
     uint32_t width, height, tile_stride, layer_stride, num_layers;
     uint32_t* layers;              // num_layers * layer_stride words (+64 pad)
     unsigned long long* keys;      // one vis-buffer key per pixel, tiled like the layers
-    bool keys_valid;
+    uint32_t* tileMin;             // per 4x4 tile: lower bound of its keys' depth words
+    bool keys_valid;               // keys and tileMin reflect the depth layer
 };
 
 struct swr_scene_t {

@@ -104,7 +104,7 @@ extern "C" swr_status swr_draw_meshlets_noalloc(const void* meshlets, uint32_t m
         LaunchScope ls("k_expand_material_flags", stream);
         k_expand_material_flags<<<(num_materials + 255) / 256, 256, 0, stream>>>(material_flags, num_materials, mats);
     }
-    launch_init_keys((const uint32_t*)depth, keys, n, stream);
+    launch_init_keys((const uint32_t*)depth, keys, nullptr, n, stream);
 
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);

@@ -13,6 +13,14 @@
 //   k_finalize       converts per-pixel keys to the reference's depth and surfaceId layers.
 // The depth test is a 64-bit atomicMax on (ordered depth, 0xFFFFFFFE - rank); the result is
 // independent of execution order and equals the single-threaded reference.
+//
+// Tile depth culling: tileMin holds, per 4x4 tile, a lower bound of the depth words of its 16
+// keys (keys only grow, and tileMin only takes minima of values its pixels had reached). Before a
+// tile is shaded, an upper bound of the triangle's depth over the tile is compared with it; a tile
+// the triangle cannot win anywhere is skipped. The vis-buffer is unchanged (only fragments that
+// would fail the depth test are skipped), while the dense scenes' overdraw mostly disappears.
+#include <cfloat>
+
 #include "swr_device.cuh"
 #include "swr_internal.h"
 
@@ -122,19 +130,56 @@ __device__ __forceinline__ void shade_fragment(const TriRec& r, uint32_t px, uin
 }
 
 // The same for pixel (tx + l % 4, ty + l / 4) of the 4x4 tile at the 4-aligned (tx, ty), l = lane % 16:
-// the tiled key offset is then the tile's base plus l.
-__device__ __forceinline__ void shade_tile_pixel(const TriRec& r, uint32_t tx, uint32_t ty, uint32_t l,
-                                                 unsigned long long* keys, uint32_t width) {
+// the tiled key offset is then the tile's base plus l. Every lane reads its pixel's key (one
+// 128-byte line per tile); the return value is a lower bound of the pixel's depth word afterwards.
+__device__ __forceinline__ uint32_t shade_tile_pixel(const TriRec& r, uint32_t tx, uint32_t ty, uint32_t l,
+                                                     unsigned long long* keys, uint32_t width) {
+    unsigned long long* p = keys + (tx << 2) + ty * width + l;
+    const unsigned long long cur = *(volatile unsigned long long*)p;
     const uint32_t px = tx + (l & 3), py = ty + (l >> 2);
     const int32_t e0 = (int32_t)((uint32_t)r.E0 + (uint32_t)r.A12 * px + (uint32_t)r.B12 * py);
     const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
     const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
-    if ((e0 | e1 | e2) < 0) return;
+    if ((e0 | e1 | e2) < 0) return (uint32_t)(cur >> 32);
     const float depth = ffma(__int2float_rn(e1), r.Z10, ffma(__int2float_rn(e2), r.Z20, r.Z0));
-    if (depth != depth) return;
+    if (depth != depth) return (uint32_t)(cur >> 32);
     const unsigned long long key = ((unsigned long long)float_order(depth) << 32) | r.lowword;
-    unsigned long long* p = keys + (tx << 2) + ty * width + l;
-    if (key > *(volatile unsigned long long*)p) atomicMax(p, key);
+    if (key <= cur) return (uint32_t)(cur >> 32);
+    atomicMax(p, key);
+    return (uint32_t)(key >> 32);
+}
+
+// Upper bound of the depth shade_tile_pixel computes for any sample of the 4x4 tile at (px, py).
+// The exact depth Z0 + Z10 e1 + Z20 e2 is affine in the pixel (the edge values are exact
+// integers), so its maximum over the tile is at a corner. A computed depth differs from the exact
+// one by at most 4u (|Z0| + |Z10 e1| + |Z20 e2|), u = 2^-24 (two conversions, two fma roundings),
+// and |e| is largest at a corner too, so corner value + 2^-20 * that sum bounds every sample.
+// NaN anywhere gives +inf (never culled).
+__device__ __forceinline__ float tile_depth_bound(const TriRec& r, uint32_t px, uint32_t py) {
+    float dmax = -FLT_MAX, a1 = 0.0f, a2 = 0.0f;
+    bool nan = false;
+#pragma unroll
+    for (int c = 0; c < 4; c++) {
+        const uint32_t x = px + (c & 1) * 3, y = py + (c >> 1) * 3;
+        const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * x + (uint32_t)r.B20 * y);
+        const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * x + (uint32_t)r.B01 * y);
+        const float f1 = __int2float_rn(e1), f2 = __int2float_rn(e2);
+        const float d = ffma(f1, r.Z10, ffma(f2, r.Z20, r.Z0));
+        nan |= d != d;
+        dmax = d > dmax ? d : dmax;
+        a1 = fmaxf(a1, fabsf(f1)), a2 = fmaxf(a2, fabsf(f2));
+    }
+    const float s = fadd(fabsf(r.Z0), fadd(fmul(fabsf(r.Z10), a1), fmul(fabsf(r.Z20), a2)));
+    return nan ? __int_as_float(0x7F800000) : fadd(dmax, fmul(s, 0x1p-20f));
+}
+
+// Raises the tile's depth bound to the minimum of the values its 16 pixels reported (the two
+// halves of the warp shade one tile each; offsets below 16 keep the reduction inside a half).
+__device__ __forceinline__ void update_tile_min(uint32_t obs, uint32_t* tileMin, uint32_t tileIdx, uint32_t known,
+                                                bool active, int lane) {
+#pragma unroll
+    for (int o = 8; o > 0; o >>= 1) obs = min(obs, __shfl_xor_sync(0xFFFFFFFFu, obs, o));
+    if (active && (lane & 15) == 0 && obs > known) atomicMax(&tileMin[tileIdx], obs);
 }
 
 // One lane rasterizes a whole triangle (fallback of the rare clipped triangle that finds the
@@ -176,32 +221,59 @@ __device__ __forceinline__ bool tile_empty(const TriRec& r, uint32_t px, uint32_
            tile_max_edge(e2, r.A01, r.B01) < 0;
 }
 
-// Rasterizes the tiles of [x0, x0 + 4*tilesX) x [y0, y0 + 4*tilesY) that are not provably empty:
-// 32 tiles are tested at a time (one per lane), then the surviving tiles are shaded two at a time.
+// True if the tile at (px, py) (4-aligned) can be shaded for r: some sample may pass the edges
+// and, when a depth bound is kept, r may beat the tile's depth bound somewhere. *known receives
+// the bound read (for the later update).
+__device__ __forceinline__ bool tile_live(const TriRec& r, uint32_t px, uint32_t py, const uint32_t* tileMin,
+                                          uint32_t tilesPerRow, uint32_t* known) {
+    if (tile_empty(r, px, py)) return false;
+    if (!tileMin) return true;
+    *known = tileMin[(py >> 2) * tilesPerRow + (px >> 2)];
+    return float_order(tile_depth_bound(r, px, py)) >= *known;
+}
+
+// Shades the live tiles of the warp-wide candidate set (the lanes in `mask` hold a tile origin
+// tpx/tpy, its depth bound tmin and a triangle selector rsel for rec()), two tiles per step, and
+// raises the tiles' depth bounds.
+template <class Rec>
+__device__ __forceinline__ void shade_live_tiles(Rec&& rec, uint32_t rsel, unsigned mask, uint32_t tpx, uint32_t tpy,
+                                                 uint32_t tmin, unsigned long long* keys, uint32_t* tileMin, uint32_t width,
+                                                 int lane) {
+    const uint32_t half = lane >> 4, tw = width >> 2;
+    while (mask) {
+        const int s0 = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int s1 = mask ? __ffs(mask) - 1 : -1;
+        if (s1 >= 0) mask &= mask - 1;
+        const int src = half ? s1 : s0;
+        const uint32_t qx = __shfl_sync(0xFFFFFFFFu, tpx, src & 31);
+        const uint32_t qy = __shfl_sync(0xFFFFFFFFu, tpy, src & 31);
+        const uint32_t qm = __shfl_sync(0xFFFFFFFFu, tmin, src & 31);
+        const uint32_t qr = __shfl_sync(0xFFFFFFFFu, rsel, src & 31);
+        uint32_t obs = 0;
+        if (src >= 0) obs = shade_tile_pixel(rec(qr), qx, qy, lane & 15, keys, width);
+        if (tileMin) update_tile_min(obs, tileMin, (qy >> 2) * tw + (qx >> 2), qm, src >= 0, lane);
+    }
+}
+
+// Rasterizes the tiles of [x0, x0 + 4*tilesX) x [y0, y0 + 4*tilesY) that are not provably empty
+// or hidden: 32 tiles are tested at a time (one per lane), then the surviving tiles are shaded two
+// at a time.
 __device__ __forceinline__ void raster_region(const TriRec& r, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
-                                              unsigned long long* keys, uint32_t width, int lane) {
+                                              unsigned long long* keys, uint32_t* tileMin, uint32_t width, int lane) {
     const int T = tilesX * tilesY;
-    const uint32_t half = lane >> 4;
+    const uint32_t tw = width >> 2;
     for (int tb = 0; tb < T; tb += 32) {
         const int t = tb + lane;
         bool live = false;
-        uint32_t tpx = 0, tpy = 0;
+        uint32_t tpx = 0, tpy = 0, tmin = 0;
         if (t < T) {
             int ty = t / tilesX, tx = t - ty * tilesX;
             tpx = x0 + tx * 4, tpy = y0 + ty * 4;
-            live = !tile_empty(r, tpx, tpy);
+            live = tile_live(r, tpx, tpy, tileMin, tw, &tmin);
         }
-        unsigned mask = __ballot_sync(0xFFFFFFFFu, live);
-        while (mask) {
-            int s0 = __ffs(mask) - 1;
-            mask &= mask - 1;
-            int s1 = mask ? __ffs(mask) - 1 : -1;
-            if (s1 >= 0) mask &= mask - 1;
-            const int src = half ? s1 : s0;
-            const uint32_t qx = __shfl_sync(0xFFFFFFFFu, tpx, src & 31);
-            const uint32_t qy = __shfl_sync(0xFFFFFFFFu, tpy, src & 31);
-            if (src >= 0) shade_tile_pixel(r, qx, qy, lane & 15, keys, width);
-        }
+        shade_live_tiles([&](uint32_t) -> const TriRec& { return r; }, 0, __ballot_sync(0xFFFFFFFFu, live), tpx, tpy, tmin,
+                         keys, tileMin, width, lane);
     }
 }
 
@@ -266,12 +338,14 @@ __device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t out
 }
 
 // ------------------------------------------------------------------ kernels
-// Per-warp shared memory: transformed vertices, index bytes, triangle records and the view.
+// Per-warp shared memory: transformed vertices, index bytes, triangle records, the view, and the
+// owner lane of each tile in the concatenated tile list of the round's small triangles.
 struct WarpSmem {
     float4 pos[64];
     uint32_t idx[96];
     TriRec tris[32];
     ViewParams view;
+    uint8_t owner[32 * kSmallTiles];
 };
 
 // Mesh stage. A work item is one meshlet of one view: a single-view draw numbers its meshlets
@@ -295,7 +369,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
             for (int k = 0; k < 16; k++) v.m[k] = a.m[k];
             v.halfW = a.halfW, v.halfH = a.halfH, v.width = a.width, v.height = a.height;
             v.bx = a.bx, v.by = a.by, v.meshletOffset = a.meshletOffset, v.count = a.count;
-            v.keys = a.keys, v.cullBitmap = a.cullBitmap;
+            v.keys = a.keys, v.cullBitmap = a.cullBitmap, v.tileMin = a.tileMin;
             S.view = v;
         }
         curView = 0;
@@ -432,19 +506,27 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
             }
             const int excl = incl - myTiles;
             const int total = __shfl_sync(0xFFFFFFFFu, incl, 31);
-            const uint32_t half = lane >> 4;
-            for (int b = 0; b < total; b += 2) {
-                const unsigned m0 = __ballot_sync(0xFFFFFFFFu, incl > b);
-                const unsigned m1 = __ballot_sync(0xFFFFFFFFu, incl > b + 1);
-                const int owner = __ffs(half ? m1 : m0) - 1;
-                const int ownerExcl = __shfl_sync(0xFFFFFFFFu, excl, owner & 31);
-                if (owner >= 0) {
-                    const TriRec& r = tris[owner];
-                    const int tile = b + (int)half - ownerExcl;
+            for (int k = 0; k < myTiles; k++) S.owner[excl + k] = (uint8_t)lane;
+            __syncwarp();
+            // 32 tiles at a time: lane j tests tile b + j of the list (empty or hidden tiles are
+            // dropped), then the live ones are shaded two per step.
+            const uint32_t tw = vp.width >> 2;
+            for (int b = 0; b < total; b += 32) {
+                const int t = b + lane;
+                const uint32_t own = t < total ? S.owner[t] : 0u;
+                const int ownerExcl = __shfl_sync(0xFFFFFFFFu, excl, own);
+                bool live = false;
+                uint32_t tpx = 0, tpy = 0, tmin = 0;
+                if (t < total) {
+                    const TriRec& r = tris[own];
+                    const int tile = t - ownerExcl;
                     const int tilesX = r.pad & 0xFF, magic = r.pad >> 8;
                     const int ty = (tile * magic) >> 8, tx = tile - ty * tilesX;
-                    shade_tile_pixel(r, (r.bbMin & 0xFFFF) + tx * 4, (r.bbMin >> 16) + ty * 4, lane & 15, vp.keys, vp.width);
+                    tpx = (r.bbMin & 0xFFFF) + tx * 4, tpy = (r.bbMin >> 16) + ty * 4;
+                    live = tile_live(r, tpx, tpy, vp.tileMin, tw, &tmin);
                 }
+                shade_live_tiles([&](uint32_t q) -> const TriRec& { return tris[q]; }, own, __ballot_sync(0xFFFFFFFFu, live),
+                                 tpx, tpy, tmin, vp.keys, vp.tileMin, vp.width, lane);
             }
             // Triangles the full queue turned away are rasterized here by the whole warp.
             unsigned ovMask = __ballot_sync(0xFFFFFFFFu, overflow);
@@ -454,7 +536,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                 const TriRec r = tris[src];
                 const uint32_t x0 = r.bbMin & 0xFFFF, y0 = r.bbMin >> 16;
                 raster_region(r, x0, y0, (int)(((r.bbMax & 0xFFFF) - x0) >> 2), (int)(((r.bbMax >> 16) - y0) >> 2),
-                              vp.keys, vp.width, lane);
+                              vp.keys, vp.tileMin, vp.width, lane);
             }
             __syncwarp();
         }
@@ -473,7 +555,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
 // triangle carries its view in pad (batched draws) or belongs to the single view.
 __global__ void __launch_bounds__(256) k_raster_big(const TriRec* __restrict__ big, const unsigned long long* __restrict__ bigBase,
                                                     const unsigned long long* control, uint32_t capacity,
-                                                    unsigned long long* keys, uint32_t width,
+                                                    unsigned long long* keys, uint32_t* tileMin, uint32_t width,
                                                     const ViewParams* __restrict__ views, uint32_t chunk) {
     const unsigned long long q = control[1];
     const uint32_t n = (uint32_t)min((unsigned long long)capacity, q >> 40);
@@ -494,8 +576,9 @@ __global__ void __launch_bounds__(256) k_raster_big(const TriRec* __restrict__ b
         }
         const TriRec r = big[lo];
         unsigned long long* vkeys = keys;
+        uint32_t* vtiles = tileMin;
         uint32_t vwidth = width;
-        if (views) vkeys = views[r.pad].keys, vwidth = views[r.pad].width;
+        if (views) vkeys = views[r.pad].keys, vtiles = views[r.pad].tileMin, vwidth = views[r.pad].width;
         const uint32_t c = (uint32_t)(w - bigBase[lo]);
         const uint32_t minX = r.bbMin & 0xFFFF, minY = r.bbMin >> 16, maxX = r.bbMax & 0xFFFF, maxY = r.bbMax >> 16;
         const uint32_t chunksX = (((maxX - minX) >> 2) + chunk - 1) / chunk;
@@ -503,18 +586,31 @@ __global__ void __launch_bounds__(256) k_raster_big(const TriRec* __restrict__ b
         const uint32_t x0 = minX + cx * (chunk * 4), y0 = minY + cy * (chunk * 4);
         const uint32_t x1 = min(x0 + chunk * 4, maxX), y1 = min(y0 + chunk * 4, maxY);
         // Empty tiles of the chunk are rejected by their corner samples inside raster_region.
-        raster_region(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys, vwidth, lane);
+        raster_region(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys, vtiles, vwidth, lane);
     }
 }
 
-__global__ void k_init_keys(const uint32_t* __restrict__ depth, unsigned long long* __restrict__ keys, uint32_t n) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        keys[i] = ((unsigned long long)float_order(__uint_as_float(depth[i])) << 32) | kKeyEmptyLow;
+// Keys from a depth layer (pre-existing depth: low word kKeyEmptyLow) and, when kept, each tile's
+// depth bound as the minimum over its 16 pixels (a tile is 16 consecutive words; the grid stride
+// is a multiple of 16, so a half-warp always covers one tile).
+__global__ void k_init_keys(const uint32_t* __restrict__ depth, unsigned long long* __restrict__ keys,
+                            uint32_t* __restrict__ tileMin, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        uint32_t hi = float_order(__uint_as_float(depth[i]));
+        keys[i] = ((unsigned long long)hi << 32) | kKeyEmptyLow;
+        if (tileMin) {
+            const unsigned half = 0xFFFFu << (threadIdx.x & 16);
+#pragma unroll
+            for (int o = 8; o > 0; o >>= 1) hi = min(hi, __shfl_xor_sync(half, hi, o));
+            if ((i & 15) == 0) tileMin[i >> 4] = hi;
+        }
+    }
 }
 
 __global__ void k_clear(uint32_t* __restrict__ l0, uint32_t* __restrict__ l1, unsigned long long* __restrict__ keys,
-                        uint32_t n, uint32_t color, uint32_t depthBits) {
-    const unsigned long long key = ((unsigned long long)float_order(__uint_as_float(depthBits)) << 32) | kKeyEmptyLow;
+                        uint32_t* __restrict__ tileMin, uint32_t n, uint32_t color, uint32_t depthBits) {
+    const uint32_t hi = float_order(__uint_as_float(depthBits));
+    const unsigned long long key = ((unsigned long long)hi << 32) | kKeyEmptyLow;
     for (uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) * 4; i < n; i += gridDim.x * blockDim.x * 4) {
         // n is a multiple of 16 (4x4 tiles), so the 16-byte vectors never straddle the end
         *(uint4*)&l0[i] = make_uint4(color, color, color, color);
@@ -523,6 +619,7 @@ __global__ void k_clear(uint32_t* __restrict__ l0, uint32_t* __restrict__ l1, un
             *(ulonglong2*)&keys[i] = make_ulonglong2(key, key);
             *(ulonglong2*)&keys[i + 2] = make_ulonglong2(key, key);
         }
+        if (tileMin && (i & 15) == 0) tileMin[i >> 4] = hi;
     }
 }
 
@@ -575,20 +672,20 @@ void launch_draw(const DrawArgs& a, cudaStream_t st, int numSMs) {
     }
     {
         LaunchScope ls("k_raster_big", st);
-        k_raster_big<<<numSMs * 8, 256, 0, st>>>(a.s.big, a.s.bigBase, a.s.control, a.s.bigCapacity, a.keys, a.width,
-                                                 a.views, chunk);
+        k_raster_big<<<numSMs * 8, 256, 0, st>>>(a.s.big, a.s.bigBase, a.s.control, a.s.bigCapacity, a.keys, a.tileMin,
+                                                 a.width, a.views, chunk);
     }
 }
 
-void launch_init_keys(const uint32_t* depthLayer, unsigned long long* keys, uint32_t n, cudaStream_t st) {
+void launch_init_keys(const uint32_t* depthLayer, unsigned long long* keys, uint32_t* tileMin, uint32_t n, cudaStream_t st) {
     LaunchScope ls("k_init_keys", st);
-    k_init_keys<<<grid_for(n, 1, 256), 256, 0, st>>>(depthLayer, keys, n);
+    k_init_keys<<<grid_for(n, 1, 256), 256, 0, st>>>(depthLayer, keys, tileMin, n);
 }
 
-void launch_clear(uint32_t* l0, uint32_t* l1, unsigned long long* keys, uint32_t n, uint32_t color, uint32_t depthBits,
-                  cudaStream_t st) {
+void launch_clear(uint32_t* l0, uint32_t* l1, unsigned long long* keys, uint32_t* tileMin, uint32_t n, uint32_t color,
+                  uint32_t depthBits, cudaStream_t st) {
     LaunchScope ls("k_clear", st);
-    k_clear<<<grid_for(n, 4, 256), 256, 0, st>>>(l0, l1, keys, n, color, depthBits);
+    k_clear<<<grid_for(n, 4, 256), 256, 0, st>>>(l0, l1, keys, tileMin, n, color, depthBits);
 }
 
 void launch_fill(uint32_t* dst, uint32_t n, uint32_t value, cudaStream_t st) {
