@@ -43,7 +43,7 @@ static_assert(sizeof(TriRec) == 64, "TriRec");
 // Per-rasterizer device scratch, reused by every draw.
 struct DrawScratch {
     unsigned long long* control;   // [0] meshlet work counter, [1] big-triangle queue (slots<<40 | chunks),
-                                   // [2] status flags, [3..6] perf counters
+                                   // [2] status flags, [3..6] perf counters, [8] chunk-stage cursor
     TriRec* big;                   // queue of triangles rasterized by the chunk kernel
     unsigned long long* bigBase;   // first chunk index of each queued triangle
     uint32_t bigCapacity;

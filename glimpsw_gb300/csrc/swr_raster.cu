@@ -376,6 +376,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
         __syncwarp();
     }
     unsigned long long nProcessed = 0, nRaster = 0, nClipped = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.s.control[8] = 0;  // the chunk stage's cursor (runs after this kernel)
 
     // Work items are fetched kFetch at a time: one contended atomic per kFetch items.
     constexpr uint32_t kFetch = 4;
@@ -551,10 +552,13 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     }
 }
 
-// Chunk stage: warps take chunk-sized pieces (chunk x chunk tiles) of queued triangles; a queued
+// Chunk stage: warps take runs of kChunkRun consecutive chunks (chunk x chunk tiles) of the queued
+// triangles from a global cursor (control[8], zeroed by the mesh stage), locate the run's first
+// chunk by binary search over the queue's chunk prefix and walk the rest sequentially. A queued
 // triangle carries its view in pad (batched draws) or belongs to the single view.
+constexpr uint32_t kChunkRun = 8;
 __global__ void __launch_bounds__(256) k_raster_big(const TriRec* __restrict__ big, const unsigned long long* __restrict__ bigBase,
-                                                    const unsigned long long* control, uint32_t capacity,
+                                                    unsigned long long* control, uint32_t capacity,
                                                     unsigned long long* keys, uint32_t* tileMin, uint32_t width,
                                                     const ViewParams* __restrict__ views, uint32_t chunk) {
     const unsigned long long q = control[1];
@@ -566,27 +570,41 @@ __global__ void __launch_bounds__(256) k_raster_big(const TriRec* __restrict__ b
     const int lastTY = (int)(((last.bbMax >> 16) - (last.bbMin >> 16)) >> 2);
     const unsigned long long total = bigBase[n - 1] + (unsigned long long)((lastTX + chunk - 1) / chunk) *
                                                           ((lastTY + chunk - 1) / chunk);
-    const unsigned long long nWarps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
-    for (unsigned long long w = (unsigned long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); w < total; w += nWarps) {
-        // largest slot with bigBase[slot] <= w
-        uint32_t lo = 0, hi = n - 1;
-        while (lo < hi) {
-            uint32_t mid = (lo + hi + 1) >> 1;
-            if (bigBase[mid] <= w) lo = mid; else hi = mid - 1;
+    while (true) {
+        unsigned long long w0 = 0;
+        if (lane == 0) w0 = atomicAdd(&control[8], (unsigned long long)kChunkRun);
+        w0 = __shfl_sync(0xFFFFFFFFu, w0, 0);
+        if (w0 >= total) break;
+        const unsigned long long w1 = min(w0 + kChunkRun, total);
+        // largest slot with bigBase[slot] <= w0
+        uint32_t slot = 0, hi = n - 1;
+        while (slot < hi) {
+            uint32_t mid = (slot + hi + 1) >> 1;
+            if (bigBase[mid] <= w0) slot = mid; else hi = mid - 1;
         }
-        const TriRec r = big[lo];
-        unsigned long long* vkeys = keys;
-        uint32_t* vtiles = tileMin;
-        uint32_t vwidth = width;
-        if (views) vkeys = views[r.pad].keys, vtiles = views[r.pad].tileMin, vwidth = views[r.pad].width;
-        const uint32_t c = (uint32_t)(w - bigBase[lo]);
-        const uint32_t minX = r.bbMin & 0xFFFF, minY = r.bbMin >> 16, maxX = r.bbMax & 0xFFFF, maxY = r.bbMax >> 16;
-        const uint32_t chunksX = (((maxX - minX) >> 2) + chunk - 1) / chunk;
-        const uint32_t cy = c / chunksX, cx = c - cy * chunksX;
-        const uint32_t x0 = minX + cx * (chunk * 4), y0 = minY + cy * (chunk * 4);
-        const uint32_t x1 = min(x0 + chunk * 4, maxX), y1 = min(y0 + chunk * 4, maxY);
-        // Empty tiles of the chunk are rejected by their corner samples inside raster_region.
-        raster_region(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys, vtiles, vwidth, lane);
+        TriRec r = big[slot];
+        unsigned long long base = bigBase[slot];
+        unsigned long long next = slot + 1 < n ? bigBase[slot + 1] : total;
+        for (unsigned long long w = w0; w < w1; w++) {
+            while (w >= next) {  // the run crossed into the next triangle(s)
+                slot++;
+                base = next;
+                next = slot + 1 < n ? bigBase[slot + 1] : total;
+                if (w < next) r = big[slot];
+            }
+            unsigned long long* vkeys = keys;
+            uint32_t* vtiles = tileMin;
+            uint32_t vwidth = width;
+            if (views) vkeys = views[r.pad].keys, vtiles = views[r.pad].tileMin, vwidth = views[r.pad].width;
+            const uint32_t c = (uint32_t)(w - base);
+            const uint32_t minX = r.bbMin & 0xFFFF, minY = r.bbMin >> 16, maxX = r.bbMax & 0xFFFF, maxY = r.bbMax >> 16;
+            const uint32_t chunksX = (((maxX - minX) >> 2) + chunk - 1) / chunk;
+            const uint32_t cy = c / chunksX, cx = c - cy * chunksX;
+            const uint32_t x0 = minX + cx * (chunk * 4), y0 = minY + cy * (chunk * 4);
+            const uint32_t x1 = min(x0 + chunk * 4, maxX), y1 = min(y0 + chunk * 4, maxY);
+            // Empty and hidden tiles of the chunk are rejected inside raster_region.
+            raster_region(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys, vtiles, vwidth, lane);
+        }
     }
 }
 
