@@ -58,6 +58,8 @@ def parse():
     p.add_argument("--neural-level-weighting", type=int, default=1, choices=[0, 1, 2],
                    help="training texture level l drawn with weight 2^(w*(5-l)): 2 by texel count, 1 by edge, 0 uniform")
     p.add_argument("--materials", type=int, default=64)
+    p.add_argument("--no-combined", action="store_true")
+    p.add_argument("--combined-copies", type=int, default=10, help="copies of the 100k-meshlet volume (10: 1M meshlets)")
     p.add_argument("--neural-width", type=int, default=2560)
     p.add_argument("--neural-height", type=int, default=1440)
     p.add_argument("--only", default="all", choices=["all", "neural"],
@@ -331,6 +333,97 @@ def multiview_section(args, api, stream):
             "autotuned": {"chunk_px": best[0] * 4, "warps_per_block": best[1],
                           "candidates_ms": {f"{cc * 4}px/{w}w": round(t, 4) for (cc, w), t in timings.items()}},
             "triangles_processed": int(c[0]), "gtri_per_s": float(c[0]) / (batched_ms / 1e3) / 1e9}
+
+
+# ----------------------------------------------------------------------------- combined stress
+def combined_section(args, api, stream):
+    """Combined stress workload: 1M meshlets (10 translated copies of the volume construction,
+    124M triangles, 1.73 GB of meshlet records), 256 materials of two 2048^2 RGBA8 layers, 16 views
+    of 1280x720..2880x1620. One batched graph launch (autotuned chunk size and warps per block)
+    draws every view; each view is then resolved with the learned decoder (trained on the 256
+    materials). Reports the batched raster time, the neural resolve time of all views, Gtri/s,
+    HBM GB/s of the raster (algorithmic bytes: 1168 B per drawn meshlet + 16 B per pixel) and
+    whether two views are bit-identical to single-view draws."""
+    import torch
+
+    from glimpsw_gb300 import autotune, scenes
+    t0 = time.perf_counter()
+    sc = scenes.combined_scene(copies=args.combined_copies, texture_size=args.texture_size)
+    scene_s = time.perf_counter() - t0
+    n = len(sc.meshlets)
+    scene = api.Scene()
+    scene.upload_meshlets(sc.meshlets)
+    texs, env = make_gpu_textures(sc, api)
+    scene.set_materials(sc.materials, texs)
+    rast = api.Rasterizer()
+    rast.EnableBinning = False
+    fbs = [api.Framebuffer(v.width, v.height, 3) for v in sc.views]
+    views = [(fb, v.proj, v.view, scenes.IDENTITY, False) for fb, v in zip(fbs, sc.views)]
+    batch = api.Batch(rast, scene, views)
+    gpu = torch.cuda.get_device_name()
+    best, _ = autotune.tune(batch, key=autotune.workload_key(gpu, views, n), repeats=2)
+
+    def timed(fn, steps):
+        for _ in range(2):
+            fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(steps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return float(np.median(ms))
+
+    raster_ms = timed(batch.render, args.steps)
+    batch.reset_counters()
+    batch.render()
+    c = batch.counters()
+    pixels = sum(v.width * v.height for v in sc.views)
+    drawn = int(c[0]) // 124
+    raster_bytes = drawn * 1168 + pixels * 16
+    # the learned decoder over the 256 materials, then the neural resolve of every view
+    model = api.NeuralMaterials(texs, latent_levels=4, seed=1)
+    t1 = time.perf_counter()
+    model.train(args.neural_steps, batch=args.neural_batch, materials_per_step=8,
+                level_weighting=args.neural_level_weighting)
+    torch.cuda.synchronize()
+    train_s = time.perf_counter() - t1
+    lights = [api.SwrLight()]
+    lights[0].type, lights[0].intensity = 0, 1500.0
+    lights[0].direction[:] = default_lights().tolist()
+    lights[0].color[:] = [1.0, 1.0, 1.0]
+    ctxs = [api.ShadingContext(scene, v.world_to_clip, world_to_clip=v.world_to_clip, skybox=env, view_pos=v.eye,
+                               lights=lights) for v in sc.views]
+
+    def frame():
+        batch.render()
+        for ctx, fb in zip(ctxs, fbs):
+            ctx.resolve_neural(rast, fb, model)
+
+    frame_ms = timed(frame, args.steps)
+    # two views against single-view draws (clear, frustum cull, draw)
+    batch.render()
+    exact = True
+    for k in (0, len(sc.views) - 1):
+        v, fb = sc.views[k], fbs[k]
+        ref = api.Framebuffer(v.width, v.height)
+        ref.clear(0xFF000000, 0.0)
+        bm = torch.zeros((n + 15) // 16, dtype=torch.int16, device="cuda")
+        api.cull_meshlets(scene, 0, n, bm, v.proj, v.view, scenes.IDENTITY, v.view, v.width, v.height, None)
+        rast.draw_meshlets(ref, n, api.ShadingContext(scene, v.world_to_clip, cull_bitmap=bm))
+        exact = exact and np.array_equal(fb.get_pixels(0), ref.get_pixels(0)) and \
+            np.array_equal(fb.get_pixels(1), ref.get_pixels(1))
+    peak, peak_kind = peaks()
+    return {"meshlets": n, "triangles": n * 124, "meshlet_bytes": int(sc.meshlets.nbytes), "materials": len(sc.materials),
+            "views": len(sc.views), "sizes": [[v.width, v.height] for v in sc.views], "pixels": pixels,
+            "scene_build_s": scene_s, "autotuned": {"chunk_px": best[0] * 4, "warps_per_block": best[1]},
+            "batched_raster_ms": raster_ms, "frame_ms_raster_plus_neural_resolve": frame_ms,
+            "triangles_processed": int(c[0]), "gtri_per_s": float(c[0]) / (raster_ms / 1e3) / 1e9,
+            "raster_hbm_gbs": raster_bytes / (raster_ms / 1e3) / 1e9, "hbm_peak_gbs": peak, "peak_kind": peak_kind,
+            "decoder_train_s": train_s, "views_bit_identical_to_single_view_draws": bool(exact)}
 
 
 # ----------------------------------------------------------------------------- learned decoder
@@ -611,6 +704,9 @@ def run_ours(args):
     multiview = None
     if not args.no_multiview:
         multiview = multiview_section(args, api, stream)
+    combined = None
+    if not args.no_combined:
+        combined = combined_section(args, api, stream)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -638,7 +734,7 @@ def run_ours(args):
                 "e2e": {"value": float(np.median(e2e_ms)), "unit": UNIT, "h2d_bytes_per_step": int(sc.meshlets.nbytes),
                         "d2h_bytes_per_step": int(W * H * 4)},
                 "gpu_launches": int(launches), "clocks": clocks.summary(), "cpu_baseline": cpu,
-                "multiview": multiview, "neural": neural}
+                "multiview": multiview, "neural": neural, "combined": combined}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -402,3 +402,42 @@ def volume_scene(n: int = 100_000, width: int = 1920, height: int = 1080, n_mate
     v1 = make_view(width, height, eye=eye + np.array([0.4, 0.2, 0.6]), target=(1.0, 0.5, 0.0))
     return Scene(m, mats, texture_size, 2, [v0, v1], texture_seed=seed * 1000, env_size=env_size, texture_detail=True,
                  name=f"volume{n}@{width}x{height}")
+
+
+def combined_scene(copies: int = 10, base_n: int = 100_000, n_materials: int = 256, n_views: int = 16, seed: int = 5,
+                   texture_size: int = 2048, env_size: int = 1024, extent: float = 100.0) -> Scene:
+    """Combined stress workload: `copies` translated copies of the volume construction (base_n
+    meshlets in a (2*extent)^3 cube each) side by side on a grid in x and z, copy c using materials
+    (m % 64) + 64 * (c % (n_materials / 64)), seen by n_views cameras above the field looking at
+    its centre, with 16:9 sizes log-uniform between 1280x720 and 2880x1620 (multiples of 4)."""
+    rng = np.random.default_rng(seed)
+    base = volume_scene(n=base_n, width=1280, height=720, n_materials=64, seed=seed, extent=extent).meshlets
+    cols = int(math.ceil(math.sqrt(copies)))
+    rows = int(math.ceil(copies / cols))
+    groups = max(1, n_materials // 64)
+    out = np.zeros(copies * base_n, dtype=MESHLET_DTYPE)
+    for c in range(copies):
+        ox = (c % cols - (cols - 1) / 2.0) * 2.0 * extent
+        oz = (c // cols - (rows - 1) / 2.0) * 2.0 * extent
+        part = out[c * base_n:(c + 1) * base_n]
+        part[:] = base
+        part["Positions"][:, 0, :] += np.float32(ox)
+        part["Positions"][:, 2, :] += np.float32(oz)
+        for f in ("BoundCenter", "ConeApex"):
+            part[f][:, 0] += np.float32(ox)
+            part[f][:, 2] += np.float32(oz)
+        part["MaterialId"] = (base["MaterialId"] % 64) + 64 * (c % groups)
+    mats = np.zeros(n_materials, dtype=MATERIAL_DTYPE)
+    mats["texture"] = np.arange(n_materials)
+    mats["alpha_cutoff"] = 255
+    half_x, half_z = cols * extent, rows * extent
+    views = []
+    for i in range(n_views):
+        s = math.exp(rng.uniform(0.0, math.log(2880.0 / 1280.0)))
+        w, h = _round4(1280 * s), _round4(720 * s)
+        ang = 2 * math.pi * i / n_views + rng.uniform(-0.2, 0.2)
+        r = rng.uniform(0.6, 1.2) * max(half_x, half_z)
+        eye = (r * math.cos(ang), rng.uniform(0.3, 1.0) * extent, r * math.sin(ang))
+        views.append(make_view(w, h, eye=eye, target=(rng.uniform(-0.3, 0.3) * half_x, 0.0, rng.uniform(-0.3, 0.3) * half_z)))
+    return Scene(out, mats, texture_size, 2, views, texture_seed=seed * 1000, env_size=env_size, texture_detail=True,
+                 name=f"combined{copies * base_n}x{n_views}")

@@ -104,3 +104,15 @@ def test_batched_two_views_equal_single_view_draws(big):
         rast.draw_meshlets(ref, n, api.ShadingContext(g.scene, v.world_to_clip, cull_bitmap=bm))
         assert np.array_equal(fb.get_pixels(0), ref.get_pixels(0))
         assert np.array_equal(fb.get_pixels(1), ref.get_pixels(1))
+
+
+def test_combined_million_meshlets_view_bit_exact():
+    """One view of the combined stress scene (1M meshlets, 124M triangles) against the oracle."""
+    import os
+    sc = scenes.combined_scene(copies=10, texture_size=8, env_size=8)
+    v = min(sc.views, key=lambda q: q.width * q.height)
+    g = GpuRenderer(sc.meshlets, sc.materials)
+    gfb, gc = g.render(v.world_to_clip, v.width, v.height)
+    ofb, _ = render_oracle(sc.meshlets, sc.materials, v.world_to_clip, v.width, v.height, threads=os.cpu_count() or 1)
+    assert_visbuffer_equal(gfb, ofb)
+    assert gc[0] == 124_000_000 and gc[1] > 100_000
