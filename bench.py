@@ -62,6 +62,7 @@ def parse():
     p.add_argument("--combined-copies", type=int, default=10, help="copies of the 100k-meshlet volume (10: 1M meshlets)")
     p.add_argument("--neural-width", type=int, default=2560)
     p.add_argument("--neural-height", type=int, default=1440)
+    p.add_argument("--no-alpha", action="store_true")
     p.add_argument("--only", default="all", choices=["all", "neural"],
                    help="neural: only the learned-decoder section (for profiling runs; prints that section)")
     return p.parse_args()
@@ -105,7 +106,8 @@ def make_gpu_textures(sc, api):
     for i in range(len(sc.materials)):
         t = api.Texture2D(api.FORMAT_RGBA8U, sc.texture_size, sc.texture_size, 16, 2)
         for layer in range(2):
-            px = scenes.value_noise_rgba_torch(sc.texture_size, sc.texture_seed + i, layer=layer, detail=sc.texture_detail)
+            px = scenes.value_noise_rgba_torch(sc.texture_size, sc.texture_seed + i, layer=layer, detail=sc.texture_detail,
+                                               cutout=sc.texture_cutout(i, layer))
             t.set_pixels_device(px, layer)
             torch.cuda.synchronize()
         t.generate_mips()
@@ -188,7 +190,7 @@ def oracle_textures_from_host(sc):
         for layer in range(2):
             # torch on the CPU (multi-threaded) computes the same texels as scenes.value_noise_rgba
             px = scenes.value_noise_rgba_torch(sc.texture_size, sc.texture_seed + i, layer=layer, device="cpu",
-                                               detail=sc.texture_detail)
+                                               detail=sc.texture_detail, cutout=sc.texture_cutout(i, layer))
             t.set_pixels(px.numpy().view(np.uint32), layer)
         t.generate_mips()
         data.append(t.data.copy())
@@ -424,6 +426,86 @@ def combined_section(args, api, stream):
             "triangles_processed": int(c[0]), "gtri_per_s": float(c[0]) / (raster_ms / 1e3) / 1e9,
             "raster_hbm_gbs": raster_bytes / (raster_ms / 1e3) / 1e9, "hbm_peak_gbs": peak, "peak_kind": peak_kind,
             "decoder_train_s": train_s, "views_bit_identical_to_single_view_draws": bool(exact)}
+
+
+# ----------------------------------------------------------------------------- alpha-tested materials
+def alpha_section(args, api, stream, sc, texs, env, lights, flush):
+    """The headline frame with every second material alpha-tested (FS_EncodeSurfaceId<true>,
+    Shading.cpp:309-331): cutoff 128, double-sided, a noise alpha channel in layer 0 (like foliage
+    cards). Same meshlets, camera and frame (cull, draw, resolve, Hi-Z); reports the frame time,
+    the per-kernel split and the share of pixels showing alpha-tested materials."""
+    import torch
+
+    from glimpsw_gb300 import scenes
+    sca = scenes.volume_scene(n=args.meshlets, width=args.width, height=args.height, texture_size=args.texture_size,
+                              n_materials=args.materials, alpha_every=2)
+    texs_a = list(texs)
+    for i in range(len(sca.materials)):
+        if sca.texture_cutout(i, 0):
+            t = api.Texture2D(api.FORMAT_RGBA8U, sca.texture_size, sca.texture_size, 16, 2)
+            for layer in range(2):
+                px = scenes.value_noise_rgba_torch(sca.texture_size, sca.texture_seed + i, layer=layer,
+                                                   detail=sca.texture_detail, cutout=sca.texture_cutout(i, layer))
+                t.set_pixels_device(px, layer)
+                torch.cuda.synchronize()
+            t.generate_mips()
+            texs_a[i] = t
+    scene = api.Scene()
+    scene.upload_meshlets(sca.meshlets)
+    scene.set_materials(sca.materials, texs_a)
+    rast = api.Rasterizer()
+    rast.EnableBinning = False
+    v0 = sca.views[0]
+    W, H = v0.width, v0.height
+    fb = api.Framebuffer(W, H, 3)
+    n = len(sca.meshlets)
+    batches = [(off, min(BATCH, n - off)) for off in range(0, n, BATCH)]
+    bitmaps = [torch.zeros((cnt + 15) // 16, dtype=torch.int16, device="cuda") for _, cnt in batches]
+    hw, hh = api.hiz_texture_size(W, H)
+    hiz = api.Texture2D(api.FORMAT_R32F, hw, hh, 16, 1)
+
+    def draw():
+        fb.clear(0xFF000000, 0.0)
+        for (off, cnt), bm in zip(batches, bitmaps):
+            api.cull_meshlets(scene, off, cnt, bm, v0.proj, v0.view, scenes.IDENTITY, v0.view, W, H, None)
+            rast.draw_meshlets(fb, cnt, api.ShadingContext(scene, v0.world_to_clip, meshlet_offset=off, cull_bitmap=bm))
+
+    def frame():
+        draw()
+        ctx = api.ShadingContext(scene, v0.world_to_clip, world_to_clip=v0.world_to_clip, skybox=env,
+                                 view_pos=v0.eye, lights=lights)
+        ctx.resolve(rast, fb)
+        api.downsample_depth(fb, hiz)
+
+    for _ in range(max(3, args.warmup)):
+        frame()
+    torch.cuda.synchronize()
+    rast.reset_counters()
+    frame()
+    c = rast.counters()
+    api.profile_enable(True)
+    ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        frame()
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms.append(a.elapsed_time(b))
+    api.profile_enable(False)
+    per = {}
+    for name, t in api.profile_collect():
+        per[name] = per.get(name, 0.0) + t / args.steps
+    draw()  # the vis-buffer ids (the resolve overwrites layer 0 with colour)
+    ids = fb.get_pixels(0)
+    shown = ids != 0xFF000000
+    mat = sca.meshlets["MaterialId"].astype(np.int64)[np.minimum(ids, n * 128 - 1) // 128]
+    alpha_px = int((shown & (sca.materials["alpha_cutoff"][mat] < 255)).sum())
+    return {"frame_ms": float(np.mean(ms)), "kernels_ms_per_step": dict(sorted(per.items())),
+            "alpha_materials": int((sca.materials["alpha_cutoff"] < 255).sum()), "materials": len(sca.materials),
+            "cutoff": 128, "triangles_processed": int(c[0]), "triangles_rasterized": int(c[1]),
+            "pixels_showing_alpha_materials": alpha_px, "pixels_covered": int(shown.sum())}
 
 
 # ----------------------------------------------------------------------------- learned decoder
@@ -698,6 +780,9 @@ def run_ours(args):
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
 
     del pinned, host_img
+    alpha = None
+    if not args.no_alpha:
+        alpha = alpha_section(args, api, stream, sc, texs, env, lights, flush)
     neural = None
     if not args.no_neural:
         neural = neural_section(args, api, stream, sc, texs, env, scene, rast, lights)
@@ -734,7 +819,7 @@ def run_ours(args):
                 "e2e": {"value": float(np.median(e2e_ms)), "unit": UNIT, "h2d_bytes_per_step": int(sc.meshlets.nbytes),
                         "d2h_bytes_per_step": int(W * H * 4)},
                 "gpu_launches": int(launches), "clocks": clocks.summary(), "cpu_baseline": cpu,
-                "multiview": multiview, "neural": neural, "combined": combined}
+                "alpha": alpha, "multiview": multiview, "neural": neural, "combined": combined}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

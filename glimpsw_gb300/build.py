@@ -17,7 +17,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libswr_gb300.so")
 SOURCES = ["swr_api.cu", "swr_raster.cu", "swr_texture.cu", "swr_shade.cu", "swr_batch.cu", "swr_noalloc.cu",
            "swr_neural.cu", "swr_neural_api.cu"]
-HEADERS = ["swr_device.cuh", "swr_internal.h", "swr_tc.cuh", "swr_neural.h"]
+HEADERS = ["swr_device.cuh", "swr_internal.h", "swr_tc.cuh", "swr_neural.h", "swr_sample.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -103,6 +103,18 @@ swr_status size_queue(swr_rasterizer r, uint32_t count) {
     return SWR_OK;
 }
 
+// The alpha pass's work list holds one entry per work item of a draw (stream-ordered growth).
+swr_status size_alpha_list(swr_rasterizer r, uint32_t count) {
+    DrawScratch& s = r->scratch;
+    if (count <= s.alphaCapacity) return SWR_OK;
+    const uint32_t want = std::max(count, 1u << 16);
+    if (s.alphaList) SWR_CUDA(cudaFreeAsync(s.alphaList, t_stream));
+    s.alphaList = nullptr, s.alphaCapacity = 0;
+    SWR_CUDA(cudaMallocAsync(&s.alphaList, (size_t)want * sizeof(uint32_t), t_stream));
+    s.alphaCapacity = want;
+    return SWR_OK;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ tracing
@@ -201,6 +213,7 @@ swr_status swr_rasterizer_destroy(swr_rasterizer r) {
     cudaFree(r->scratch.control);
     cudaFree(r->scratch.big);  // cudaFree synchronises for stream-ordered allocations
     cudaFree(r->scratch.bigBase);
+    cudaFree(r->scratch.alphaList);
     if (r->hostStatus) cudaFreeHost(r->hostStatus);
     if (r->statusEvent) cudaEventDestroy(r->statusEvent);
     delete r;
@@ -377,6 +390,7 @@ swr_status swr_scene_upload_meshlets(swr_scene s, const void* meshlets, uint32_t
         }
         s->meshlets = p;
         s->capacity = cap;
+        s->version++;
     }
     if (count)
         SWR_CUDA(cudaMemcpyAsync(s->meshlets + (size_t)first * kMeshletSize, meshlets, (size_t)count * kMeshletSize,
@@ -388,6 +402,7 @@ swr_status swr_scene_upload_meshlets(swr_scene s, const void* meshlets, uint32_t
 swr_status swr_scene_set_materials(swr_scene s, const swr_material* materials, uint32_t count) {
     if (!s || (!materials && count)) return fail(SWR_EINVAL, "swr_scene_set_materials: bad argument");
     std::vector<DevMaterial> h(count);
+    bool hasAlpha = false;
     for (uint32_t i = 0; i < count; i++) {
         DevMaterial& d = h[i];
         memset(&d, 0, sizeof(d));
@@ -397,10 +412,13 @@ swr_status swr_scene_set_materials(swr_scene s, const swr_material* materials, u
             d.has_texture = 1;
             d.tex = materials[i].texture->d;
         }
+        hasAlpha = hasAlpha || material_alpha_tested(d);
     }
     cudaFree(s->materials);
     s->materials = nullptr;
     s->num_materials = 0;
+    s->hasAlpha = hasAlpha;
+    s->version++;
     if (count) {
         SWR_CUDA(cudaMalloc(&s->materials, count * sizeof(DevMaterial)));
         SWR_CUDA(cudaMemcpy(s->materials, h.data(), count * sizeof(DevMaterial), cudaMemcpyHostToDevice));
@@ -427,6 +445,7 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
     if (count == 0) return SWR_OK;
     swr_status st = ensure_scratch(r);
     if (st == SWR_OK) st = size_queue(r, count);
+    if (st == SWR_OK && sc->hasAlpha) st = size_alpha_list(r, count);
     if (st != SWR_OK) return st;
     if (!fb->keys_valid) {
         launch_init_keys(fb->layers + fb->layer_stride, fb->keys, fb->tileMin, fb->width * fb->height, t_stream);
@@ -452,6 +471,7 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
     a.keys = fb->keys;
     a.tileMin = fb->tileMin;
     a.s = r->scratch;
+    if (!sc->hasAlpha) a.s.alphaList = nullptr;  // no alpha pass
     SWR_CUDA(cudaMemsetAsync(r->scratch.control, 0, 3 * sizeof(unsigned long long), t_stream));
     launch_draw(a, t_stream, num_sms());
     SWR_CHECK_LAUNCH("swr_draw_meshlets");

@@ -97,6 +97,7 @@ struct swr_batch_t {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     unsigned long long kernelNodes = 0;
+    uint64_t sceneVersion = 0;     // scene->version the graph was recorded with
 };
 
 namespace {
@@ -155,6 +156,16 @@ swr_status upload_views(swr_batch b, const swr_view_desc* views) {
 // The frame, recorded once on a private stream into a graph (event tracing is paused while
 // capturing; the graph's kernels are counted at every replay).
 swr_status capture(swr_batch b) {
+    // the alpha pass's work list: one entry per (view, meshlet) work item
+    const uint32_t items = b->count * b->numViews;
+    if (b->scene->hasAlpha && b->scratch.alphaCapacity < items) {
+        cudaFree(b->scratch.alphaList);
+        b->scratch.alphaList = nullptr, b->scratch.alphaCapacity = 0;
+        cudaError_t e = cudaMalloc(&b->scratch.alphaList, (size_t)std::max(items, 1u) * sizeof(uint32_t));
+        if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_batch: alpha work list");
+        b->scratch.alphaCapacity = std::max(items, 1u);
+    }
+    b->sceneVersion = b->scene->version;
     cudaStream_t cs;
     cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_batch: stream");
@@ -174,6 +185,7 @@ swr_status capture(swr_batch b) {
         a.clipMode = (!b->rast->enable_binning && b->rast->enable_clipping) ? 1 : 0;
         a.countClipped = (b->rast->enable_binning || b->rast->enable_clipping) ? 1 : 0;
         a.s = b->scratch;
+        if (!b->scene->hasAlpha) a.s.alphaList = nullptr;  // no alpha pass
         a.views = b->dViews;
         a.viewStart = b->dViewStart;
         a.numViews = nv;
@@ -275,6 +287,7 @@ swr_status swr_batch_set_tuning(swr_batch b, uint32_t chunk_tiles, uint32_t warp
 
 swr_status swr_batch_render(swr_batch b) {
     if (!b) return swr_internal_fail(SWR_EINVAL, "swr_batch_render: NULL batch");
+    if (b->exec && b->sceneVersion != b->scene->version) drop_graph(b);  // meshlets or materials moved
     if (!b->exec) {
         swr_status st = capture(b);
         if (st != SWR_OK) return st;
@@ -319,6 +332,7 @@ swr_status swr_batch_destroy(swr_batch b) {
     cudaFree(b->scratch.control);
     cudaFree(b->scratch.big);
     cudaFree(b->scratch.bigBase);
+    cudaFree(b->scratch.alphaList);
     delete b;
     return SWR_OK;
 }

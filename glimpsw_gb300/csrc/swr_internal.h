@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -29,6 +30,14 @@ struct DevMaterial {
     DevTexture tex;
 };
 
+// True if a material's meshlets take the alpha-tested vis-buffer shader: FragmentShaderId 1 for
+// AlphaCutoff < 255 (Shading.cpp:305). A cutoff of 0 passes every texel and a material without a
+// texture is taken to pass every fragment (the reference dereferences the texture unconditionally),
+// so both draw as opaque.
+inline __host__ __device__ bool material_alpha_tested(const DevMaterial& m) {
+    return m.alpha_cutoff - 1u < 254u && m.has_texture;
+}
+
 // A triangle ready to rasterize: edge equations at pixel (0,0), depth plane and tie-break rank.
 struct TriRec {
     int32_t E0, E1, E2;
@@ -40,13 +49,34 @@ struct TriRec {
 };
 static_assert(sizeof(TriRec) == 64, "TriRec");
 
+// TriRec::pad bit of a queued triangle whose material is alpha-tested (FS_EncodeSurfaceId<true>);
+// the rest of pad is the view index.
+constexpr uint32_t kTriAlpha = 0x80000000u;
+
+// What the alpha test of a queued triangle needs besides its TriRec; stored in the queue slot
+// after it. Its bbMin/bbMax words overlay TriRec::bbMin/bbMax and are zero, so the slot owns no
+// chunks of its own.
+struct AlphaExt {
+    float W0, W0S, W1S, W2S;     // perspective terms (TriangleEdgeVars, Rasterizer.cpp:320-328)
+    float ru[3], rv[3];          // TriangleClipData rows of a clipped triangle (Rasterizer.cpp:455-458)
+    uint32_t tc0, tc1;           // packed half2 texcoords of vertices 0 and 1
+    uint32_t zero0, zero1;       // = 0 (bbMin, bbMax of the overlaid TriRec)
+    uint32_t tc2;                // texcoord of vertex 2
+    uint32_t material;           // material index | kTriAlpha when clipped
+};
+static_assert(sizeof(AlphaExt) == sizeof(TriRec) && offsetof(AlphaExt, zero0) == offsetof(TriRec, bbMin) &&
+                  offsetof(AlphaExt, zero1) == offsetof(TriRec, bbMax), "AlphaExt overlays TriRec");
+
 // Per-rasterizer device scratch, reused by every draw.
 struct DrawScratch {
     unsigned long long* control;   // [0] meshlet work counter, [1] big-triangle queue (slots<<40 | chunks),
-                                   // [2] status flags, [3..6] perf counters, [8] chunk-stage cursor
+                                   // [2] status flags, [3..6] perf counters, [8] chunk-stage cursor,
+                                   // [9] alpha list length, [10] alpha-pass cursor
     TriRec* big;                   // queue of triangles rasterized by the chunk kernel
     unsigned long long* bigBase;   // first chunk index of each queued triangle
     uint32_t bigCapacity;
+    uint32_t* alphaList;           // work items of alpha-tested meshlets (nullptr: the draw has none)
+    uint32_t alphaCapacity;
 };
 
 enum : unsigned long long { kStatusBigOverflow = 1ull, kStatusClipOverflow = 2ull };
@@ -134,6 +164,8 @@ struct swr_scene_t {
     uint32_t count, capacity;
     swr::DevMaterial* materials;
     uint32_t num_materials;
+    bool hasAlpha;                 // some material selects FS_EncodeSurfaceId<true> (swr::material_alpha_tested)
+    uint64_t version;              // bumped when meshlets or materials move (recorded draw graphs re-capture)
 };
 
 struct swr_texture_t {

@@ -1,18 +1,22 @@
 // Meshlet rasterizer kernels: mesh shader (ShadeMeshlet), clip codes, triangle setup, clipping and
-// vis-buffer rasterization (FS_EncodeSurfaceId<false>) for sm_103a.
+// vis-buffer rasterization (FS_EncodeSurfaceId<false> and, for alpha-tested materials,
+// FS_EncodeSurfaceId<true>) for sm_103a.
 //
 // Work decomposition:
 //   k_draw_meshlets  one warp per meshlet (dynamic fetch). Lanes transform the 64 vertices into
 //                    shared memory, then own one triangle each: clip codes, setup and edge
 //                    equations in registers. Triangles whose 4-aligned box covers at most
 //                    kSmallTiles 4x4 tiles are rasterized by the whole warp, two tiles (32 pixels)
-//                    per step; larger and clipped triangles go to a device queue.
+//                    per step; larger and clipped triangles, and every triangle of an
+//                    alpha-tested material, go to a device queue.
 //   k_raster_big     warps take 32x32-pixel chunks of queued triangles (flattened by a prefix of
 //                    chunk counts kept in the queue), reject empty chunks by their corners and
 //                    rasterize the rest two tiles per step.
 //   k_finalize       converts per-pixel keys to the reference's depth and surfaceId layers.
 // The depth test is a 64-bit atomicMax on (ordered depth, 0xFFFFFFFE - rank); the result is
-// independent of execution order and equals the single-threaded reference.
+// independent of execution order and equals the single-threaded reference. The alpha test is a
+// function of the triangle and the fragment alone, so it only removes fragments and keeps that
+// property.
 //
 // Tile depth culling: tileMin holds, per 4x4 tile, a lower bound of the depth words of its 16
 // keys (keys only grow, and tileMin only takes minima of values its pixels had reached). Before a
@@ -20,9 +24,11 @@
 // the triangle cannot win anywhere is skipped. The vis-buffer is unchanged (only fragments that
 // would fail the depth test are skipped), while the dense scenes' overdraw mostly disappears.
 #include <cfloat>
+#include <type_traits>
 
 #include "swr_device.cuh"
 #include "swr_internal.h"
+#include "swr_sample.cuh"
 
 namespace swr {
 
@@ -36,6 +42,7 @@ struct Vtx { float x, y, z, w; };
 struct Setup {
     uint32_t Pos0, Pos1, Pos2;
     float Z0, Z1, Z2;
+    float W0, W1, W2;  // 1 / w of the vertices (simd::perspective_div)
 };
 
 // TrianglePacket::GetBoundingBox / GetRenderBoundingBox (Rasterizer.cpp:331-351).
@@ -74,6 +81,7 @@ __device__ __forceinline__ bool tri_setup(Vtx v0, Vtx v1, Vtx v2, int halfW, int
     render_bbox(t, halfW, halfH, bbMin, bbMax);
     if (lo16(bbMin) >= lo16(bbMax) || hi16(bbMin) >= hi16(bbMax)) keep = false;
     t.Z0 = fmul(v0.z, rw0), t.Z1 = fmul(v1.z, rw1), t.Z2 = fmul(v2.z, rw2);
+    t.W0 = rw0, t.W1 = rw1, t.W2 = rw2;
     return keep;
 }
 
@@ -84,10 +92,10 @@ __device__ __forceinline__ int32_t compute_edge(int32_t a, int32_t x, int32_t b,
     return w >> 4;
 }
 
-// TriangleEdgeVars::Setup (Rasterizer.cpp:296-329), depth terms only (the opaque vis-buffer
-// shader does not read the perspective-correct barycentrics).
+// TriangleEdgeVars::Setup (Rasterizer.cpp:296-329), depth terms (the opaque vis-buffer shader
+// does not read the perspective-correct barycentrics; alpha_ext adds them from *rcpAreaOut).
 __device__ __forceinline__ void edge_setup(const Setup& t, int halfW, int halfH, uint32_t bbMin, uint32_t bbMax,
-                                           uint32_t rank, TriRec& r) {
+                                           uint32_t rank, TriRec& r, float* rcpAreaOut = nullptr) {
     int32_t x0 = lo16(t.Pos0), y0 = hi16(t.Pos0);
     int32_t x1 = lo16(t.Pos1), y1 = hi16(t.Pos1);
     int32_t x2 = lo16(t.Pos2), y2 = hi16(t.Pos2);
@@ -111,6 +119,7 @@ __device__ __forceinline__ void edge_setup(const Setup& t, int halfW, int halfH,
     r.bbMin = bbMin, r.bbMax = bbMax;
     r.lowword = 0xFFFFFFFEu - rank;
     r.pad = 0;
+    if (rcpAreaOut) *rcpAreaOut = rcpArea;
 }
 
 // ------------------------------------------------------------------ fragments
@@ -208,6 +217,168 @@ __device__ __forceinline__ bool enqueue_big(const TriRec& r, const DrawArgs& a, 
     return false;
 }
 
+// ------------------------------------------------------------------ alpha test
+// FS_EncodeSurfaceId<true> (Shading.cpp:309-331): after the depth test, the fragment's
+// perspective-correct barycentrics (Rasterizer.h:300-317, rcp14 modelled as 1/w) interpolate the
+// vertices' texcoords (FragmentVars::Interpolate = BaryLerp, Rasterizer.h:101-104), the material's
+// texture is sampled at the implicit LOD of the 4x4 tile (SampleImplicitLod, Texture.h:403-410,
+// with the 2x2 finite differences texutil::dFdx/dFdy, Texture.h:258-275) and the fragment survives
+// if the texel is >= AlphaCutoff << 24. Every sample of a visited tile takes part in the
+// differences and in the tile's filter choice, covered or not, as the reference's 16 lanes do.
+
+// Mesh::TexCoords[VertexId]. The index byte is not bounded by the reference, whose record holds
+// NormalTangents and Indices after the 64 texcoords: indices below 224 read that word of the
+// record, larger ones (the next record in the reference) read 0.
+__device__ __forceinline__ uint32_t texcoord_word(const uint8_t* mp, uint32_t idx) {
+    return idx < 224 ? *(const uint32_t*)(mp + kOffTexCoords + 4 * idx) : 0u;
+}
+
+// Alpha-test terms of a triangle from its setup (TriangleEdgeVars W terms, Rasterizer.cpp:320-328).
+__device__ __forceinline__ AlphaExt alpha_ext(const Setup& t, float rcpArea, uint32_t tc0, uint32_t tc1, uint32_t tc2,
+                                              uint32_t material) {
+    AlphaExt x;
+    x.W0 = t.W0;
+    x.W0S = fmul(t.W0, rcpArea), x.W1S = fmul(t.W1, rcpArea), x.W2S = fmul(t.W2, rcpArea);
+#pragma unroll
+    for (int k = 0; k < 3; k++) x.ru[k] = 0.0f, x.rv[k] = 0.0f;
+    x.tc0 = tc0, x.tc1 = tc1, x.tc2 = tc2;
+    x.zero0 = 0, x.zero1 = 0;
+    x.material = material;
+    return x;
+}
+
+struct TexCoord { float u, v; };
+
+// Interpolated texcoord of the sample whose edge values are (u, v) (as floats).
+__device__ __forceinline__ TexCoord alpha_texcoord(const AlphaExt& x, float u, float v) {
+    const float pw0 = ffma(fadd(u, v), -x.W0S, x.W0);
+    const float w = ffma(u, x.W1S, ffma(v, x.W2S, pw0));
+    float rcpW = fdiv(1.0f, w);
+    rcpW = fmul(rcpW, ffma(-w, rcpW, 2.0f));  // Newton-Raphson step
+    float bu = fmul(u, fmul(x.W1S, rcpW)), bv = fmul(v, fmul(x.W2S, rcpW));
+    if (x.material & kTriAlpha) {  // clipped: barycentrics of the source triangle
+        const float cu = ffma(bu, x.ru[1], ffma(bv, x.ru[2], x.ru[0]));
+        const float cv = ffma(bu, x.rv[1], ffma(bv, x.rv[2], x.rv[0]));
+        bu = cu, bv = cv;
+    }
+    const float b0 = fsub(fsub(1.0f, bu), bv);
+    TexCoord s;
+    s.u = ffma(h2f(x.tc0 & 0xFFFF), b0, ffma(h2f(x.tc1 & 0xFFFF), bu, fmul(h2f(x.tc2 & 0xFFFF), bv)));
+    s.v = ffma(h2f(x.tc0 >> 16), b0, ffma(h2f(x.tc1 >> 16), bu, fmul(h2f(x.tc2 >> 16), bv)));
+    return s;
+}
+
+// CalcMipLevel(grad) - LerpFracBits (Texture.h:271-275, 408) from the differences of the scaled
+// sample positions (d/dx su, d/dx sv, d/dy su, d/dy sv).
+__device__ __forceinline__ int32_t alpha_mip(float gx, float gy, float gz, float gw) {
+    const float dx = ffma(gx, gx, fmul(gy, gy)), dy = ffma(gz, gz, fmul(gw, gw));
+    return (ilog2_x86(vmax(dx, dy)) >> 1) - 8;
+}
+
+// shade_tile_pixel with the alpha test, called by all 32 lanes: each half-warp shades one tile of
+// the same triangle (valid is false on a half without a tile). The x and y differences pair
+// lanes l ^ 1 and l ^ 4 of a half.
+__device__ __forceinline__ uint32_t shade_tile_pixel_alpha(const TriRec& r, const AlphaExt& x, const DevTexture& tex,
+                                                           uint32_t cutoff, uint32_t tx, uint32_t ty, bool valid, int lane,
+                                                           unsigned long long* keys, uint32_t width) {
+    const uint32_t l = lane & 15;
+    unsigned long long* p = keys + (tx << 2) + ty * width + l;
+    const unsigned long long cur = valid ? *(volatile unsigned long long*)p : 0ull;
+    const uint32_t px = tx + (l & 3), py = ty + (l >> 2);
+    const int32_t e0 = (int32_t)((uint32_t)r.E0 + (uint32_t)r.A12 * px + (uint32_t)r.B12 * py);
+    const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
+    const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
+    const float u = __int2float_rn(e1), v = __int2float_rn(e2);
+    const float depth = ffma(u, r.Z10, ffma(v, r.Z20, r.Z0));
+    const unsigned long long key = ((unsigned long long)float_order(depth) << 32) | r.lowword;
+    bool pass = valid && (e0 | e1 | e2) >= 0 && depth == depth && key > cur;
+    if (__any_sync(0xFFFFFFFFu, pass)) {
+        const TexCoord s = alpha_texcoord(x, u, v);
+        const float su = fmul(s.u, tex.scale_lerp_u), sv = fmul(s.v, tex.scale_lerp_v);
+        const float sux = __shfl_xor_sync(0xFFFFFFFFu, su, 1), svx = __shfl_xor_sync(0xFFFFFFFFu, sv, 1);
+        const float suy = __shfl_xor_sync(0xFFFFFFFFu, su, 4), svy = __shfl_xor_sync(0xFFFFFFFFu, sv, 4);
+        const bool ox = l & 1, oy = l & 4;  // dFdx = p[l | 1] - p[l & ~1], dFdy = p[l | 4] - p[l & ~4]
+        const int32_t mip = alpha_mip(ox ? fsub(su, sux) : fsub(sux, su), ox ? fsub(sv, svx) : fsub(svx, sv),
+                                      oy ? fsub(su, suy) : fsub(suy, su), oy ? fsub(sv, svy) : fsub(svy, sv));
+        const bool nearest = (__ballot_sync(0xFFFFFFFFu, mip > 0) & (0xFFFFu << (lane & 16))) != 0;
+        if (pass) pass = sample_rgba8(tex, s.u, s.v, 0, mip, nearest) >= cutoff;
+    }
+    if (!pass) return (uint32_t)(cur >> 32);
+    atomicMax(p, key);
+    return (uint32_t)(key >> 32);
+}
+
+// One lane rasterizes a whole alpha-tested triangle, the 16 samples of each tile in turn
+// (fallback of a triangle that finds the queue full; slow but exact).
+__device__ __noinline__ void raster_serial_alpha(const TriRec& r, const AlphaExt& x, const DevMaterial* materials,
+                                                 unsigned long long* keys, uint32_t width) {
+    const DevMaterial& mt = materials[x.material & ~kTriAlpha];
+    const uint32_t cutoff = mt.alpha_cutoff << 24;
+    const uint32_t minX = r.bbMin & 0xFFFF, minY = r.bbMin >> 16, maxX = r.bbMax & 0xFFFF, maxY = r.bbMax >> 16;
+    for (uint32_t ty = minY; ty < maxY; ty += 4) {
+        for (uint32_t tx = minX; tx < maxX; tx += 4) {
+            float su[16], sv[16], tu[16], tv[16];
+            unsigned pass = 0;
+            for (uint32_t l = 0; l < 16; l++) {
+                const uint32_t px = tx + (l & 3), py = ty + (l >> 2);
+                const int32_t e0 = (int32_t)((uint32_t)r.E0 + (uint32_t)r.A12 * px + (uint32_t)r.B12 * py);
+                const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
+                const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
+                const float u = __int2float_rn(e1), v = __int2float_rn(e2);
+                const float depth = ffma(u, r.Z10, ffma(v, r.Z20, r.Z0));
+                const unsigned long long key = ((unsigned long long)float_order(depth) << 32) | r.lowword;
+                if ((e0 | e1 | e2) >= 0 && depth == depth && key > *(volatile unsigned long long*)(keys + (tx << 2) + ty * width + l))
+                    pass |= 1u << l;
+                const TexCoord s = alpha_texcoord(x, u, v);
+                tu[l] = s.u, tv[l] = s.v;
+                su[l] = fmul(s.u, mt.tex.scale_lerp_u), sv[l] = fmul(s.v, mt.tex.scale_lerp_v);
+            }
+            if (!pass) continue;
+            int32_t mip[16];
+            bool nearest = false;
+            for (uint32_t l = 0; l < 16; l++) {
+                const uint32_t lx = l & ~1u, hx = l | 1u, ly = l & ~4u, hy = l | 4u;
+                mip[l] = alpha_mip(fsub(su[hx], su[lx]), fsub(sv[hx], sv[lx]), fsub(su[hy], su[ly]), fsub(sv[hy], sv[ly]));
+                nearest |= mip[l] > 0;
+            }
+            for (uint32_t l = 0; l < 16; l++) {
+                if (!((pass >> l) & 1) || sample_rgba8(mt.tex, tu[l], tv[l], 0, mip[l], nearest) < cutoff) continue;
+                const uint32_t px = tx + (l & 3), py = ty + (l >> 2);
+                const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
+                const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
+                const float depth = ffma(__int2float_rn(e1), r.Z10, ffma(__int2float_rn(e2), r.Z20, r.Z0));
+                atomicMax(keys + (tx << 2) + ty * width + l, ((unsigned long long)float_order(depth) << 32) | r.lowword);
+            }
+        }
+    }
+}
+
+// Appends an alpha-tested triangle and its AlphaExt (in the next slot, which owns no chunks) to
+// the chunk queue; false when the queue is full (the caller rasterizes it). A pair that finds
+// one slot left leaves an empty record there, so every slot below the capacity is written.
+__device__ __forceinline__ bool enqueue_alpha(const TriRec& r, const AlphaExt& x, const DrawArgs& a, uint32_t chunk) {
+    const int tilesX = ((r.bbMax & 0xFFFF) - (r.bbMin & 0xFFFF)) >> 2;
+    const int tilesY = ((r.bbMax >> 16) - (r.bbMin >> 16)) >> 2;
+    const unsigned long long chunks = (unsigned long long)((tilesX + chunk - 1) / chunk) *
+                                      (unsigned long long)((tilesY + chunk - 1) / chunk);
+    const unsigned long long old = atomicAdd(&a.s.control[1], (2ull << 40) | chunks);
+    const unsigned long long slot = old >> 40, base = old & ((1ull << 40) - 1);
+    if (slot + 1 < a.s.bigCapacity) {
+        a.s.big[slot] = r;
+        a.s.big[slot + 1] = *(const TriRec*)&x;
+        a.s.bigBase[slot] = base;
+        a.s.bigBase[slot + 1] = base + chunks;
+        return true;
+    }
+    if (slot < a.s.bigCapacity) {
+        TriRec e = {};
+        a.s.big[slot] = e;
+        a.s.bigBase[slot] = base;
+    }
+    atomicOr(&a.s.control[2], kStatusBigOverflow);
+    return false;
+}
+
 // Largest value over the tile [px, px+3] x [py, py+3] of the affine edge function e(px, py) + A*dx + B*dy.
 __device__ __forceinline__ int32_t tile_max_edge(int32_t e, int32_t A, int32_t B) {
     return e + (A > 0 ? 3 * A : 0) + (B > 0 ? 3 * B : 0);
@@ -256,11 +427,36 @@ __device__ __forceinline__ void shade_live_tiles(Rec&& rec, uint32_t rsel, unsig
     }
 }
 
+// shade_live_tiles for alpha-tested triangles of one material (texture tex, cutoff << 24): a
+// candidate's triangle is tris[rsel], its alpha terms exts[rsel] (the two tiles of a step may
+// belong to different triangles).
+__device__ __forceinline__ void shade_live_tiles_alpha(const TriRec* tris, const AlphaExt* exts, uint32_t rsel,
+                                                       const DevTexture& tex, uint32_t cutoff, unsigned mask,
+                                                       uint32_t tpx, uint32_t tpy, uint32_t tmin,
+                                                       unsigned long long* keys, uint32_t* tileMin, uint32_t width,
+                                                       int lane) {
+    const uint32_t half = lane >> 4, tw = width >> 2;
+    while (mask) {
+        const int s0 = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int s1 = mask ? __ffs(mask) - 1 : -1;
+        if (s1 >= 0) mask &= mask - 1;
+        const int src = half ? s1 : s0;
+        const uint32_t qx = __shfl_sync(0xFFFFFFFFu, tpx, src & 31);
+        const uint32_t qy = __shfl_sync(0xFFFFFFFFu, tpy, src & 31);
+        const uint32_t qm = __shfl_sync(0xFFFFFFFFu, tmin, src & 31);
+        const uint32_t qr = __shfl_sync(0xFFFFFFFFu, rsel, src & 31);
+        const uint32_t obs = shade_tile_pixel_alpha(tris[qr], exts[qr], tex, cutoff, qx, qy, src >= 0, lane, keys, width);
+        if (tileMin) update_tile_min(obs, tileMin, (qy >> 2) * tw + (qx >> 2), qm, src >= 0, lane);
+    }
+}
+
 // Rasterizes the tiles of [x0, x0 + 4*tilesX) x [y0, y0 + 4*tilesY) that are not provably empty
-// or hidden: 32 tiles are tested at a time (one per lane), then the surviving tiles are shaded two
-// at a time.
-__device__ __forceinline__ void raster_region(const TriRec& r, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
-                                              unsigned long long* keys, uint32_t* tileMin, uint32_t width, int lane) {
+// or hidden: 32 tiles are tested at a time (one per lane), then shade(mask, tpx, tpy, tmin) shades
+// the surviving ones.
+template <class Shade>
+__device__ __forceinline__ void raster_region_with(const TriRec& r, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
+                                                   const uint32_t* tileMin, uint32_t width, int lane, Shade&& shade) {
     const int T = tilesX * tilesY;
     const uint32_t tw = width >> 2;
     for (int tb = 0; tb < T; tb += 32) {
@@ -272,21 +468,48 @@ __device__ __forceinline__ void raster_region(const TriRec& r, uint32_t x0, uint
             tpx = x0 + tx * 4, tpy = y0 + ty * 4;
             live = tile_live(r, tpx, tpy, tileMin, tw, &tmin);
         }
-        shade_live_tiles([&](uint32_t) -> const TriRec& { return r; }, 0, __ballot_sync(0xFFFFFFFFu, live), tpx, tpy, tmin,
-                         keys, tileMin, width, lane);
+        shade(__ballot_sync(0xFFFFFFFFu, live), tpx, tpy, tmin);
     }
+}
+
+// raster_region_with for an opaque triangle, two tiles per step.
+__device__ __forceinline__ void raster_region(const TriRec& r, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
+                                              unsigned long long* keys, uint32_t* tileMin, uint32_t width, int lane) {
+    raster_region_with(r, x0, y0, tilesX, tilesY, tileMin, width, lane,
+                       [&](unsigned mask, uint32_t tpx, uint32_t tpy, uint32_t tmin) {
+                           shade_live_tiles([&](uint32_t) -> const TriRec& { return r; }, 0, mask, tpx, tpy, tmin, keys,
+                                            tileMin, width, lane);
+                       });
+}
+
+// The same for the alpha-tested triangle *rp with alpha terms *xp (material texture tex, cutoff << 24).
+__device__ __forceinline__ void raster_region_alpha(const TriRec* rp, const AlphaExt* xp, const DevTexture& tex,
+                                                    uint32_t cutoff, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
+                                                    unsigned long long* keys, uint32_t* tileMin, uint32_t width, int lane) {
+    raster_region_with(*rp, x0, y0, tilesX, tilesY, tileMin, width, lane,
+                       [&](unsigned mask, uint32_t tpx, uint32_t tpy, uint32_t tmin) {
+                           shade_live_tiles_alpha(rp, xp, 0, tex, cutoff, mask, tpx, tpy, tmin, keys, tileMin, width, lane);
+                       });
 }
 
 // Clipper::ClipTriangles + FlushPacket (Rasterizer.cpp:398-491) for this lane's triangle; the
 // lanes of a packet are independent (each prim restarts its new-vertex slots). Fan outputs are
 // set up with TrianglePacket::Setup and queued with rank (packet, clipped, lane, fan index).
+// For an alpha-tested material (alphaMat != ~0u) the barycentric rows are clipped too and become
+// the outputs' TriangleClipData; the texcoords are those of the source triangle (record mp, index
+// bytes idxBytes).
 __device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t outcodes, const DrawArgs& a,
                                             const ViewParams& vp, uint32_t viewIndex, uint32_t chunk, int cullMode,
-                                            uint32_t gMeshlet, uint32_t prim, unsigned long long& nRaster) {
-    float V[4][16];  // x, y, z, w of the polygon's vertices (barycentric rows are not needed here)
+                                            uint32_t gMeshlet, uint32_t prim, unsigned long long& nRaster,
+                                            uint32_t alphaMat, const uint8_t* mp, const uint8_t* idxBytes) {
+    const bool alpha = alphaMat != ~0u;
+    const int rows = alpha ? 6 : 4;
+    float V[6][16];  // x, y, z, w and the barycentric u, v of the polygon's vertices
     V[0][0] = v0.x, V[1][0] = v0.y, V[2][0] = v0.z, V[3][0] = v0.w;
     V[0][1] = v1.x, V[1][1] = v1.y, V[2][1] = v1.z, V[3][1] = v1.w;
     V[0][2] = v2.x, V[1][2] = v2.y, V[2][2] = v2.z, V[3][2] = v2.w;
+    V[4][0] = 0.0f, V[4][1] = 1.0f, V[4][2] = 0.0f;
+    V[5][0] = 0.0f, V[5][1] = 0.0f, V[5][2] = 1.0f;
     uint8_t idx[16] = { 0, 1, 2 };
     uint32_t vertCount = 3, nextIdx = 3;
     const float guard[2] = { vp.bx, vp.by };
@@ -312,7 +535,7 @@ __device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t out
             if (da >= 0) out[outCount++] = (uint8_t)ia;
             if ((da >= 0) != (db >= 0)) {
                 float t = fdiv(da, fsub(da, db));
-                for (int k = 0; k < 4; k++) V[k][nextIdx] = ffma(V[k][ib], t, ffma(-t, V[k][ia], V[k][ia]));
+                for (int k = 0; k < rows; k++) V[k][nextIdx] = ffma(V[k][ib], t, ffma(-t, V[k][ia], V[k][ia]));
                 out[outCount++] = (uint8_t)nextIdx++;
             }
         }
@@ -330,16 +553,67 @@ __device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t out
         uint32_t bbMin, bbMax;
         if (!tri_setup(a0, a1, a2, vp.halfW, vp.halfH, cullMode, t, bbMin, bbMax)) continue;
         TriRec r;
-        edge_setup(t, vp.halfW, vp.halfH, bbMin, bbMax, make_rank(gMeshlet, prim, 1, vi), r);
+        float rcpArea;
+        edge_setup(t, vp.halfW, vp.halfH, bbMin, bbMax, make_rank(gMeshlet, prim, 1, vi), r, &rcpArea);
         r.pad = viewIndex;
-        if (!enqueue_big(r, a, chunk)) raster_serial(r, vp.keys, vp.width);
         nRaster++;
+        if (alpha) {
+            AlphaExt x = alpha_ext(t, rcpArea, texcoord_word(mp, idxBytes[prim]), texcoord_word(mp, idxBytes[128 + prim]),
+                                   texcoord_word(mp, idxBytes[256 + prim]), alphaMat | kTriAlpha);
+            const float u0 = V[4][i0], w0 = V[5][i0];  // TriangleClipData, Rasterizer.cpp:455-458
+            x.ru[0] = u0, x.ru[1] = fsub(V[4][i1], u0), x.ru[2] = fsub(V[4][i2], u0);
+            x.rv[0] = w0, x.rv[1] = fsub(V[5][i1], w0), x.rv[2] = fsub(V[5][i2], w0);
+            r.pad = viewIndex | kTriAlpha;
+            if (!enqueue_alpha(r, x, a, chunk)) raster_serial_alpha(r, x, a.materials, vp.keys, vp.width);
+            continue;
+        }
+        if (!enqueue_big(r, a, chunk)) raster_serial(r, vp.keys, vp.width);
     }
+}
+
+// Triangle p of a meshlet for one lane of a 32-triangle step: its clip-space vertices (the
+// meshlet's transformed vertices pos, gathered as simd::gather_preload64 does) and
+// Clipper::ComputeClipCodes (Rasterizer.cpp:353-397) per lane.
+struct LaneTri {
+    Vtx v0, v1, v2;
+    uint32_t partial;   // OR of the vertices' out codes
+    bool acc, nontriv;  // trivially accepted / accepted but needs clipping
+};
+__device__ __forceinline__ LaneTri lane_triangle(const float4* pos, const uint8_t* idxBytes, uint32_t p, bool valid,
+                                                 const ViewParams& vp) {
+    LaneTri lt;
+    const float4 q0 = pos[preload64_index(idxBytes[p & 127])];
+    const float4 q1 = pos[preload64_index(idxBytes[128 + (p & 127)])];
+    const float4 q2 = pos[preload64_index(idxBytes[256 + (p & 127)])];
+    lt.v0 = { q0.x, q0.y, q0.z, q0.w }, lt.v1 = { q1.x, q1.y, q1.z, q1.w }, lt.v2 = { q2.x, q2.y, q2.z, q2.w };
+    uint32_t partial = 0, combined = 0x3F;
+    bool trivial = true;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const Vtx& q = i == 0 ? lt.v0 : (i == 1 ? lt.v1 : lt.v2);
+        uint32_t oc = 0;
+        oc |= (q.x < -q.w) ? 1u : 0u;
+        oc |= (q.x > q.w) ? 2u : 0u;
+        oc |= (q.y < -q.w) ? 4u : 0u;
+        oc |= (q.y > q.w) ? 8u : 0u;
+        oc |= (q.z < -q.w) ? 16u : 0u;
+        oc |= (q.z > q.w) ? 32u : 0u;
+        partial |= oc;
+        combined &= oc;
+        trivial = trivial && (fabsf(q.x) < fmul(q.w, vp.bx) && fabsf(q.y) < fmul(q.w, vp.by));
+    }
+    if (partial & 0x30u) trivial = false;
+    const bool accept = valid && combined == 0;
+    lt.partial = partial;
+    lt.acc = accept && trivial;
+    lt.nontriv = accept && !trivial;
+    return lt;
 }
 
 // ------------------------------------------------------------------ kernels
 // Per-warp shared memory: transformed vertices, index bytes, triangle records, the view, and the
-// owner lane of each tile in the concatenated tile list of the round's small triangles.
+// owner lane of each tile in the concatenated tile list of the round's small triangles. The alpha
+// pass also keeps each small triangle's alpha terms.
 struct WarpSmem {
     float4 pos[64];
     uint32_t idx[96];
@@ -347,21 +621,30 @@ struct WarpSmem {
     ViewParams view;
     uint8_t owner[32 * kSmallTiles];
 };
+struct WarpSmemAlpha : WarpSmem {
+    AlphaExt exts[32];
+};
 
 // Mesh stage. A work item is one meshlet of one view: a single-view draw numbers its meshlets
 // 0..count-1; a batched draw concatenates the meshlet ranges of its views (viewStart is their
 // prefix), so one launch serves views of any size.
+// Two passes: the opaque pass (kAlpha false) draws every meshlet with the opaque shader and
+// appends the work items of alpha-tested meshlets to alphaList; the alpha pass (kAlpha true)
+// draws those with FS_EncodeSurfaceId<true>. The order of the passes does not change the keys.
+template <bool kAlpha>
 __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
+    using Smem = typename std::conditional<kAlpha, WarpSmemAlpha, WarpSmem>::type;
     extern __shared__ __align__(16) unsigned char smemRaw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    WarpSmem& S = ((WarpSmem*)smemRaw)[warp];
+    Smem& S = ((Smem*)smemRaw)[warp];
     float4* pos = S.pos;
     const uint8_t* idxBytes = (const uint8_t*)S.idx;
     TriRec* tris = S.tris;
     const ViewParams& vp = S.view;
     const uint32_t chunk = a.chunkTiles ? a.chunkTiles : kChunkTiles;
     const bool multi = a.views != nullptr;
-    const uint32_t totalItems = multi ? a.viewStart[a.numViews] : a.count;
+    const uint32_t totalItems = kAlpha ? (uint32_t)a.s.control[9] : (multi ? a.viewStart[a.numViews] : a.count);
+    unsigned long long* const cursor = &a.s.control[kAlpha ? 10 : 0];
     uint32_t curView = 0xFFFFFFFFu;
     if (!multi) {
         if (lane == 0) {
@@ -376,7 +659,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
         __syncwarp();
     }
     unsigned long long nProcessed = 0, nRaster = 0, nClipped = 0;
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.s.control[8] = 0;  // the chunk stage's cursor (runs after this kernel)
+    if (!kAlpha && blockIdx.x == 0 && threadIdx.x == 0) a.s.control[8] = 0;  // the chunk stage's cursor (runs later)
 
     // Work items are fetched kFetch at a time: one contended atomic per kFetch items.
     constexpr uint32_t kFetch = 4;
@@ -384,13 +667,14 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     while (true) {
         if (fetchLeft == 0) {
             uint32_t b = 0;
-            if (lane == 0) b = (uint32_t)atomicAdd(&a.s.control[0], (unsigned long long)kFetch);
+            if (lane == 0) b = (uint32_t)atomicAdd(cursor, (unsigned long long)kFetch);
             fetchBase = __shfl_sync(0xFFFFFFFFu, b, 0);
             fetchLeft = kFetch;
         }
-        const uint32_t item = fetchBase++;
+        const uint32_t idx = fetchBase++;
         fetchLeft--;
-        if (item >= totalItems) break;
+        if (idx >= totalItems) break;
+        const uint32_t item = kAlpha ? a.s.alphaList[idx] : idx;
         uint32_t m = item, view = 0;
         if (multi) {
             uint32_t lo = 0, hi = a.numViews - 1;  // largest view with viewStart <= item
@@ -415,8 +699,16 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
         const uint32_t matId = *(const uint32_t*)(mp + kOffMaterialId);
         const uint32_t nv = hdr & 0xFF, nt = min((hdr >> 8) & 0xFF, 128u);  // record arrays hold 64 / 128
         int cullMode = kCullFrontCCW;
-        if (matId != 0xFFFFFFFFu && matId < a.numMaterials)
-            cullMode = a.materials[matId].is_double_sided ? kCullNone : kCullFrontCCW;  // Shading.cpp:302-306
+        bool alphaTested = false;  // FragmentShaderId 1
+        if (matId != 0xFFFFFFFFu && matId < a.numMaterials) {  // Shading.cpp:302-306
+            const DevMaterial& mt = a.materials[matId];
+            cullMode = mt.is_double_sided ? kCullNone : kCullFrontCCW;
+            alphaTested = material_alpha_tested(mt);
+        }
+        if (!kAlpha && alphaTested) {  // drawn by the alpha pass
+            if (lane == 0) a.s.alphaList[atomicAdd(&a.s.control[9], 1ull)] = item;
+            continue;
+        }
         if (nt == 0) continue;
         nProcessed += nt;
 
@@ -440,61 +732,52 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
 
         for (uint32_t base = 0; base < nt; base += 32) {
             const uint32_t p = base + lane;
-            const bool valid = p < nt;
-            const float4 q0 = pos[preload64_index(idxBytes[p & 127])];
-            const float4 q1 = pos[preload64_index(idxBytes[128 + (p & 127)])];
-            const float4 q2 = pos[preload64_index(idxBytes[256 + (p & 127)])];
-            Vtx v0 = { q0.x, q0.y, q0.z, q0.w }, v1 = { q1.x, q1.y, q1.z, q1.w }, v2 = { q2.x, q2.y, q2.z, q2.w };
-
-            // Clipper::ComputeClipCodes (Rasterizer.cpp:353-397), per lane.
-            uint32_t partial = 0, combined = 0x3F;
-            bool trivial = true;
-#pragma unroll
-            for (int i = 0; i < 3; i++) {
-                const Vtx& q = i == 0 ? v0 : (i == 1 ? v1 : v2);
-                uint32_t oc = 0;
-                oc |= (q.x < -q.w) ? 1u : 0u;
-                oc |= (q.x > q.w) ? 2u : 0u;
-                oc |= (q.y < -q.w) ? 4u : 0u;
-                oc |= (q.y > q.w) ? 8u : 0u;
-                oc |= (q.z < -q.w) ? 16u : 0u;
-                oc |= (q.z > q.w) ? 32u : 0u;
-                partial |= oc;
-                combined &= oc;
-                trivial = trivial && (fabsf(q.x) < fmul(q.w, vp.bx) && fabsf(q.y) < fmul(q.w, vp.by));
-            }
-            if (partial & 0x30u) trivial = false;
-            const bool accept = valid && combined == 0;
-            const bool acc = accept && trivial;
-            const bool nontriv = accept && !trivial;
-            if (a.countClipped) nClipped += __popc(__ballot_sync(0xFFFFFFFFu, nontriv)) * (lane == 0);
+            const LaneTri lt = lane_triangle(pos, idxBytes, p, p < nt, vp);
+            const Vtx &v0 = lt.v0, &v1 = lt.v1, &v2 = lt.v2;
+            if (a.countClipped) nClipped += __popc(__ballot_sync(0xFFFFFFFFu, lt.nontriv)) * (lane == 0);
 
             int myTiles = 0;     // tiles of this lane's small triangle (0 if none)
             bool overflow = false;
-            if (acc) {
+            if (lt.acc) {
                 Setup t;
                 uint32_t bbMin, bbMax;
                 if (tri_setup(v0, v1, v2, vp.halfW, vp.halfH, cullMode, t, bbMin, bbMax)) {
                     TriRec r;
-                    edge_setup(t, vp.halfW, vp.halfH, bbMin, bbMax, make_rank(g, p, 0, 0), r);
+                    float rcpArea;
+                    edge_setup(t, vp.halfW, vp.halfH, bbMin, bbMax, make_rank(g, p, 0, 0), r, &rcpArea);
                     nRaster++;
+                    AlphaExt x;
+                    if constexpr (kAlpha)
+                        x = alpha_ext(t, rcpArea, texcoord_word(mp, idxBytes[p]), texcoord_word(mp, idxBytes[128 + p]),
+                                      texcoord_word(mp, idxBytes[256 + p]), matId);
                     const int tilesX = ((bbMax & 0xFFFF) - (bbMin & 0xFFFF)) >> 2;
                     const int tilesY = ((bbMax >> 16) - (bbMin >> 16)) >> 2;
                     if (tilesX * tilesY <= kSmallTiles) {
                         // tile index -> row by a multiply-shift (exact for tile < 16, tilesX <= 16)
                         r.pad = (uint32_t)tilesX | ((uint32_t)((256 + tilesX - 1) / tilesX) << 8);
                         tris[lane] = r;
+                        if constexpr (kAlpha) S.exts[lane] = x;
                         myTiles = tilesX * tilesY;
                     } else {
-                        r.pad = view;
-                        if (!enqueue_big(r, a, chunk)) {
+                        bool queued;
+                        if constexpr (kAlpha) {
+                            r.pad = view | kTriAlpha;
+                            queued = enqueue_alpha(r, x, a, chunk);
+                            if (!queued) S.exts[lane] = x;
+                        } else {
+                            r.pad = view;
+                            queued = enqueue_big(r, a, chunk);
+                        }
+                        if (!queued) {
                             tris[lane] = r;
                             overflow = true;
                         }
                     }
                 }
             }
-            if (nontriv && a.clipMode) clip_and_queue(v0, v1, v2, partial, a, vp, view, chunk, cullMode, g, p, nRaster);
+            if (lt.nontriv && a.clipMode)
+                clip_and_queue(v0, v1, v2, lt.partial, a, vp, view, chunk, cullMode, g, p, nRaster, kAlpha ? matId : ~0u, mp,
+                               idxBytes);
             __syncwarp();
 
             // Small triangles: the warp walks the concatenated tile lists of all of them, two
@@ -526,8 +809,15 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                     tpx = (r.bbMin & 0xFFFF) + tx * 4, tpy = (r.bbMin >> 16) + ty * 4;
                     live = tile_live(r, tpx, tpy, vp.tileMin, tw, &tmin);
                 }
-                shade_live_tiles([&](uint32_t q) -> const TriRec& { return tris[q]; }, own, __ballot_sync(0xFFFFFFFFu, live),
-                                 tpx, tpy, tmin, vp.keys, vp.tileMin, vp.width, lane);
+                const unsigned liveMask = __ballot_sync(0xFFFFFFFFu, live);
+                if constexpr (kAlpha) {
+                    const DevMaterial& mt = a.materials[matId];
+                    shade_live_tiles_alpha(tris, S.exts, own, mt.tex, mt.alpha_cutoff << 24, liveMask, tpx, tpy, tmin,
+                                           vp.keys, vp.tileMin, vp.width, lane);
+                } else {
+                    shade_live_tiles([&](uint32_t q) -> const TriRec& { return tris[q]; }, own, liveMask, tpx, tpy, tmin,
+                                     vp.keys, vp.tileMin, vp.width, lane);
+                }
             }
             // Triangles the full queue turned away are rasterized here by the whole warp.
             unsigned ovMask = __ballot_sync(0xFFFFFFFFu, overflow);
@@ -536,8 +826,14 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                 ovMask &= ovMask - 1;
                 const TriRec r = tris[src];
                 const uint32_t x0 = r.bbMin & 0xFFFF, y0 = r.bbMin >> 16;
-                raster_region(r, x0, y0, (int)(((r.bbMax & 0xFFFF) - x0) >> 2), (int)(((r.bbMax >> 16) - y0) >> 2),
-                              vp.keys, vp.tileMin, vp.width, lane);
+                const int tx = (int)(((r.bbMax & 0xFFFF) - x0) >> 2), ty = (int)(((r.bbMax >> 16) - y0) >> 2);
+                if constexpr (kAlpha) {
+                    const DevMaterial& mt = a.materials[matId];
+                    raster_region_alpha(&tris[src], &S.exts[src], mt.tex, mt.alpha_cutoff << 24, x0, y0, tx, ty, vp.keys,
+                                        vp.tileMin, vp.width, lane);
+                } else {
+                    raster_region(r, x0, y0, tx, ty, vp.keys, vp.tileMin, vp.width, lane);
+                }
             }
             __syncwarp();
         }
@@ -555,13 +851,27 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
 // Chunk stage: warps take runs of kChunkRun consecutive chunks (chunk x chunk tiles) of the queued
 // triangles from a global cursor (control[8], zeroed by the mesh stage), locate the run's first
 // chunk by binary search over the queue's chunk prefix and walk the rest sequentially. A queued
-// triangle carries its view in pad (batched draws) or belongs to the single view.
+// triangle carries its view in pad (batched draws) or belongs to the single view; an alpha-tested
+// one (kTriAlpha) has its AlphaExt in the next slot, which owns no chunks and is never selected.
 constexpr uint32_t kChunkRun = 8;
-__global__ void __launch_bounds__(256) k_raster_big(const TriRec* __restrict__ big, const unsigned long long* __restrict__ bigBase,
+
+// A chunk of the alpha-tested triangle whose record (and AlphaExt after it) is at q, kept out of
+// line so that the opaque chunks keep the kernel's registers.
+__device__ __noinline__ void raster_chunk_alpha(const TriRec* q, const DevMaterial* materials, uint32_t x0, uint32_t y0,
+                                                int tilesX, int tilesY, unsigned long long* keys, uint32_t* tileMin,
+                                                uint32_t width, int lane) {
+    const AlphaExt* xp = (const AlphaExt*)&q[1];
+    const DevMaterial& mt = materials[xp->material & ~kTriAlpha];
+    raster_region_alpha(q, xp, mt.tex, mt.alpha_cutoff << 24, x0, y0, tilesX, tilesY, keys, tileMin, width, lane);
+}
+
+__global__ void __launch_bounds__(256, 5) k_raster_big(const TriRec* __restrict__ big, const unsigned long long* __restrict__ bigBase,
                                                     unsigned long long* control, uint32_t capacity,
                                                     unsigned long long* keys, uint32_t* tileMin, uint32_t width,
-                                                    const ViewParams* __restrict__ views, uint32_t chunk) {
+                                                    const ViewParams* __restrict__ views, uint32_t chunk,
+                                                    const DevMaterial* __restrict__ materials) {
     const unsigned long long q = control[1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) control[9] = control[10] = 0;  // the next draw's alpha list
     const uint32_t n = (uint32_t)min((unsigned long long)capacity, q >> 40);
     if (n == 0) return;
     const int lane = threadIdx.x & 31;
@@ -595,7 +905,10 @@ __global__ void __launch_bounds__(256) k_raster_big(const TriRec* __restrict__ b
             unsigned long long* vkeys = keys;
             uint32_t* vtiles = tileMin;
             uint32_t vwidth = width;
-            if (views) vkeys = views[r.pad].keys, vtiles = views[r.pad].tileMin, vwidth = views[r.pad].width;
+            if (views) {
+                const ViewParams& v = views[r.pad & ~kTriAlpha];
+                vkeys = v.keys, vtiles = v.tileMin, vwidth = v.width;
+            }
             const uint32_t c = (uint32_t)(w - base);
             const uint32_t minX = r.bbMin & 0xFFFF, minY = r.bbMin >> 16, maxX = r.bbMax & 0xFFFF, maxY = r.bbMax >> 16;
             const uint32_t chunksX = (((maxX - minX) >> 2) + chunk - 1) / chunk;
@@ -603,7 +916,12 @@ __global__ void __launch_bounds__(256) k_raster_big(const TriRec* __restrict__ b
             const uint32_t x0 = minX + cx * (chunk * 4), y0 = minY + cy * (chunk * 4);
             const uint32_t x1 = min(x0 + chunk * 4, maxX), y1 = min(y0 + chunk * 4, maxY);
             // Empty and hidden tiles of the chunk are rejected inside raster_region.
-            raster_region(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys, vtiles, vwidth, lane);
+            if (r.pad & kTriAlpha) {
+                raster_chunk_alpha(big + slot, materials, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys,
+                                   vtiles, vwidth, lane);
+            } else {
+                raster_region(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys, vtiles, vwidth, lane);
+            }
         }
     }
 }
@@ -676,22 +994,30 @@ static int grid_for(uint32_t n, int perThread, int block) {
 
 void launch_draw(const DrawArgs& a, cudaStream_t st, int numSMs) {
     const uint32_t warps = a.warpsPerBlock ? a.warpsPerBlock : kWarpsPerBlock;
-    const size_t smem = warps * sizeof(WarpSmem);
-    static size_t s_smemSet = 0;
+    const size_t smem = warps * sizeof(WarpSmem), smemAlpha = warps * sizeof(WarpSmemAlpha);
+    static size_t s_smemSet = 0, s_smemSetAlpha = 0;
     if (smem > s_smemSet && smem > 48 * 1024) {
-        cudaFuncSetAttribute(k_draw_meshlets, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_draw_meshlets<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         s_smemSet = smem;
+    }
+    if (a.s.alphaList && smemAlpha > s_smemSetAlpha && smemAlpha > 48 * 1024) {
+        cudaFuncSetAttribute(k_draw_meshlets<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemAlpha);
+        s_smemSetAlpha = smemAlpha;
     }
     const uint32_t chunk = a.chunkTiles ? a.chunkTiles : kChunkTiles;
     {
         // 64 registers a thread (launch bounds) leave room for 32 resident warps per SM
         LaunchScope ls("k_draw_meshlets", st);
-        k_draw_meshlets<<<numSMs * (32 / warps), warps * 32, smem, st>>>(a);
+        k_draw_meshlets<false><<<numSMs * (32 / warps), warps * 32, smem, st>>>(a);
+    }
+    if (a.s.alphaList) {  // the scene has alpha-tested materials
+        LaunchScope ls("k_draw_meshlets_alpha", st);
+        k_draw_meshlets<true><<<numSMs * (32 / warps), warps * 32, smemAlpha, st>>>(a);
     }
     {
         LaunchScope ls("k_raster_big", st);
         k_raster_big<<<numSMs * 8, 256, 0, st>>>(a.s.big, a.s.bigBase, a.s.control, a.s.bigCapacity, a.keys, a.tileMin,
-                                                 a.width, a.views, chunk);
+                                                 a.width, a.views, chunk, a.materials);
     }
 }
 

@@ -226,15 +226,17 @@ def _lattice_rgba(size: int, lat: np.ndarray) -> np.ndarray:
     return (top * (256 - ty) + bot * ty) >> 16
 
 
-def value_noise_rgba(size: int, seed: int, cells: int = 32, layer: int = 0, detail: bool = False) -> np.ndarray:
+def value_noise_rgba(size: int, seed: int, cells: int = 32, layer: int = 0, detail: bool = False,
+                     cutout: bool = False) -> np.ndarray:
     """Seeded RGBA8 value noise (bilinear over a cells x cells lattice, wrapping), uint32[size, size].
-    With detail, a second octave with 8-texel cells is blended in at 1/4 weight."""
+    With detail, a second octave with 8-texel cells is blended in at 1/4 weight. Layer 0 is opaque
+    (alpha 255) unless cutout, where its alpha is noise too (for alpha-tested materials)."""
     # layer 1 = tangent-space normal XY (centred near 128), metallic, roughness (Scene.h:8-10)
     v = _lattice_rgba(size, _noise_lattice(seed, cells, layer))
     if detail:
         v = (3 * v + _lattice_rgba(size, _noise_lattice(seed + 104729, size // 8, layer))) >> 2
     v = v.astype(np.uint32)
-    if layer == 0:
+    if layer == 0 and not cutout:
         v[..., 3] = 255
     return v[..., 0] | (v[..., 1] << 8) | (v[..., 2] << 16) | (v[..., 3] << 24)
 
@@ -254,7 +256,8 @@ def _noise_lattice(seed: int, cells: int, layer: int) -> np.ndarray:
 ROUGHNESS_MIN = 51  # 0.2
 
 
-def value_noise_rgba_torch(size: int, seed: int, cells: int = 32, layer: int = 0, device="cuda", detail: bool = False):
+def value_noise_rgba_torch(size: int, seed: int, cells: int = 32, layer: int = 0, device="cuda", detail: bool = False,
+                           cutout: bool = False):
     """value_noise_rgba computed on the device with torch (same integer arithmetic, same texels);
     returns an int32 tensor of shape (size, size) holding the packed RGBA8 words."""
     import torch
@@ -279,7 +282,7 @@ def value_noise_rgba_torch(size: int, seed: int, cells: int = 32, layer: int = 0
     v = lattice(_noise_lattice(seed, cells, layer))
     if detail:
         v = (3 * v + lattice(_noise_lattice(seed + 104729, size // 8, layer))) >> 2
-    if layer == 0:
+    if layer == 0 and not cutout:
         v[..., 3] = 255
     packed = v[..., 0] | (v[..., 1] << 8) | (v[..., 2] << 16) | (v[..., 3] << 24)
     return (packed - ((packed >> 31) << 32)).to(torch.int32)
@@ -323,8 +326,13 @@ class Scene:
     def num_meshlets(self) -> int:
         return len(self.meshlets)
 
+    def texture_cutout(self, i: int, layer: int) -> bool:
+        """Layer 0 of an alpha-tested material carries a noise alpha channel."""
+        return layer == 0 and int(self.materials["alpha_cutoff"][i]) < 255
+
     def texture_pixels(self, i: int, layer: int) -> np.ndarray:
-        return value_noise_rgba(self.texture_size, self.texture_seed + i, layer=layer, detail=self.texture_detail)
+        return value_noise_rgba(self.texture_size, self.texture_seed + i, layer=layer, detail=self.texture_detail,
+                                cutout=self.texture_cutout(i, layer))
 
 
 def grid_scene(n_side: int = 32, width: int = 1280, height: int = 720, seed: int = 1,
@@ -384,10 +392,12 @@ def multiview_scene(n: int = 200_000, n_cameras: int = 58, seed: int = 3, cube_s
 
 def volume_scene(n: int = 100_000, width: int = 1920, height: int = 1080, n_materials: int = 64,
                  seed: int = 2, texture_size: int = 2048, extent: float = 100.0,
-                 env_size: int = 1024) -> Scene:
+                 env_size: int = 1024, alpha_every: int = 0, alpha_cutoff: int = 128) -> Scene:
     """Large plain-path scene: n meshlets scattered in a (2*extent)^3 volume with log-uniform
     scale 0.1-10 and random yaw, n_materials materials of two RGBA8 layers, seen by a camera on
-    the volume's -z face looking in (plus a perturbed second camera for the Hi-Z frame)."""
+    the volume's -z face looking in (plus a perturbed second camera for the Hi-Z frame).
+    With alpha_every = k > 0, every k-th material is alpha-tested (cutoff alpha_cutoff, double-sided,
+    noise alpha in layer 0), like foliage cards."""
     rng = np.random.default_rng(seed)
     centers = rng.uniform(-extent, extent, size=(n, 3))
     scales = np.exp(rng.uniform(math.log(0.1), math.log(10.0), n))
@@ -397,6 +407,9 @@ def volume_scene(n: int = 100_000, width: int = 1920, height: int = 1080, n_mate
     mats = np.zeros(n_materials, dtype=MATERIAL_DTYPE)
     mats["texture"] = np.arange(n_materials)
     mats["alpha_cutoff"] = 255
+    if alpha_every > 0:
+        mats["alpha_cutoff"][::alpha_every] = alpha_cutoff
+        mats["is_double_sided"][::alpha_every] = 1
     eye = np.array([0.0, 0.0, -1.3 * extent])
     v0 = make_view(width, height, eye=eye, target=(0.0, 0.0, 0.0))
     v1 = make_view(width, height, eye=eye + np.array([0.4, 0.2, 0.6]), target=(1.0, 0.5, 0.0))

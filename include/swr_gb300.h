@@ -58,7 +58,10 @@ typedef struct swr_texture_t* swr_texture;
 #define SWR_COUNTER_BIN_QUEUE_FLUSHES 3
 #define SWR_NUM_COUNTERS 4
 
-/* Material (Scene.h:7-14); texture may be NULL. */
+/* Material (Scene.h:7-14); texture may be NULL. alpha_cutoff < 255 selects the alpha-tested
+ * vis-buffer shader (FS_EncodeSurfaceId<true>, Shading.cpp:302-331): a fragment is kept if the
+ * texture's layer-0 texel at its implicit LOD has alpha >= alpha_cutoff. A material without a
+ * texture (which the reference would dereference) keeps every fragment. */
 typedef struct {
     swr_texture texture;
     uint8_t is_double_sided;
@@ -122,8 +125,9 @@ swr_status swr_rasterizer_get_counters(swr_rasterizer r, uint64_t out[SWR_NUM_CO
 swr_status swr_rasterizer_reset_counters(swr_rasterizer r);
 
 /* Rasterizer::DrawMeshlets(Framebuffer&, count, ShaderBinding) (Rasterizer.h:213,
- * Rasterizer.cpp:493-644) with ShaderBinding{VisBufferShader, &ctx}. Depth test GREATER with
- * equal depths resolved to the first-submitted triangle of a single-threaded draw. */
+ * Rasterizer.cpp:493-644) with ShaderBinding{VisBufferShader, &ctx}: FragmentShaderId 0 (opaque)
+ * or 1 (alpha-tested) per meshlet material. Depth test GREATER with equal depths resolved to the
+ * first-submitted triangle of a single-threaded draw. */
 swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t count, uint32_t shader_table,
                              const swr_shading_context* ctx);
 

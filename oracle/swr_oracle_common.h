@@ -94,4 +94,18 @@ static inline V4 transform_point(const float* m, float x, float y, float z) {
     return r;
 }
 
+// One half of a packed half2 (vcvtph2ps, exact).
+static inline float half_to_float(uint32_t h) {
+    uint32_t s = (h >> 15) & 1, e = (h >> 10) & 31, m = h & 1023;
+    float v;
+    if (e == 0) v = std::ldexp((float)m, -24);
+    else if (e == 31) v = m ? NAN : INFINITY;
+    else v = std::ldexp((float)(m | 1024), (int)e - 25);
+    return s ? -v : v;
+}
+
+// Texture2D::SampleLevel<SurfaceSampler> on an RGBA8 texture for the 16 lanes of a 4x4 tile
+// (u, v, mip levels per lane; the filter is chosen over all 16), swr_oracle_resolve.cpp.
+void sample_rgba8(const orc_texture& t, const float* u, const float* v, int layer, const int32_t* mipIn, uint32_t* out);
+
 }  // namespace orc

@@ -213,12 +213,115 @@ static void draw_triangle(DrawCtx& dc, const EdgeVars& e, uint32_t bbMin, uint32
     }
 }
 
+// Inputs of FS_EncodeSurfaceId<true> (Shading.cpp:309-331) for one triangle: the material's
+// texture (layer 0) and cutoff, the texcoords of the triangle's three vertices and, for a clipped
+// triangle, its TriangleClipData rows (Rasterizer.cpp:455-458).
+struct AlphaTri {
+    const orc_texture* tex;
+    uint32_t cutoff;        // AlphaCutoff << 24
+    float uv[3][2];
+    bool clipped;
+    float ru[3], rv[3];
+};
+
+// Mesh::TexCoords[VertexId] (Shading.cpp:320-322). The index byte is not bounded by the
+// reference: an index past the 64 texcoords reads the words that follow them in the record
+// (NormalTangents, Indices). That is restated for indices below 224; indices from 224 on would
+// read the next record and read 0 here.
+static uint32_t texcoord_word(const Meshlet& mesh, uint32_t idx) {
+    if (idx >= 224) return 0;
+    uint32_t w;
+    memcpy(&w, (const uint8_t*)&mesh + offsetof(Meshlet, TexCoords) + 4 * idx, 4);
+    return w;
+}
+
+// DrawTriangle<FS_EncodeSurfaceId<true>, IsClipped> (Rasterizer.h:250-328, Shading.cpp:309-331)
+// tile by tile, as the reference's 16 lanes: every lane of a visited tile computes its
+// perspective-correct barycentrics, texcoord and scaled sample position, whether or not it is
+// covered; the implicit LOD takes 2x2 finite differences across the tile (texutil::dFdx/dFdy,
+// Texture.h:258-275) and the filter is chosen over all 16 lanes (Texture.h:432).
+static void draw_triangle_alpha(DrawCtx& dc, const EdgeVars& e, uint32_t bbMin, uint32_t bbMax, uint32_t meshletId,
+                                uint32_t primId, const AlphaTri& at) {
+    orc_framebuffer* fb = dc.fb;
+    uint32_t minX = bbMin & 0xFFFF, minY = bbMin >> 16;
+    uint32_t maxX = bbMax & 0xFFFF, maxY = bbMax >> 16;
+    float* depthBuf = (float*)&fb->data[1 * fb->layer_stride];
+    uint32_t* colorBuf = &fb->data[0];
+    uint32_t surfaceId = (dc.sc->meshlet_offset + meshletId) * 128u + primId;
+    const orc_texture& tex = *at.tex;
+
+    for (uint32_t ty = std::max(minY, dc.rowBegin & ~3u); ty < maxY && ty < dc.rowEnd; ty += 4) {
+        for (uint32_t tx = minX; tx < maxX; tx += 4) {
+            float u[16], v[16], depth[16];
+            uint32_t mask = 0;
+            for (uint32_t l = 0; l < 16; l++) {
+                uint32_t x = tx + (l & 3), y = ty + (l >> 2);
+                int32_t e0 = (int32_t)((uint32_t)e.Edge0 + (uint32_t)e.A12 * x + (uint32_t)e.B12 * y);
+                int32_t e1 = (int32_t)((uint32_t)e.Edge1 + (uint32_t)e.A20 * x + (uint32_t)e.B20 * y);
+                int32_t e2 = (int32_t)((uint32_t)e.Edge2 + (uint32_t)e.A01 * x + (uint32_t)e.B01 * y);
+                if ((e0 | e1 | e2) >= 0) mask |= 1u << l;
+                u[l] = (float)e1, v[l] = (float)e2;
+                depth[l] = std::fma(u[l], e.Z10, std::fma(v[l], e.Z20, e.Z0));
+            }
+            if (mask == 0) continue;  // DrawTriangle visits only tiles with a covered sample
+            // depth test (Shading.cpp:312-313); rows this call does not own are never written
+            for (uint32_t l = 0; l < 16; l++) {
+                uint32_t y = ty + (l >> 2);
+                if (!((mask >> l) & 1)) continue;
+                if (y < dc.rowBegin || y >= dc.rowEnd || !(depth[l] > depthBuf[pixel_offset(fb, tx + (l & 3), y)]))
+                    mask &= ~(1u << l);
+            }
+            if (mask == 0) continue;
+
+            float uvx[16], uvy[16], su[16], sv[16];
+            for (uint32_t l = 0; l < 16; l++) {
+                // perspective correction (Rasterizer.h:300-317)
+                float pw0 = std::fma(u[l] + v[l], -e.W0S, e.W0);
+                float w = std::fma(u[l], e.W1S, std::fma(v[l], e.W2S, pw0));
+                float rcpW = approx_rcp(w);
+                rcpW *= std::fma(-w, rcpW, 2.0f);
+                float bu = u[l] * (e.W1S * rcpW);
+                float bv = v[l] * (e.W2S * rcpW);
+                if (at.clipped) {
+                    float cu = std::fma(bu, at.ru[1], std::fma(bv, at.ru[2], at.ru[0]));
+                    float cv = std::fma(bu, at.rv[1], std::fma(bv, at.rv[2], at.rv[0]));
+                    bu = cu, bv = cv;
+                }
+                float b0 = 1 - bu - bv;
+                // FragmentVars::Interpolate = BaryLerp (Rasterizer.h:101-104)
+                uvx[l] = std::fma(at.uv[0][0], b0, std::fma(at.uv[1][0], bu, at.uv[2][0] * bv));
+                uvy[l] = std::fma(at.uv[0][1], b0, std::fma(at.uv[1][1], bu, at.uv[2][1] * bv));
+                su[l] = uvx[l] * tex.scale_lerp_u;
+                sv[l] = uvy[l] * tex.scale_lerp_v;
+            }
+            // SampleImplicitLod (Texture.h:403-410): CalcMipLevel(grad) - LerpFracBits
+            int32_t mip[16];
+            for (uint32_t l = 0; l < 16; l++) {
+                float gx = su[l | 1] - su[l & ~1u], gy = sv[l | 1] - sv[l & ~1u];
+                float gz = su[l | 4] - su[l & ~4u], gw = sv[l | 4] - sv[l & ~4u];
+                float dx = std::fma(gx, gx, gy * gy);
+                float dy = std::fma(gz, gz, gw * gw);
+                mip[l] = (ilog2_x86(vmax(dx, dy)) >> 1) - 8;
+            }
+            uint32_t color[16];
+            sample_rgba8(tex, uvx, uvy, 0, mip, color);
+            for (uint32_t l = 0; l < 16; l++) {
+                if (!((mask >> l) & 1) || color[l] < at.cutoff) continue;  // Shading.cpp:326
+                uint32_t off = pixel_offset(fb, tx + (l & 3), ty + (l >> 2));
+                depthBuf[off] = depth[l];
+                colorBuf[off] = surfaceId;
+            }
+        }
+    }
+}
+
 // ShadeMeshlet, Shading.cpp:281-307. ShadedMeshlet (Rasterizer.h:82-99) with vertices past the
 // transformed 16-vertex chunks zero-initialised (uninitialised stack memory in the reference).
 struct Shaded {
     uint32_t PrimCount;
     int CullMode;
     uint32_t FragmentShaderId;
+    uint32_t MaterialId;
     uint8_t Indices[3][128];
     Vtx Pos[64];
 };
@@ -227,6 +330,7 @@ static void shade_meshlet(const orc_shading_context* sc, uint32_t index, Shaded&
     out.PrimCount = 0;
     out.CullMode = CULL_FRONT_CCW;
     out.FragmentShaderId = 0;
+    out.MaterialId = UINT32_MAX;
     if (sc->cull_bitmap != nullptr) {
         uint16_t mask = sc->cull_bitmap[index / 16];
         if (((mask >> (index % 16)) & 1) == 0) return;
@@ -242,6 +346,7 @@ static void shade_meshlet(const orc_shading_context* sc, uint32_t index, Shaded&
     }
     out.PrimCount = mesh.NumTriangles;
     memcpy(out.Indices, mesh.Indices, sizeof(mesh.Indices));
+    out.MaterialId = mesh.MaterialId;
     if (mesh.MaterialId != UINT32_MAX) {
         const orc_material& mat = sc->materials[mesh.MaterialId];
         out.CullMode = mat.is_double_sided ? CULL_NONE : CULL_FRONT_CCW;
@@ -251,7 +356,7 @@ static void shade_meshlet(const orc_shading_context* sc, uint32_t index, Shaded&
 
 // Clipper::ClipTriangles + FlushPacket, Rasterizer.cpp:398-491, for one packet. Emits the
 // clipped triangles in output order (prim id, then fan index); a callback draws each one.
-struct ClipOut { TriSetup t; bool keep; uint32_t primId; };
+struct ClipOut { TriSetup t; bool keep; uint32_t primId; float ru[3], rv[3]; };
 
 static void clip_packet(const Vtx v[3][16], const ClipCodes& cc, uint16_t nonTrivialMask, float bx, float by,
                         int halfW, int halfH, int cullMode, std::vector<ClipOut>& outs) {
@@ -308,6 +413,9 @@ static void clip_packet(const Vtx v[3][16], const ClipCodes& cc, uint16_t nonTri
             ClipOut co;
             co.keep = tri_setup(a, b, c, halfW, halfH, cullMode, co.t);
             co.primId = primId;
+            float u0 = V[4][i0], v0 = V[5][i0];  // TriangleClipData, Rasterizer.cpp:455-458
+            co.ru[0] = u0, co.ru[1] = V[4][i1] - u0, co.ru[2] = V[4][i2] - u0;
+            co.rv[0] = v0, co.rv[1] = V[5][i1] - v0, co.rv[2] = V[5][i2] - v0;
             outs.push_back(co);
             if (++outIdx >= 8 * 16) return;  // output truncation, Rasterizer.cpp:470-472
         }
@@ -333,12 +441,28 @@ static void draw_meshlets(DrawCtx& dc, uint32_t count, const orc_raster_flags* f
         shade_meshlet(sc, meshIdx, mesh);
         if (mesh.PrimCount == 0) continue;
         if (dc.counters) dc.counters[ORC_TRIS_PROCESSED] += mesh.PrimCount;
+        // FS_EncodeSurfaceId<true> for alpha-tested materials. The reference dereferences the
+        // material's texture unconditionally; a material without one passes every fragment here.
+        const orc_texture* alphaTex = nullptr;
+        uint32_t cutoff = 0;
         if (mesh.FragmentShaderId != 0) {
-            // FS_EncodeSurfaceId<true> samples the material with barycentrics from rcp14;
-            // this oracle restates only the opaque entry point.
-            fprintf(stderr, "orc_draw_meshlets: alpha-tested materials are not supported by the oracle\n");
-            abort();
+            const orc_material& mat = sc->materials[mesh.MaterialId];
+            if (mat.texture != UINT32_MAX && sc->textures && sc->textures[mat.texture].data) alphaTex = &sc->textures[mat.texture];
+            cutoff = (uint32_t)mat.alpha_cutoff << 24;
         }
+        const Meshlet& rec = ((const Meshlet*)sc->meshlets)[sc->meshlet_offset + meshIdx];
+        auto alpha_tri = [&](uint32_t prim, const ClipOut* co) {
+            AlphaTri at = {};
+            at.tex = alphaTex;
+            at.cutoff = cutoff;
+            for (int k = 0; k < 3; k++) {
+                uint32_t w = texcoord_word(rec, mesh.Indices[k][prim]);  // UnpackHalf2x16, Shading.cpp:228-231
+                at.uv[k][0] = half_to_float(w & 0xFFFF), at.uv[k][1] = half_to_float(w >> 16);
+            }
+            at.clipped = co != nullptr;
+            if (co) memcpy(at.ru, co->ru, sizeof(at.ru)), memcpy(at.rv, co->rv, sizeof(at.rv));
+            return at;
+        };
 
         for (uint32_t primOffset = 0; primOffset < mesh.PrimCount; primOffset += 16) {
             Vtx v[3][16];
@@ -363,7 +487,8 @@ static void draw_meshlets(DrawCtx& dc, uint32_t count, const orc_raster_flags* f
                     render_bbox(t, halfW, halfH, bbMin, bbMax);
                     EdgeVars e;
                     edge_setup(t, halfW, halfH, e);
-                    draw_triangle(dc, e, bbMin, bbMax, meshIdx, primOffset + l);
+                    if (alphaTex) draw_triangle_alpha(dc, e, bbMin, bbMax, meshIdx, primOffset + l, alpha_tri(primOffset + l, nullptr));
+                    else draw_triangle(dc, e, bbMin, bbMax, meshIdx, primOffset + l);
                     if (dc.counters) dc.counters[ORC_TRIS_RASTERIZED]++;
                 }
             }
@@ -376,7 +501,9 @@ static void draw_meshlets(DrawCtx& dc, uint32_t count, const orc_raster_flags* f
                     render_bbox(co.t, halfW, halfH, bbMin, bbMax);
                     EdgeVars e;
                     edge_setup(co.t, halfW, halfH, e);
-                    draw_triangle(dc, e, bbMin, bbMax, meshIdx, primOffset + co.primId);
+                    uint32_t prim = primOffset + co.primId;
+                    if (alphaTex) draw_triangle_alpha(dc, e, bbMin, bbMax, meshIdx, prim, alpha_tri(prim, &co));
+                    else draw_triangle(dc, e, bbMin, bbMax, meshIdx, prim);
                     if (dc.counters) dc.counters[ORC_TRIS_RASTERIZED]++;
                 }
             }

@@ -66,14 +66,6 @@ inline uint32_t pack_rgba8(F4 v) {
     return sat_u8(round2i(v.x * 255.0f)) | (sat_u8(round2i(v.y * 255.0f)) << 8) | (sat_u8(round2i(v.z * 255.0f)) << 16) |
            (sat_u8(round2i(v.w * 255.0f)) << 24);
 }
-inline float half_to_float(uint32_t h) {  // exact (vcvtph2ps)
-    uint32_t s = (h >> 15) & 1, e = (h >> 10) & 31, m = h & 1023;
-    float v;
-    if (e == 0) v = std::ldexp((float)m, -24);
-    else if (e == 31) v = m ? NAN : INFINITY;
-    else v = std::ldexp((float)(m | 1024), (int)e - 25);
-    return s ? -v : v;
-}
 inline float unpack_f11(uint32_t x) { x <<= 17; return u2f((x & 0x0FFE0000u) + 0x38000000u); }
 inline float unpack_f10(uint32_t x) { x <<= 18; return u2f((x & 0x0FFC0000u) + 0x38000000u); }
 inline F3 unpack_r11g11b10(uint32_t p) { return { unpack_f11(p >> 21), unpack_f11(p >> 10), unpack_f10(p) }; }
@@ -97,6 +89,8 @@ inline F3 unmap_oct(float u, float v) {
     n.y -= mulsign(t, n.y);
     return normalize3(n);
 }
+
+}  // namespace
 
 // ---------------------------------------------------------------------------- sampler
 // Texture2D::SampleLevel<SurfaceSampler> (Texture.h:412-459, Shading.cpp:6-10) for RGBA8 textures,
@@ -132,6 +126,8 @@ void sample_rgba8(const orc_texture& t, const float* u, const float* v, int laye
         out[l] = lerp16(rb1, rb2, fy) | (lerp16(ga1, ga2, fy) << 8);
     }
 }
+
+namespace {
 
 // Texture2D::SampleOctLevel<EnvSampler> (Texture.h:467-480, Shading.cpp:11-15) on an R11G11B10 map:
 // ClampToEdge, bilinear in float, blend of two mips when the level has a fraction.

@@ -33,13 +33,16 @@ CLIP_FROM_OBJECT = np.array([1, 0, 0, 0,
 
 
 def render_oracle(meshlets, materials, object_to_clip, width, height, count=None, binning=False, clipping=True,
-                  guardband=True, meshlet_offset=0, cull_bitmap=None, clear=(0xFF000000, 0.0), fb=None, threads=1):
-    """Oracle frame; with threads > 1 the rows are split over threads and the counters are not kept."""
+                  guardband=True, meshlet_offset=0, cull_bitmap=None, clear=(0xFF000000, 0.0), fb=None, threads=1,
+                  textures=None):
+    """Oracle frame; with threads > 1 the rows are split over threads and the counters are not kept.
+    textures (oracle textures by material texture index) feed the alpha test of alpha-tested materials."""
     from oracle import oracle as O
     if fb is None:
         fb = O.Framebuffer(width, height)
         fb.clear(*clear)
-    ctx = O.Context(meshlets, materials, object_to_clip, meshlet_offset=meshlet_offset, cull_bitmap=cull_bitmap)
+    ctx = O.Context(meshlets, materials, object_to_clip, meshlet_offset=meshlet_offset, cull_bitmap=cull_bitmap,
+                    textures=textures)
     n = len(meshlets) - meshlet_offset if count is None else count
     counters = O.draw_meshlets(fb, ctx, n, binning=binning, clipping=clipping, guardband=guardband, threads=threads)
     return fb, counters
