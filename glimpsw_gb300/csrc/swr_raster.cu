@@ -34,6 +34,8 @@ namespace swr {
 
 constexpr int kWarpsPerBlock = 8;
 constexpr int kSmallTiles = 16;
+constexpr int kPacketTiles = 128;  // in-warp tile budget of a 32-triangle step
+constexpr int kSpreadTiles = 4;    // over budget, triangles above this many tiles are queued
 constexpr int kChunkTiles = 8;  // chunk = 8x8 tiles = 32x32 pixels
 
 struct Vtx { float x, y, z, w; };
@@ -138,27 +140,7 @@ __device__ __forceinline__ void shade_fragment(const TriRec& r, uint32_t px, uin
     if (key > *(volatile unsigned long long*)p) atomicMax(p, key);
 }
 
-// The same for pixel (tx + l % 4, ty + l / 4) of the 4x4 tile at the 4-aligned (tx, ty), l = lane % 16:
-// the tiled key offset is then the tile's base plus l. Every lane reads its pixel's key (one
-// 128-byte line per tile); the return value is a lower bound of the pixel's depth word afterwards.
-__device__ __forceinline__ uint32_t shade_tile_pixel(const TriRec& r, uint32_t tx, uint32_t ty, uint32_t l,
-                                                     unsigned long long* keys, uint32_t width) {
-    unsigned long long* p = keys + (tx << 2) + ty * width + l;
-    const unsigned long long cur = *(volatile unsigned long long*)p;
-    const uint32_t px = tx + (l & 3), py = ty + (l >> 2);
-    const int32_t e0 = (int32_t)((uint32_t)r.E0 + (uint32_t)r.A12 * px + (uint32_t)r.B12 * py);
-    const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
-    const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
-    if ((e0 | e1 | e2) < 0) return (uint32_t)(cur >> 32);
-    const float depth = ffma(__int2float_rn(e1), r.Z10, ffma(__int2float_rn(e2), r.Z20, r.Z0));
-    if (depth != depth) return (uint32_t)(cur >> 32);
-    const unsigned long long key = ((unsigned long long)float_order(depth) << 32) | r.lowword;
-    if (key <= cur) return (uint32_t)(cur >> 32);
-    atomicMax(p, key);
-    return (uint32_t)(key >> 32);
-}
-
-// Upper bound of the depth shade_tile_pixel computes for any sample of the 4x4 tile at (px, py).
+// Upper bound of the depth tile_pixel_key computes for any sample of the 4x4 tile at (px, py).
 // The exact depth Z0 + Z10 e1 + Z20 e2 is affine in the pixel (the edge values are exact
 // integers), so its maximum over the tile is at a corner. A computed depth differs from the exact
 // one by at most 4u (|Z0| + |Z10 e1| + |Z20 e2|), u = 2^-24 (two conversions, two fma roundings),
@@ -183,11 +165,13 @@ __device__ __forceinline__ float tile_depth_bound(const TriRec& r, uint32_t px, 
 }
 
 // Raises the tile's depth bound to the minimum of the values its 16 pixels reported (the two
-// halves of the warp shade one tile each; offsets below 16 keep the reduction inside a half).
+// halves of the warp shade one tile each: two whole-warp reductions, each over one half's values).
 __device__ __forceinline__ void update_tile_min(uint32_t obs, uint32_t* tileMin, uint32_t tileIdx, uint32_t known,
                                                 bool active, int lane) {
-#pragma unroll
-    for (int o = 8; o > 0; o >>= 1) obs = min(obs, __shfl_xor_sync(0xFFFFFFFFu, obs, o));
+    const bool upper = lane & 16;
+    const uint32_t lo = __reduce_min_sync(0xFFFFFFFFu, upper ? 0xFFFFFFFFu : obs);
+    const uint32_t hi = __reduce_min_sync(0xFFFFFFFFu, upper ? obs : 0xFFFFFFFFu);
+    obs = upper ? hi : lo;
     if (active && (lane & 15) == 0 && obs > known) atomicMax(&tileMin[tileIdx], obs);
 }
 
@@ -275,7 +259,8 @@ __device__ __forceinline__ int32_t alpha_mip(float gx, float gy, float gz, float
     return (ilog2_x86(vmax(dx, dy)) >> 1) - 8;
 }
 
-// shade_tile_pixel with the alpha test, called by all 32 lanes: each half-warp shades one tile of
+// The opaque tile shading of shade_live_tiles with the alpha test, for pixel (tx + l % 4,
+// ty + l / 4), l = lane % 16, called by all 32 lanes: each half-warp shades one tile of
 // the same triangle (valid is false on a half without a tile). The x and y differences pair
 // lanes l ^ 1 and l ^ 4 of a half.
 __device__ __forceinline__ uint32_t shade_tile_pixel_alpha(const TriRec& r, const AlphaExt& x, const DevTexture& tex,
@@ -406,24 +391,58 @@ __device__ __forceinline__ bool tile_live(const TriRec& r, uint32_t px, uint32_t
 // Shades the live tiles of the warp-wide candidate set (the lanes in `mask` hold a tile origin
 // tpx/tpy, its depth bound tmin and a triangle selector rsel for rec()), two tiles per step, and
 // raises the tiles' depth bounds.
+// The key DrawTriangle + FS_EncodeSurfaceId<false> (Rasterizer.h:287-323, Shading.cpp:309-331)
+// offers for pixel (tx + l % 4, ty + l / 4) of the 4x4 tile at the 4-aligned (tx, ty), 0 if the
+// sample is outside the triangle or its depth is NaN. The tiled key offset is the tile's base
+// plus l, so a tile's 16 keys are one 128-byte line.
+__device__ __forceinline__ unsigned long long tile_pixel_key(const TriRec& r, uint32_t tx, uint32_t ty, uint32_t l) {
+    const uint32_t px = tx + (l & 3), py = ty + (l >> 2);
+    const int32_t e0 = (int32_t)((uint32_t)r.E0 + (uint32_t)r.A12 * px + (uint32_t)r.B12 * py);
+    const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
+    const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
+    if ((e0 | e1 | e2) < 0) return 0ull;
+    const float depth = ffma(__int2float_rn(e1), r.Z10, ffma(__int2float_rn(e2), r.Z20, r.Z0));
+    if (depth != depth) return 0ull;  // NaN never passes `Depth > old`
+    return ((unsigned long long)float_order(depth) << 32) | r.lowword;
+}
+
+// Shades the live tiles of the warp-wide candidate set (the lanes in `mask` hold a tile origin
+// tpx/tpy, its depth bound tmin and a triangle selector rsel for rec()) and raises the tiles' depth
+// bounds (each pixel reports a lower bound of its depth word afterwards). Four tiles per step: each
+// half-warp takes two, and a lane's two key loads are issued together (the walk is bound by their
+// latency).
 template <class Rec>
 __device__ __forceinline__ void shade_live_tiles(Rec&& rec, uint32_t rsel, unsigned mask, uint32_t tpx, uint32_t tpy,
                                                  uint32_t tmin, unsigned long long* keys, uint32_t* tileMin, uint32_t width,
                                                  int lane) {
-    const uint32_t half = lane >> 4, tw = width >> 2;
+    const uint32_t half = lane >> 4, tw = width >> 2, l = lane & 15;
+    const uint32_t txy = tpx | (tpy << 16);  // tile origins are below 2896
     while (mask) {
-        const int s0 = __ffs(mask) - 1;
-        mask &= mask - 1;
-        const int s1 = mask ? __ffs(mask) - 1 : -1;
-        if (s1 >= 0) mask &= mask - 1;
-        const int src = half ? s1 : s0;
-        const uint32_t qx = __shfl_sync(0xFFFFFFFFu, tpx, src & 31);
-        const uint32_t qy = __shfl_sync(0xFFFFFFFFu, tpy, src & 31);
-        const uint32_t qm = __shfl_sync(0xFFFFFFFFu, tmin, src & 31);
-        const uint32_t qr = __shfl_sync(0xFFFFFFFFu, rsel, src & 31);
-        uint32_t obs = 0;
-        if (src >= 0) obs = shade_tile_pixel(rec(qr), qx, qy, lane & 15, keys, width);
-        if (tileMin) update_tile_min(obs, tileMin, (qy >> 2) * tw + (qx >> 2), qm, src >= 0, lane);
+        int s[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            s[k] = mask ? __ffs(mask) - 1 : -1;
+            if (s[k] >= 0) mask &= mask - 1;
+        }
+        const int srcA = half ? s[1] : s[0], srcB = half ? s[3] : s[2];
+        const uint32_t pa_ = __shfl_sync(0xFFFFFFFFu, txy, srcA & 31), pb_ = __shfl_sync(0xFFFFFFFFu, txy, srcB & 31);
+        const uint32_t ax = pa_ & 0xFFFF, ay = pa_ >> 16, bx = pb_ & 0xFFFF, by = pb_ >> 16;
+        const uint32_t am = __shfl_sync(0xFFFFFFFFu, tmin, srcA & 31), ar = __shfl_sync(0xFFFFFFFFu, rsel, srcA & 31);
+        const uint32_t bm = __shfl_sync(0xFFFFFFFFu, tmin, srcB & 31), br = __shfl_sync(0xFFFFFFFFu, rsel, srcB & 31);
+        unsigned long long* pa = keys + (ax << 2) + ay * width + l;
+        unsigned long long* pb = keys + (bx << 2) + by * width + l;
+        const unsigned long long curA = srcA >= 0 ? *(volatile unsigned long long*)pa : 0ull;
+        const unsigned long long curB = srcB >= 0 ? *(volatile unsigned long long*)pb : 0ull;
+        const unsigned long long keyA = srcA >= 0 ? tile_pixel_key(rec(ar), ax, ay, l) : 0ull;
+        const unsigned long long keyB = srcB >= 0 ? tile_pixel_key(rec(br), bx, by, l) : 0ull;
+        if (keyA > curA) atomicMax(pa, keyA);
+        if (keyB > curB) atomicMax(pb, keyB);
+        if (tileMin) {
+            update_tile_min((uint32_t)((keyA > curA ? keyA : curA) >> 32), tileMin, (ay >> 2) * tw + (ax >> 2), am, srcA >= 0,
+                            lane);
+            update_tile_min((uint32_t)((keyB > curB ? keyB : curB) >> 32), tileMin, (by >> 2) * tw + (bx >> 2), bm, srcB >= 0,
+                            lane);
+        }
     }
 }
 
@@ -490,6 +509,87 @@ __device__ __forceinline__ void raster_region_alpha(const TriRec* rp, const Alph
                        [&](unsigned mask, uint32_t tpx, uint32_t tpy, uint32_t tmin) {
                            shade_live_tiles_alpha(rp, xp, 0, tex, cutoff, mask, tpx, tpy, tmin, keys, tileMin, width, lane);
                        });
+}
+
+// ------------------------------------------------------------------ overdraw shader
+// FS_Overdraw (Shading.cpp:333-342) for pixel l of the 4x4 tile at (tx, ty), called by all 32
+// lanes (a half-warp per tile; valid is false on a half without one). DrawTriangle visits the tile
+// only if a sample is covered; then every sample counts, covered ones in the high word of the
+// pixel's counter and the others in the low word, and the tile's 16 depths feed a maximum kept in
+// the key's high word (NaN never replaces: vmaxps keeps the old value).
+__device__ __forceinline__ void shade_tile_pixel_overdraw(const TriRec& r, uint32_t tx, uint32_t ty, bool valid, int lane,
+                                                          unsigned long long* keys, unsigned long long* counts,
+                                                          uint32_t width) {
+    const uint32_t l = lane & 15;
+    const uint32_t px = tx + (l & 3), py = ty + (l >> 2);
+    const int32_t e0 = (int32_t)((uint32_t)r.E0 + (uint32_t)r.A12 * px + (uint32_t)r.B12 * py);
+    const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
+    const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
+    const bool covered = valid && (e0 | e1 | e2) >= 0;
+    if (!((__ballot_sync(0xFFFFFFFFu, covered) >> (lane & 16)) & 0xFFFFu) || !valid) return;
+    const uint32_t off = (tx << 2) + ty * width + l;
+    atomicAdd(&counts[off], covered ? (1ull << 32) : 1ull);
+    const float depth = ffma(__int2float_rn(e1), r.Z10, ffma(__int2float_rn(e2), r.Z20, r.Z0));
+    if (depth != depth) return;
+    const unsigned long long key = (unsigned long long)float_order(depth) << 32;
+    if (key > *(volatile unsigned long long*)&keys[off]) atomicMax(&keys[off], key);
+}
+
+// shade_live_tiles for the overdraw shader (no depth bounds: every tile a triangle covers counts).
+template <class Rec>
+__device__ __forceinline__ void shade_live_tiles_overdraw(Rec&& rec, uint32_t rsel, unsigned mask, uint32_t tpx, uint32_t tpy,
+                                                          unsigned long long* keys, unsigned long long* counts,
+                                                          uint32_t width, int lane) {
+    const uint32_t half = lane >> 4;
+    while (mask) {
+        const int s0 = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int s1 = mask ? __ffs(mask) - 1 : -1;
+        if (s1 >= 0) mask &= mask - 1;
+        const int src = half ? s1 : s0;
+        const uint32_t qx = __shfl_sync(0xFFFFFFFFu, tpx, src & 31);
+        const uint32_t qy = __shfl_sync(0xFFFFFFFFu, tpy, src & 31);
+        const uint32_t qr = __shfl_sync(0xFFFFFFFFu, rsel, src & 31);
+        shade_tile_pixel_overdraw(rec(qr), qx, qy, src >= 0, lane, keys, counts, width);
+    }
+}
+
+__device__ __forceinline__ void raster_region_overdraw(const TriRec& r, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
+                                                       unsigned long long* keys, unsigned long long* counts,
+                                                       uint32_t width, int lane) {
+    raster_region_with(r, x0, y0, tilesX, tilesY, nullptr, width, lane,
+                       [&](unsigned mask, uint32_t tpx, uint32_t tpy, uint32_t) {
+                           shade_live_tiles_overdraw([&](uint32_t) -> const TriRec& { return r; }, 0, mask, tpx, tpy, keys,
+                                                     counts, width, lane);
+                       });
+}
+
+// One lane draws a whole triangle with the overdraw shader (the full-queue fallback of a clipped
+// triangle).
+__device__ __noinline__ void raster_serial_overdraw(const TriRec& r, unsigned long long* keys, unsigned long long* counts,
+                                                    uint32_t width) {
+    const uint32_t minX = r.bbMin & 0xFFFF, minY = r.bbMin >> 16, maxX = r.bbMax & 0xFFFF, maxY = r.bbMax >> 16;
+    for (uint32_t ty = minY; ty < maxY; ty += 4) {
+        for (uint32_t tx = minX; tx < maxX; tx += 4) {
+            unsigned cov = 0;
+            for (uint32_t l = 0; l < 16; l++) {
+                const uint32_t px = tx + (l & 3), py = ty + (l >> 2);
+                const int32_t e0 = (int32_t)((uint32_t)r.E0 + (uint32_t)r.A12 * px + (uint32_t)r.B12 * py);
+                const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
+                const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
+                if ((e0 | e1 | e2) >= 0) cov |= 1u << l;
+            }
+            if (!cov) continue;
+            for (uint32_t l = 0; l < 16; l++) {
+                const uint32_t px = tx + (l & 3), py = ty + (l >> 2), off = (tx << 2) + ty * width + l;
+                atomicAdd(&counts[off], ((cov >> l) & 1) ? (1ull << 32) : 1ull);
+                const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
+                const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
+                const float depth = ffma(__int2float_rn(e1), r.Z10, ffma(__int2float_rn(e2), r.Z20, r.Z0));
+                if (depth == depth) atomicMax(&keys[off], (unsigned long long)float_order(depth) << 32);
+            }
+        }
+    }
 }
 
 // Clipper::ClipTriangles + FlushPacket (Rasterizer.cpp:398-491) for this lane's triangle; the
@@ -567,7 +667,9 @@ __device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t out
             if (!enqueue_alpha(r, x, a, chunk)) raster_serial_alpha(r, x, a.materials, vp.keys, vp.width);
             continue;
         }
-        if (!enqueue_big(r, a, chunk)) raster_serial(r, vp.keys, vp.width);
+        if (enqueue_big(r, a, chunk)) continue;
+        if (a.counts) raster_serial_overdraw(r, vp.keys, a.counts, vp.width);
+        else raster_serial(r, vp.keys, vp.width);
     }
 }
 
@@ -628,11 +730,14 @@ struct WarpSmemAlpha : WarpSmem {
 // Mesh stage. A work item is one meshlet of one view: a single-view draw numbers its meshlets
 // 0..count-1; a batched draw concatenates the meshlet ranges of its views (viewStart is their
 // prefix), so one launch serves views of any size.
-// Two passes: the opaque pass (kAlpha false) draws every meshlet with the opaque shader and
-// appends the work items of alpha-tested meshlets to alphaList; the alpha pass (kAlpha true)
-// draws those with FS_EncodeSurfaceId<true>. The order of the passes does not change the keys.
-template <bool kAlpha>
+// Vis-buffer draws take two passes: the opaque pass draws every opaque meshlet and appends the
+// work items of alpha-tested meshlets to alphaList; the alpha pass draws those with
+// FS_EncodeSurfaceId<true>. The order of the passes does not change the keys. OverdrawShader draws
+// take one pass over every meshlet.
+enum : int { kPassOpaque = 0, kPassAlpha = 1, kPassOverdraw = 2 };
+template <int kPass>
 __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
+    constexpr bool kAlpha = kPass == kPassAlpha, kOver = kPass == kPassOverdraw;
     using Smem = typename std::conditional<kAlpha, WarpSmemAlpha, WarpSmem>::type;
     extern __shared__ __align__(16) unsigned char smemRaw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -645,6 +750,8 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     const bool multi = a.views != nullptr;
     const uint32_t totalItems = kAlpha ? (uint32_t)a.s.control[9] : (multi ? a.viewStart[a.numViews] : a.count);
     unsigned long long* const cursor = &a.s.control[kAlpha ? 10 : 0];
+    unsigned long long* const idleWarps = &a.s.control[kAlpha ? 12 : 11];  // warps past their last item
+    const uint32_t numWarps = gridDim.x * (blockDim.x >> 5);
     uint32_t curView = 0xFFFFFFFFu;
     if (!multi) {
         if (lane == 0) {
@@ -661,19 +768,48 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     unsigned long long nProcessed = 0, nRaster = 0, nClipped = 0;
     if (!kAlpha && blockIdx.x == 0 && threadIdx.x == 0) a.s.control[8] = 0;  // the chunk stage's cursor (runs later)
 
-    // Work items are fetched kFetch at a time: one contended atomic per kFetch items.
+    // Work items are fetched kFetch at a time: one contended atomic per kFetch items. Batched
+    // draws, most of whose (view, meshlet) items are culled, fetch 32 at a time and test the 32
+    // cull bits at once (one item per lane), then walk the visible ones.
     constexpr uint32_t kFetch = 4;
     uint32_t fetchBase = 0, fetchLeft = 0;
+    unsigned fetchMask = 0;  // batched draws: visible items of the current fetch (bit j: item fetchBase + j)
     while (true) {
-        if (fetchLeft == 0) {
-            uint32_t b = 0;
-            if (lane == 0) b = (uint32_t)atomicAdd(cursor, (unsigned long long)kFetch);
-            fetchBase = __shfl_sync(0xFFFFFFFFu, b, 0);
-            fetchLeft = kFetch;
+        uint32_t idx;
+        if (multi && !kAlpha) {
+            if (fetchMask == 0) {
+                uint32_t b = 0;
+                if (lane == 0) b = (uint32_t)atomicAdd(cursor, 32ull);
+                fetchBase = __shfl_sync(0xFFFFFFFFu, b, 0);
+                if (fetchBase >= totalItems) break;
+                const uint32_t it = fetchBase + lane;
+                bool vis = false;
+                if (it < totalItems) {
+                    uint32_t lo = 0, hi = a.numViews - 1;  // largest view with viewStart <= it
+                    while (lo < hi) {
+                        uint32_t mid = (lo + hi + 1) >> 1;
+                        if (a.viewStart[mid] <= it) lo = mid; else hi = mid - 1;
+                    }
+                    const uint32_t mm = it - a.viewStart[lo];
+                    const uint16_t* bm = a.views[lo].cullBitmap;
+                    vis = bm == nullptr || ((bm[mm >> 4] >> (mm & 15)) & 1);
+                }
+                fetchMask = __ballot_sync(0xFFFFFFFFu, vis);
+                if (fetchMask == 0) continue;
+            }
+            idx = fetchBase + (__ffs(fetchMask) - 1);
+            fetchMask &= fetchMask - 1;
+        } else {
+            if (fetchLeft == 0) {
+                uint32_t b = 0;
+                if (lane == 0) b = (uint32_t)atomicAdd(cursor, (unsigned long long)kFetch);
+                fetchBase = __shfl_sync(0xFFFFFFFFu, b, 0);
+                fetchLeft = kFetch;
+            }
+            idx = fetchBase++;
+            fetchLeft--;
+            if (idx >= totalItems) break;
         }
-        const uint32_t idx = fetchBase++;
-        fetchLeft--;
-        if (idx >= totalItems) break;
         const uint32_t item = kAlpha ? a.s.alphaList[idx] : idx;
         uint32_t m = item, view = 0;
         if (multi) {
@@ -695,6 +831,13 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
 
         const uint32_t g = vp.meshletOffset + m;
         const uint8_t* mp = a.meshlets + (size_t)g * kMeshletSize;
+        // The record's positions (all 64 slots) and index bytes are loaded together with its header,
+        // not after it: one memory round trip per meshlet instead of two.
+        const float* P = (const float*)(mp + kOffPositions);
+        const float px0 = P[lane], py0 = P[64 + lane], pz0 = P[128 + lane];
+        const float px1 = P[32 + lane], py1 = P[96 + lane], pz1 = P[160 + lane];
+        const uint32_t* I = (const uint32_t*)(mp + kOffIndices);
+        const uint32_t ix0 = I[lane], ix1 = I[32 + lane], ix2 = I[64 + lane];
         const uint32_t hdr = *(const uint32_t*)(mp + kOffNumVertices);
         const uint32_t matId = *(const uint32_t*)(mp + kOffMaterialId);
         const uint32_t nv = hdr & 0xFF, nt = min((hdr >> 8) & 0xFF, 128u);  // record arrays hold 64 / 128
@@ -705,29 +848,29 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
             cullMode = mt.is_double_sided ? kCullNone : kCullFrontCCW;
             alphaTested = material_alpha_tested(mt);
         }
-        if (!kAlpha && alphaTested) {  // drawn by the alpha pass
+        if (kPass == kPassOpaque && alphaTested) {  // drawn by the alpha pass
             if (lane == 0) a.s.alphaList[atomicAdd(&a.s.control[9], 1ull)] = item;
             continue;
         }
         if (nt == 0) continue;
         nProcessed += nt;
 
-        // ShadeMeshlet vertex loop (Shading.cpp:295-298): 16-vertex chunks up to NumVertices.
+        // ShadeMeshlet vertex loop (Shading.cpp:295-298): 16-vertex chunks up to NumVertices; the
+        // slots past them are zero.
         const uint32_t nvr = min((nv + 15) & ~15u, 64u);
-        const float* P = (const float*)(mp + kOffPositions);
-        for (uint32_t v = lane; v < 64; v += 32) {
+        auto xform = [&](uint32_t v, float x, float y, float z) {
             float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
             if (v < nvr) {
-                float x = P[v], y = P[64 + v], z = P[128 + v];
                 c.x = ffma(x, vp.m[0], ffma(y, vp.m[4], ffma(z, vp.m[8], vp.m[12])));
                 c.y = ffma(x, vp.m[1], ffma(y, vp.m[5], ffma(z, vp.m[9], vp.m[13])));
                 c.z = ffma(x, vp.m[2], ffma(y, vp.m[6], ffma(z, vp.m[10], vp.m[14])));
                 c.w = ffma(x, vp.m[3], ffma(y, vp.m[7], ffma(z, vp.m[11], vp.m[15])));
             }
             pos[v] = c;
-        }
-        const uint32_t* I = (const uint32_t*)(mp + kOffIndices);
-        for (uint32_t k = lane; k < 96; k += 32) S.idx[k] = I[k];
+        };
+        xform(lane, px0, py0, pz0);
+        xform(32 + lane, px1, py1, pz1);
+        S.idx[lane] = ix0, S.idx[32 + lane] = ix1, S.idx[64 + lane] = ix2;
         __syncwarp();
 
         for (uint32_t base = 0; base < nt; base += 32) {
@@ -780,6 +923,32 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                                idxBytes);
             __syncwarp();
 
+            // Once half of the warps have run out of work items, the warps still busy are the
+            // kernel's tail (in a sparse frame, a few visible meshlets are all of it). A packet whose
+            // small triangles cover more than kPacketTiles tiles would then keep this warp busy for
+            // many steps while the others idle: its triangles of more than kSpreadTiles tiles go to
+            // the queue, whose chunks spread over all warps of the chunk stage. (Sparser budgets, or
+            // a second level once 90 % of the warps are idle, cost the dense frame more than they
+            // gain in the sparse one.)
+            bool spread = false;
+            if (__reduce_add_sync(0xFFFFFFFFu, (unsigned)myTiles) > kPacketTiles) {
+                unsigned long long idle = 0;
+                if (lane == 0) idle = *(volatile unsigned long long*)idleWarps;
+                spread = __shfl_sync(0xFFFFFFFFu, idle, 0) * 2 >= numWarps;
+            }
+            if (spread && myTiles > kSpreadTiles) {
+                TriRec r = tris[lane];
+                bool queued;
+                if constexpr (kAlpha) {
+                    r.pad = view | kTriAlpha;
+                    queued = enqueue_alpha(r, S.exts[lane], a, chunk);
+                } else {
+                    r.pad = view;
+                    queued = enqueue_big(r, a, chunk);
+                }
+                if (queued) myTiles = 0;
+            }
+
             // Small triangles: the warp walks the concatenated tile lists of all of them, two
             // tiles (32 pixels) per step, so tiny triangles share steps.
             int incl = myTiles;
@@ -814,6 +983,9 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                     const DevMaterial& mt = a.materials[matId];
                     shade_live_tiles_alpha(tris, S.exts, own, mt.tex, mt.alpha_cutoff << 24, liveMask, tpx, tpy, tmin,
                                            vp.keys, vp.tileMin, vp.width, lane);
+                } else if constexpr (kOver) {
+                    shade_live_tiles_overdraw([&](uint32_t q) -> const TriRec& { return tris[q]; }, own, liveMask, tpx, tpy,
+                                              vp.keys, a.counts, vp.width, lane);
                 } else {
                     shade_live_tiles([&](uint32_t q) -> const TriRec& { return tris[q]; }, own, liveMask, tpx, tpy, tmin,
                                      vp.keys, vp.tileMin, vp.width, lane);
@@ -831,6 +1003,8 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                     const DevMaterial& mt = a.materials[matId];
                     raster_region_alpha(&tris[src], &S.exts[src], mt.tex, mt.alpha_cutoff << 24, x0, y0, tx, ty, vp.keys,
                                         vp.tileMin, vp.width, lane);
+                } else if constexpr (kOver) {
+                    raster_region_overdraw(r, x0, y0, tx, ty, vp.keys, a.counts, vp.width, lane);
                 } else {
                     raster_region(r, x0, y0, tx, ty, vp.keys, vp.tileMin, vp.width, lane);
                 }
@@ -842,18 +1016,20 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     // perf counters (Rasterizer.h:366-370)
     nRaster = __reduce_add_sync(0xFFFFFFFFu, (unsigned)nRaster);
     if (lane == 0) {
+        atomicAdd(idleWarps, 1ull);
         if (nProcessed) atomicAdd(&a.s.control[3], nProcessed);
         if (nRaster) atomicAdd(&a.s.control[4], nRaster);
         if (nClipped) atomicAdd(&a.s.control[5], nClipped);
     }
 }
 
-// Chunk stage: warps take runs of kChunkRun consecutive chunks (chunk x chunk tiles) of the queued
+// Chunk stage: warps take runs of up to kChunkRun consecutive chunks (chunk x chunk tiles) of the queued
 // triangles from a global cursor (control[8], zeroed by the mesh stage), locate the run's first
 // chunk by binary search over the queue's chunk prefix and walk the rest sequentially. A queued
 // triangle carries its view in pad (batched draws) or belongs to the single view; an alpha-tested
 // one (kTriAlpha) has its AlphaExt in the next slot, which owns no chunks and is never selected.
 constexpr uint32_t kChunkRun = 8;
+constexpr uint32_t kRunsPerWarp = 4;  // a shorter run when the queue holds fewer chunks than this many runs a warp
 
 // A chunk of the alpha-tested triangle whose record (and AlphaExt after it) is at q, kept out of
 // line so that the opaque chunks keep the kernel's registers.
@@ -865,13 +1041,15 @@ __device__ __noinline__ void raster_chunk_alpha(const TriRec* q, const DevMateri
     raster_region_alpha(q, xp, mt.tex, mt.alpha_cutoff << 24, x0, y0, tilesX, tilesY, keys, tileMin, width, lane);
 }
 
+template <bool kOver>
 __global__ void __launch_bounds__(256, 5) k_raster_big(const TriRec* __restrict__ big, const unsigned long long* __restrict__ bigBase,
                                                     unsigned long long* control, uint32_t capacity,
                                                     unsigned long long* keys, uint32_t* tileMin, uint32_t width,
                                                     const ViewParams* __restrict__ views, uint32_t chunk,
-                                                    const DevMaterial* __restrict__ materials) {
+                                                    const DevMaterial* __restrict__ materials, unsigned long long* counts) {
     const unsigned long long q = control[1];
-    if (blockIdx.x == 0 && threadIdx.x == 0) control[9] = control[10] = 0;  // the next draw's alpha list
+    if (blockIdx.x == 0 && threadIdx.x == 0)  // the next draw's alpha list and idle-warp counts
+        control[9] = control[10] = control[11] = control[12] = 0;
     const uint32_t n = (uint32_t)min((unsigned long long)capacity, q >> 40);
     if (n == 0) return;
     const int lane = threadIdx.x & 31;
@@ -880,12 +1058,15 @@ __global__ void __launch_bounds__(256, 5) k_raster_big(const TriRec* __restrict_
     const int lastTY = (int)(((last.bbMax >> 16) - (last.bbMin >> 16)) >> 2);
     const unsigned long long total = bigBase[n - 1] + (unsigned long long)((lastTX + chunk - 1) / chunk) *
                                                           ((lastTY + chunk - 1) / chunk);
+    // a sparse queue (few big triangles) is spread with shorter runs so that every warp gets work
+    const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
+    const unsigned long long run = max(1ull, min((unsigned long long)kChunkRun, total / (warps * kRunsPerWarp)));
     while (true) {
         unsigned long long w0 = 0;
-        if (lane == 0) w0 = atomicAdd(&control[8], (unsigned long long)kChunkRun);
+        if (lane == 0) w0 = atomicAdd(&control[8], run);
         w0 = __shfl_sync(0xFFFFFFFFu, w0, 0);
         if (w0 >= total) break;
-        const unsigned long long w1 = min(w0 + kChunkRun, total);
+        const unsigned long long w1 = min(w0 + run, total);
         // largest slot with bigBase[slot] <= w0
         uint32_t slot = 0, hi = n - 1;
         while (slot < hi) {
@@ -916,7 +1097,9 @@ __global__ void __launch_bounds__(256, 5) k_raster_big(const TriRec* __restrict_
             const uint32_t x0 = minX + cx * (chunk * 4), y0 = minY + cy * (chunk * 4);
             const uint32_t x1 = min(x0 + chunk * 4, maxX), y1 = min(y0 + chunk * 4, maxY);
             // Empty and hidden tiles of the chunk are rejected inside raster_region.
-            if (r.pad & kTriAlpha) {
+            if constexpr (kOver) {
+                raster_region_overdraw(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys, counts, vwidth, lane);
+            } else if (r.pad & kTriAlpha) {
                 raster_chunk_alpha(big + slot, materials, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys,
                                    vtiles, vwidth, lane);
             } else {
@@ -978,6 +1161,21 @@ __global__ void k_finalize(const unsigned long long* __restrict__ keys, uint32_t
     }
 }
 
+// OverdrawShader results: layer 0 += the counters (two saturating 16-bit halves, as the
+// reference's _mm512_adds_epu16 accumulate them), layer 1 = the maximum depth where a sample
+// raised it.
+__global__ void k_finalize_overdraw(const unsigned long long* __restrict__ keys, const unsigned long long* __restrict__ counts,
+                                    uint32_t* __restrict__ l0, uint32_t* __restrict__ l1, uint32_t n) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const unsigned long long c = counts[i];
+        const uint32_t old = l0[i];
+        const unsigned long long lo = (old & 0xFFFFu) + (c & 0xFFFFFFFFull), hi = (old >> 16) + (c >> 32);
+        l0[i] = (uint32_t)min(lo, 0xFFFFull) | ((uint32_t)min(hi, 0xFFFFull) << 16);
+        const unsigned long long k = keys[i];
+        if ((uint32_t)k != kKeyEmptyLow) l1[i] = __float_as_uint(float_unorder((uint32_t)(k >> 32)));
+    }
+}
+
 // Framebuffer::GetPixels de-tiling (ImageHelpers.cpp:109-147) into a row-major device buffer.
 __global__ void k_detile(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, uint32_t width, uint32_t height) {
     const uint32_t n = width * height;
@@ -996,28 +1194,43 @@ void launch_draw(const DrawArgs& a, cudaStream_t st, int numSMs) {
     const uint32_t warps = a.warpsPerBlock ? a.warpsPerBlock : kWarpsPerBlock;
     const size_t smem = warps * sizeof(WarpSmem), smemAlpha = warps * sizeof(WarpSmemAlpha);
     static size_t s_smemSet = 0, s_smemSetAlpha = 0;
-    if (smem > s_smemSet && smem > 48 * 1024) {
-        cudaFuncSetAttribute(k_draw_meshlets<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        s_smemSet = smem;
+    static size_t s_smemSetOver = 0;
+    if (smem > 48 * 1024) {
+        size_t& set = a.counts ? s_smemSetOver : s_smemSet;
+        if (smem > set) {
+            cudaFuncSetAttribute(a.counts ? k_draw_meshlets<kPassOverdraw> : k_draw_meshlets<kPassOpaque>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            set = smem;
+        }
     }
     if (a.s.alphaList && smemAlpha > s_smemSetAlpha && smemAlpha > 48 * 1024) {
-        cudaFuncSetAttribute(k_draw_meshlets<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemAlpha);
+        cudaFuncSetAttribute(k_draw_meshlets<kPassAlpha>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemAlpha);
         s_smemSetAlpha = smemAlpha;
     }
     const uint32_t chunk = a.chunkTiles ? a.chunkTiles : kChunkTiles;
+    const int grid = numSMs * (32 / warps);  // 64 registers a thread leave room for 32 resident warps per SM
+    if (a.counts) {  // OverdrawShader: one pass, every meshlet
+        {
+            LaunchScope ls("k_draw_meshlets_overdraw", st);
+            k_draw_meshlets<kPassOverdraw><<<grid, warps * 32, smem, st>>>(a);
+        }
+        LaunchScope ls("k_raster_big_overdraw", st);
+        k_raster_big<true><<<numSMs * 8, 256, 0, st>>>(a.s.big, a.s.bigBase, a.s.control, a.s.bigCapacity, a.keys, nullptr,
+                                                       a.width, a.views, chunk, a.materials, a.counts);
+        return;
+    }
     {
-        // 64 registers a thread (launch bounds) leave room for 32 resident warps per SM
         LaunchScope ls("k_draw_meshlets", st);
-        k_draw_meshlets<false><<<numSMs * (32 / warps), warps * 32, smem, st>>>(a);
+        k_draw_meshlets<kPassOpaque><<<grid, warps * 32, smem, st>>>(a);
     }
     if (a.s.alphaList) {  // the scene has alpha-tested materials
         LaunchScope ls("k_draw_meshlets_alpha", st);
-        k_draw_meshlets<true><<<numSMs * (32 / warps), warps * 32, smemAlpha, st>>>(a);
+        k_draw_meshlets<kPassAlpha><<<grid, warps * 32, smemAlpha, st>>>(a);
     }
     {
         LaunchScope ls("k_raster_big", st);
-        k_raster_big<<<numSMs * 8, 256, 0, st>>>(a.s.big, a.s.bigBase, a.s.control, a.s.bigCapacity, a.keys, a.tileMin,
-                                                 a.width, a.views, chunk, a.materials);
+        k_raster_big<false><<<numSMs * 8, 256, 0, st>>>(a.s.big, a.s.bigBase, a.s.control, a.s.bigCapacity, a.keys,
+                                                        a.tileMin, a.width, a.views, chunk, a.materials, nullptr);
     }
 }
 
@@ -1040,6 +1253,12 @@ void launch_fill(uint32_t* dst, uint32_t n, uint32_t value, cudaStream_t st) {
 void launch_finalize(const unsigned long long* keys, uint32_t* l0, uint32_t* l1, uint32_t n, cudaStream_t st) {
     LaunchScope ls("k_finalize", st);
     k_finalize<<<grid_for(n, 2, 256), 256, 0, st>>>(keys, l0, l1, n);
+}
+
+void launch_finalize_overdraw(const unsigned long long* keys, const unsigned long long* counts, uint32_t* l0, uint32_t* l1,
+                              uint32_t n, cudaStream_t st) {
+    LaunchScope ls("k_finalize_overdraw", st);
+    k_finalize_overdraw<<<grid_for(n, 1, 256), 256, 0, st>>>(keys, counts, l0, l1, n);
 }
 
 void launch_detile(const uint32_t* src, uint32_t* dst, uint32_t width, uint32_t height, cudaStream_t st) {

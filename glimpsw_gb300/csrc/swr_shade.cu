@@ -176,12 +176,13 @@ struct ResolveArgs {
     uint32_t numLights;
     DevTexture sky;
     int hasSky;
+    uint32_t debugLayer;    // SWR_DEBUG_* of the debug mode
 };
 
 // Neural resolve: the emit pass records, per pixel, the texels of the levels the model decodes
 // (4 slots: the nearest texel, or the bilinear quad's 00 10 01 11 texels; ~0 = none) and counts
 // them per material; the shade pass reads the decoded texels from the same slots.
-enum { kResolvePlain = 0, kResolveEmit = 1, kResolveNeural = 2 };
+enum { kResolvePlain = 0, kResolveEmit = 1, kResolveNeural = 2, kResolveDebug = 3 };
 struct NeuralResolve {
     const DevTexture* tex;             // model textures (data == nullptr: not decoded)
     uint32_t numMaterials, decodedLevels;  // texture levels below decodedLevels are decoded
@@ -228,6 +229,40 @@ __device__ F3 sample_env(const DevTexture& t, F3 dir) {
     return { ra.x + (rb.x - ra.x) * fy, ra.y + (rb.y - ra.y) * fy, ra.z + (rb.z - ra.z) * fy };
 }
 
+// Turbo colormap (Google Research 2019, polynomial fit; Shading.cpp:249-260) in the reference's
+// Horner order.
+__device__ __forceinline__ F3 colormap_turbo(float x) {
+    constexpr float c[18] = {
+        0.13572138f, 4.61539260f,  -42.66032258f, 132.13108234f, -152.94239396f, 59.28637943f,
+        0.09140261f, 2.19418839f,  4.84296658f,   -14.18503333f, 4.27729857f,    2.82956604f,
+        0.10667330f, 12.64194608f, -60.58204836f, 110.36276771f, -89.90310912f,  27.34824973f,
+    };
+    auto poly = [&](int k) { return x * (x * (x * (x * (x * c[k + 5] + c[k + 4]) + c[k + 3]) + c[k + 2]) + c[k + 1]) + c[k]; };
+    return { poly(0), poly(6), poly(12) };
+}
+
+// RGBA8u::Unpack of the RGB bytes (Texture.h:28-36).
+__device__ __forceinline__ F3 unpack_rgb8(uint32_t p) {
+    const float s = 1.0f / 255;
+    return { (float)(p & 255) * s, (float)((p >> 8) & 255) * s, (float)((p >> 16) & 255) * s };
+}
+
+// ResolveDebug's colour of one non-sky pixel (Shading.cpp:748-768) as RGBA8u::Pack({c, 1}); data is
+// the pixel's layer-0 word, the surface values are read for layers 1-3 only.
+__device__ __forceinline__ uint32_t debug_pixel(uint32_t layer, uint32_t data, uint32_t albedo, F3 N, float metallic,
+                                                float roughness) {
+    F3 c = { 0.0f, 0.0f, 0.0f };
+    if (layer == SWR_DEBUG_BASE_COLOR) c = unpack_rgb8(albedo);
+    else if (layer == SWR_DEBUG_NORMALS) c = { N.x * 0.5f + 0.5f, N.y * 0.5f + 0.5f, N.z * 0.5f + 0.5f };
+    else if (layer == SWR_DEBUG_METALLIC_ROUGHNESS) c = { metallic, roughness, 0.0f };
+    else if (layer == SWR_DEBUG_MESHLET_ID) c = unpack_rgb8((data / 128u) * 123456789u);
+    else if (layer == SWR_DEBUG_TRIANGLE_ID) c = unpack_rgb8(data * 123456789u);
+    else if (layer == SWR_DEBUG_OVERDRAW_PIXEL) c = colormap_turbo((float)(data >> 16) / 30.0f);
+    else if (layer == SWR_DEBUG_OVERDRAW_QUAD) c = colormap_turbo(((float)(data >> 16) + (float)(data & 0xFFFF) * 0.5f) / 30.0f);
+    return sat_u8(round2i(c.x * 255.0f)) | (sat_u8(round2i(c.y * 255.0f)) << 8) | (sat_u8(round2i(c.z * 255.0f)) << 16) |
+           (255u << 24);
+}
+
 template <int kMode>
 __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a, NeuralResolve nr) {
     const uint32_t lane = threadIdx.x & 31, l = lane & 15, half = lane >> 4;
@@ -255,6 +290,15 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a, NeuralResolve nr
 
     F3 color = { 0.f, 0.f, 0.f };
     unsigned long long req[4] = { ~0ull, ~0ull, ~0ull, ~0ull };
+    // ResolveDebug: sky pixels get a checkerboard of 4x4 tiles; layers other than the surface
+    // ones need no surface
+    const uint32_t background = ((x0 ^ y0) & 4) ? 0xFFA0A0A0u : 0xFFFFFFFFu;
+    if constexpr (kMode == kResolveDebug) {
+        if (skyBits == 0xFFFF || a.debugLayer - 1u >= 3u) {
+            a.color[off] = isSky ? background : debug_pixel(a.debugLayer, id, 0u, F3{}, 0.0f, 0.0f);
+            return;
+        }
+    }
     if constexpr (kMode == kResolveEmit) {
         if (skyBits == 0xFFFF) {
             uint4* dst = (uint4*)(nr.pixelReq + (size_t)off * 4);
@@ -342,7 +386,7 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a, NeuralResolve nr
             const int32_t mip = ilog2_x86(vmax(ddx2, ddy2)) >> 1;
             const bool nearest = __ballot_sync(hm, mip > 0) & hm;
             if ((iter >> l) & 1) {
-                if constexpr (kMode == kResolvePlain) {
+                if constexpr (kMode == kResolvePlain || kMode == kResolveDebug) {
                     albedo = sample_rgba8(tex, texU, texV, 0, mip, nearest);
                     if (tex.num_layers >= 2) nmr = sample_rgba8(tex, texU, texV, 1, mip, nearest);
                 } else {
@@ -422,6 +466,10 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a, NeuralResolve nr
         }
         const float metallic = (float)((nmr >> 16) & 255) * (1.0f / 255);
         const float roughness = (float)((nmr >> 24) & 255) * (1.0f / 255);
+        if constexpr (kMode == kResolveDebug) {
+            a.color[off] = isSky ? background : debug_pixel(a.debugLayer, id, albedo, N, metallic, roughness);
+            return;
+        }
 
         // ---- EvalLighting (Shading.cpp:602-645)
         const float invPi = 0.3183098861837907f;
@@ -651,6 +699,27 @@ swr_status swr_resolve(swr_rasterizer r, swr_framebuffer fb, const swr_shading_c
     if (a.lights) cudaFreeAsync((void*)a.lights, st);
     if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_resolve");
     fb->keys_valid = false;  // layer 0 now holds colour; a later draw rebuilds its keys from depth
+    return SWR_OK;
+}
+
+swr_status swr_resolve_debug(swr_rasterizer r, swr_framebuffer fb, const swr_shading_context* ctx, uint32_t layer) {
+    (void)r;
+    if (layer > SWR_DEBUG_OVERDRAW_QUAD) return swr_internal_fail(SWR_EINVAL, "swr_resolve_debug: unknown debug layer");
+    ResolveArgs a = {};
+    swr_status s = build_resolve_args(fb, ctx, a, "swr_resolve_debug");
+    if (s != SWR_OK) return s;
+    a.debugLayer = layer;
+    cudaStream_t st = swr_internal_stream();
+    const uint32_t tiles = (fb->width / 4) * (fb->height / 4);
+    cudaError_t e;
+    {
+        LaunchScope ls("k_resolve_debug", st);
+        k_resolve<kResolveDebug><<<(tiles * 16 + 255) / 256, 256, 0, st>>>(a, NeuralResolve{});
+        e = cudaGetLastError();
+    }
+    if (a.lights) cudaFreeAsync((void*)a.lights, st);
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_resolve_debug");
+    fb->keys_valid = false;  // layer 0 now holds colour
     return SWR_OK;
 }
 

@@ -45,6 +45,21 @@ typedef struct swr_texture_t* swr_texture;
 /* ShadingContext::VisBufferShader (Shading.cpp:649-654): mesh shader ShadeMeshlet with fragment
  * entry points FS_EncodeSurfaceId<false> (0) and FS_EncodeSurfaceId<true> (1). */
 #define SWR_SHADER_VISBUFFER 0u
+/* ShadingContext::OverdrawShader (Shading.cpp:656): FS_Overdraw (333-342) for every fragment entry
+ * point. No depth test: each 4x4 tile a triangle covers adds 1 to the high 16 bits of its covered
+ * pixels' layer-0 words and 1 to the low 16 bits of the others (saturating), and layer 1 keeps the
+ * maximum depth of all 16 samples. Clear layer 0 to 0 first (Main.cpp:213). */
+#define SWR_SHADER_OVERDRAW 2u
+
+/* DebugLayer (Shading.h:8) for swr_resolve_debug. */
+#define SWR_DEBUG_NONE 0u
+#define SWR_DEBUG_BASE_COLOR 1u
+#define SWR_DEBUG_NORMALS 2u
+#define SWR_DEBUG_METALLIC_ROUGHNESS 3u
+#define SWR_DEBUG_MESHLET_ID 4u
+#define SWR_DEBUG_TRIANGLE_ID 5u
+#define SWR_DEBUG_OVERDRAW_PIXEL 6u
+#define SWR_DEBUG_OVERDRAW_QUAD 7u
 
 /* Texel formats (pixfmt::*, Texture.h:23-200). */
 #define SWR_FORMAT_RGBA8U 0u
@@ -230,6 +245,11 @@ swr_status swr_downsample_depth(swr_framebuffer fb, swr_texture dest);
 /* ShadingContext::Resolve(Rasterizer&, Framebuffer&) (Shading.cpp:658-690): shades the vis-buffer
  * into RGBA8 colour written over layer 0. The light-sprite overlay (691-731) is not drawn. */
 swr_status swr_resolve(swr_rasterizer r, swr_framebuffer fb, const swr_shading_context* ctx);
+/* ShadingContext::ResolveDebug(Rasterizer&, Framebuffer&, DebugLayer) (Shading.cpp:734-773): the
+ * selected SWR_DEBUG_* layer as RGBA8 over layer 0: surface base colour, normal or metal/rough
+ * (from the vis-buffer), hashed meshlet or triangle ids, or the OverdrawShader's counters through
+ * the Turbo colormap; sky pixels (depth <= 0) get a grey/white checkerboard of 4x4 tiles. */
+swr_status swr_resolve_debug(swr_rasterizer r, swr_framebuffer fb, const swr_shading_context* ctx, uint32_t layer);
 
 /* ---- Learned texture decoder (no counterpart in the reference) ----
  * One model holds, per material, an FP16 latent pyramid of 8 channels (latent level k has the size

@@ -53,7 +53,11 @@ class OrcShadingContext(C.Structure):
 
 
 class OrcRasterFlags(C.Structure):
-    _fields_ = [("enable_binning", C.c_int), ("enable_clipping", C.c_int), ("enable_guardband", C.c_int)]
+    _fields_ = [("enable_binning", C.c_int), ("enable_clipping", C.c_int), ("enable_guardband", C.c_int),
+                ("shader", C.c_int)]
+
+
+SHADER_VISBUFFER, SHADER_OVERDRAW = 0, 2
 
 
 def lib():
@@ -163,8 +167,8 @@ class Context:
 
 
 def draw_meshlets(fb: Framebuffer, ctx: Context, count: int, binning=False, clipping=True, guardband=True,
-                  threads: int = 1) -> np.ndarray:
-    flags = OrcRasterFlags(int(binning), int(clipping), int(guardband))
+                  threads: int = 1, shader: int = SHADER_VISBUFFER) -> np.ndarray:
+    flags = OrcRasterFlags(int(binning), int(clipping), int(guardband), int(shader))
     counters = np.zeros(4, dtype=np.uint64)
     if threads > 1:
         lib().orc_draw_meshlets_mt(C.byref(fb.s), C.c_uint32(count), C.byref(ctx.s), C.byref(flags),
@@ -195,6 +199,11 @@ def resolve(fb: Framebuffer, ctx: Context, threads: int = 1):
         lib().orc_resolve(C.byref(fb.s), C.byref(ctx.s))
 
 
+def resolve_debug(fb: Framebuffer, ctx: Context, layer: int, threads: int = 1):
+    """ShadingContext::ResolveDebug (Shading.cpp:734-773), layer as DebugLayer (Shading.h:8)."""
+    lib().orc_resolve_debug_mt(C.byref(fb.s), C.byref(ctx.s), C.c_uint32(layer), C.c_uint32(threads))
+
+
 def set_approx_mode(mode: int) -> bool:
     if not lib().orc_approx_mode_available(mode):
         return False
@@ -211,5 +220,6 @@ def hiz_texture_size(width: int, height: int) -> tuple[int, int]:
 
 
 __all__ = ["Framebuffer", "Texture", "Context", "draw_meshlets", "cull_meshlets", "downsample_depth",
-           "resolve", "set_approx_mode", "hiz_texture_size", "lib"]
+           "resolve", "resolve_debug", "set_approx_mode", "hiz_texture_size", "lib", "SHADER_VISBUFFER",
+           "SHADER_OVERDRAW"]
 _ = os

@@ -73,10 +73,13 @@ typedef struct {
     uint32_t num_meshlets;          // size of the meshlet pool (bounds surface ids in the resolve)
 } orc_shading_context;
 
-// Rasterizer flags (Rasterizer.h:205-208).
+// Rasterizer flags (Rasterizer.h:205-208) and the shader table of the draw: 0 VisBufferShader,
+// 2 OverdrawShader (Shading.cpp:649-656).
 typedef struct {
     int enable_binning, enable_clipping, enable_guardband;
+    int shader;
 } orc_raster_flags;
+enum { ORC_SHADER_VISBUFFER = 0, ORC_SHADER_OVERDRAW = 2 };
 
 // PerfCounter (Rasterizer.h:366-370): processed, rasterized, clipped, bin flushes.
 enum { ORC_TRIS_PROCESSED = 0, ORC_TRIS_RASTERIZED = 1, ORC_TRIS_CLIPPED = 2, ORC_BIN_FLUSHES = 3 };
@@ -127,6 +130,13 @@ void orc_downsample_depth(const orc_framebuffer* fb, orc_texture* dest);
 void orc_resolve(orc_framebuffer* fb, const orc_shading_context* ctx);
 void orc_resolve_rows(orc_framebuffer* fb, const orc_shading_context* ctx, uint32_t row_begin, uint32_t row_end);
 void orc_resolve_mt(orc_framebuffer* fb, const orc_shading_context* ctx, uint32_t num_threads);
+
+// ShadingContext::ResolveDebug (Shading.cpp:734-773); layer is a DebugLayer (Shading.h:8):
+// 0 None, 1 BaseColor, 2 Normals, 3 MetallicRoughness, 4 MeshletId, 5 TriangleId,
+// 6 OverdrawPixel, 7 OverdrawQuad.
+void orc_resolve_debug_rows(orc_framebuffer* fb, const orc_shading_context* ctx, uint32_t layer,
+                            uint32_t row_begin, uint32_t row_end);
+void orc_resolve_debug_mt(orc_framebuffer* fb, const orc_shading_context* ctx, uint32_t layer, uint32_t num_threads);
 
 #ifdef __cplusplus
 }

@@ -315,6 +315,44 @@ static void draw_triangle_alpha(DrawCtx& dc, const EdgeVars& e, uint32_t bbMin, 
     }
 }
 
+// DrawTriangle<FS_Overdraw> (Rasterizer.h:250-328, Shading.cpp:333-342): no depth test; every tile
+// of the box with a covered sample adds 1 to the high 16 bits of its covered pixels' colour words
+// and 1 to the low 16 bits of the others (saturating, _mm512_adds_epu16), and stores
+// max(Depth, old) on all 16 samples.
+static inline uint32_t adds_epu16(uint32_t a, uint32_t b) {
+    uint32_t lo = std::min((a & 0xFFFF) + (b & 0xFFFF), 0xFFFFu), hi = std::min((a >> 16) + (b >> 16), 0xFFFFu);
+    return lo | (hi << 16);
+}
+static void draw_triangle_overdraw(DrawCtx& dc, const EdgeVars& e, uint32_t bbMin, uint32_t bbMax) {
+    orc_framebuffer* fb = dc.fb;
+    uint32_t minX = bbMin & 0xFFFF, minY = bbMin >> 16;
+    uint32_t maxX = bbMax & 0xFFFF, maxY = bbMax >> 16;
+    float* depthBuf = (float*)&fb->data[1 * fb->layer_stride];
+    uint32_t* colorBuf = &fb->data[0];
+    for (uint32_t ty = std::max(minY, dc.rowBegin & ~3u); ty < maxY && ty < dc.rowEnd; ty += 4) {
+        for (uint32_t tx = minX; tx < maxX; tx += 4) {
+            float depth[16];
+            uint32_t mask = 0;
+            for (uint32_t l = 0; l < 16; l++) {
+                uint32_t x = tx + (l & 3), y = ty + (l >> 2);
+                int32_t e0 = (int32_t)((uint32_t)e.Edge0 + (uint32_t)e.A12 * x + (uint32_t)e.B12 * y);
+                int32_t e1 = (int32_t)((uint32_t)e.Edge1 + (uint32_t)e.A20 * x + (uint32_t)e.B20 * y);
+                int32_t e2 = (int32_t)((uint32_t)e.Edge2 + (uint32_t)e.A01 * x + (uint32_t)e.B01 * y);
+                if ((e0 | e1 | e2) >= 0) mask |= 1u << l;
+                depth[l] = std::fma((float)e1, e.Z10, std::fma((float)e2, e.Z20, e.Z0));
+            }
+            if (mask == 0) continue;
+            for (uint32_t l = 0; l < 16; l++) {
+                uint32_t y = ty + (l >> 2);
+                if (y < dc.rowBegin || y >= dc.rowEnd) continue;
+                uint32_t off = pixel_offset(fb, tx + (l & 3), y);
+                colorBuf[off] = adds_epu16(colorBuf[off], ((mask >> l) & 1) ? 0x00010000u : 0x00000001u);
+                depthBuf[off] = vmax(depth[l], depthBuf[off]);
+            }
+        }
+    }
+}
+
 // ShadeMeshlet, Shading.cpp:281-307. ShadedMeshlet (Rasterizer.h:82-99) with vertices past the
 // transformed 16-vertex chunks zero-initialised (uninitialised stack memory in the reference).
 struct Shaded {
@@ -445,7 +483,8 @@ static void draw_meshlets(DrawCtx& dc, uint32_t count, const orc_raster_flags* f
         // material's texture unconditionally; a material without one passes every fragment here.
         const orc_texture* alphaTex = nullptr;
         uint32_t cutoff = 0;
-        if (mesh.FragmentShaderId != 0) {
+        const bool overdraw = flags->shader == ORC_SHADER_OVERDRAW;  // one entry point for every FS id (Rasterizer.h:356-360)
+        if (mesh.FragmentShaderId != 0 && !overdraw) {
             const orc_material& mat = sc->materials[mesh.MaterialId];
             if (mat.texture != UINT32_MAX && sc->textures && sc->textures[mat.texture].data) alphaTex = &sc->textures[mat.texture];
             cutoff = (uint32_t)mat.alpha_cutoff << 24;
@@ -487,7 +526,8 @@ static void draw_meshlets(DrawCtx& dc, uint32_t count, const orc_raster_flags* f
                     render_bbox(t, halfW, halfH, bbMin, bbMax);
                     EdgeVars e;
                     edge_setup(t, halfW, halfH, e);
-                    if (alphaTex) draw_triangle_alpha(dc, e, bbMin, bbMax, meshIdx, primOffset + l, alpha_tri(primOffset + l, nullptr));
+                    if (overdraw) draw_triangle_overdraw(dc, e, bbMin, bbMax);
+                    else if (alphaTex) draw_triangle_alpha(dc, e, bbMin, bbMax, meshIdx, primOffset + l, alpha_tri(primOffset + l, nullptr));
                     else draw_triangle(dc, e, bbMin, bbMax, meshIdx, primOffset + l);
                     if (dc.counters) dc.counters[ORC_TRIS_RASTERIZED]++;
                 }
@@ -502,7 +542,8 @@ static void draw_meshlets(DrawCtx& dc, uint32_t count, const orc_raster_flags* f
                     EdgeVars e;
                     edge_setup(co.t, halfW, halfH, e);
                     uint32_t prim = primOffset + co.primId;
-                    if (alphaTex) draw_triangle_alpha(dc, e, bbMin, bbMax, meshIdx, prim, alpha_tri(prim, &co));
+                    if (overdraw) draw_triangle_overdraw(dc, e, bbMin, bbMax);
+                    else if (alphaTex) draw_triangle_alpha(dc, e, bbMin, bbMax, meshIdx, prim, alpha_tri(prim, &co));
                     else draw_triangle(dc, e, bbMin, bbMax, meshIdx, prim);
                     if (dc.counters) dc.counters[ORC_TRIS_RASTERIZED]++;
                 }

@@ -462,3 +462,84 @@ extern "C" void orc_resolve_mt(orc_framebuffer* fb, const orc_shading_context* s
     }
     for (auto& th : threads) th.join();
 }
+
+// ------------------------------------------------------------------------- debug layers
+namespace orc {
+namespace {
+
+// Turbo colormap (Google Research 2019, polynomial fit; Shading.cpp:249-260), evaluated in Horner
+// form in the reference's operation order.
+F3 colormap_turbo(float x) {
+    static const float c[18] = {
+        0.13572138f, 4.61539260f,  -42.66032258f, 132.13108234f, -152.94239396f, 59.28637943f,
+        0.09140261f, 2.19418839f,  4.84296658f,   -14.18503333f, 4.27729857f,    2.82956604f,
+        0.10667330f, 12.64194608f, -60.58204836f, 110.36276771f, -89.90310912f,  27.34824973f,
+    };
+    auto poly = [&](const float* k) { return x * (x * (x * (x * (x * k[5] + k[4]) + k[3]) + k[2]) + k[1]) + k[0]; };
+    return { poly(c), poly(c + 6), poly(c + 12) };
+}
+
+}  // namespace
+}  // namespace orc
+
+// ShadingContext::ResolveDebug (Shading.cpp:734-773): the selected layer as RGBA8 over the
+// vis-buffer (or, for the overdraw layers, the OverdrawShader's counters); sky pixels (depth <= 0)
+// get a checkerboard of 4x4 tiles.
+extern "C" void orc_resolve_debug_rows(orc_framebuffer* fb, const orc_shading_context* sc, uint32_t layer,
+                                       uint32_t row_begin, uint32_t row_end) {
+    const float W = (float)fb->width, H = (float)fb->height;
+    const float scaleU = 2.0f / W, scaleV = 2.0f / H;
+    const float centerU = 0.5f * scaleU - 1.0f, centerV = 0.5f * scaleV - 1.0f;
+    uint32_t* colorLayer = fb->data;
+    const float* depthLayer = (const float*)(fb->data + fb->layer_stride);
+    for (uint32_t y0 = row_begin & ~3u; y0 < std::min(row_end, fb->height); y0 += 4) {
+        for (uint32_t x0 = 0; x0 < fb->width; x0 += 4) {
+            uint32_t tileOffset = ((x0 & ~3u) << 2) + (y0 & ~3u) * fb->width;
+            uint32_t data[L];
+            float su[L], sv[L];
+            uint16_t sky = 0;
+            for (int l = 0; l < L; l++) {
+                data[l] = colorLayer[tileOffset + l];
+                if (depthLayer[tileOffset + l] <= 0.0f) sky |= (uint16_t)(1u << l);
+                su[l] = (float)(int32_t)(x0 + (l & 3)) * scaleU + centerU;
+                sv[l] = (float)(int32_t)(y0 + (l >> 2)) * scaleV + centerV;
+            }
+            Surface surf[L] = {};
+            if (layer >= 1 && layer <= 3) resolve_surface(sc, data, (uint16_t)~sky, su, sv, W, H, surf);
+            const uint32_t background = ((x0 ^ y0) & 4) ? 0xFFA0A0A0u : 0xFFFFFFFFu;
+            for (int l = 0; l < L; l++) {
+                F3 c = { 0.0f, 0.0f, 0.0f };
+                if (layer == 1) {
+                    F4 a = unpack_rgba8(surf[l].albedo);
+                    c = { a.x, a.y, a.z };
+                } else if (layer == 2) {
+                    c = { surf[l].normal.x * 0.5f + 0.5f, surf[l].normal.y * 0.5f + 0.5f, surf[l].normal.z * 0.5f + 0.5f };
+                } else if (layer == 3) {
+                    c = { surf[l].metallic, surf[l].roughness, 0.0f };
+                } else if (layer == 4 || layer == 5) {
+                    F4 a = unpack_rgba8((layer == 4 ? data[l] / 128u : data[l]) * 123456789u);
+                    c = { a.x, a.y, a.z };
+                } else if (layer == 6) {
+                    c = colormap_turbo((float)(data[l] >> 16) / 30.0f);
+                } else if (layer == 7) {
+                    float countPix = (float)(data[l] >> 16), countFrag = (float)(data[l] & 0xFFFF);
+                    c = colormap_turbo((countPix + countFrag * 0.5f) / 30.0f);
+                }
+                colorLayer[tileOffset + l] = ((sky >> l) & 1) ? background : pack_rgba8({ c.x, c.y, c.z, 1.0f });
+            }
+        }
+    }
+}
+
+extern "C" void orc_resolve_debug_mt(orc_framebuffer* fb, const orc_shading_context* sc, uint32_t layer,
+                                     uint32_t num_threads) {
+    num_threads = std::max(num_threads, 1u);
+    std::vector<std::thread> threads;
+    uint32_t rows = ((fb->height + num_threads - 1) / num_threads + 3) & ~3u;
+    for (uint32_t t = 0; t < num_threads; t++) {
+        uint32_t r0 = t * rows, r1 = std::min(fb->height, r0 + rows);
+        if (r0 >= r1) break;
+        threads.emplace_back([=]() { orc_resolve_debug_rows(fb, sc, layer, r0, r1); });
+    }
+    for (auto& th : threads) th.join();
+}

@@ -34,7 +34,7 @@ CLIP_FROM_OBJECT = np.array([1, 0, 0, 0,
 
 def render_oracle(meshlets, materials, object_to_clip, width, height, count=None, binning=False, clipping=True,
                   guardband=True, meshlet_offset=0, cull_bitmap=None, clear=(0xFF000000, 0.0), fb=None, threads=1,
-                  textures=None):
+                  textures=None, shader=0):
     """Oracle frame; with threads > 1 the rows are split over threads and the counters are not kept.
     textures (oracle textures by material texture index) feed the alpha test of alpha-tested materials."""
     from oracle import oracle as O
@@ -44,7 +44,8 @@ def render_oracle(meshlets, materials, object_to_clip, width, height, count=None
     ctx = O.Context(meshlets, materials, object_to_clip, meshlet_offset=meshlet_offset, cull_bitmap=cull_bitmap,
                     textures=textures)
     n = len(meshlets) - meshlet_offset if count is None else count
-    counters = O.draw_meshlets(fb, ctx, n, binning=binning, clipping=clipping, guardband=guardband, threads=threads)
+    counters = O.draw_meshlets(fb, ctx, n, binning=binning, clipping=clipping, guardband=guardband, threads=threads,
+                               shader=shader)
     return fb, counters
 
 
@@ -59,7 +60,7 @@ class GpuRenderer:
         self.rast = api.Rasterizer()
 
     def render(self, object_to_clip, width, height, count=None, binning=False, clipping=True, guardband=True,
-               meshlet_offset=0, cull_bitmap=None, clear=(0xFF000000, 0.0), fb=None):
+               meshlet_offset=0, cull_bitmap=None, clear=(0xFF000000, 0.0), fb=None, shader=0):
         api = self.api
         if fb is None:
             fb = api.Framebuffer(width, height)
@@ -70,7 +71,7 @@ class GpuRenderer:
         ctx = api.ShadingContext(self.scene, object_to_clip, meshlet_offset=meshlet_offset, cull_bitmap=cull_bitmap)
         n = (self._count() - meshlet_offset) if count is None else count
         self.rast.reset_counters()
-        self.rast.draw_meshlets(fb, n, ctx)
+        self.rast.draw_meshlets(fb, n, ctx, shader)
         return fb, self.rast.counters()
 
     def _count(self):
