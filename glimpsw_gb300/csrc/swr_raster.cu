@@ -34,6 +34,7 @@ namespace swr {
 
 constexpr int kWarpsPerBlock = 8;
 constexpr int kSmallTiles = 16;
+static_assert(kSmallTiles <= 16, "the small triangles' tile -> row multiply-shift is exact for at most 16 tiles");
 constexpr int kPacketTiles = 128;  // in-warp tile budget of a 32-triangle step
 constexpr int kSpreadTiles = 4;    // over budget, triangles above this many tiles are queued
 constexpr int kChunkTiles = 8;  // chunk = 8x8 tiles = 32x32 pixels
@@ -63,7 +64,8 @@ __device__ __forceinline__ void render_bbox(const Setup& t, int halfW, int halfH
 // TrianglePacket::Setup (Rasterizer.cpp:257-289); returns the lane's keep bit.
 __device__ __forceinline__ bool tri_setup(Vtx v0, Vtx v1, Vtx v2, int halfW, int halfH, int cullMode, Setup& t,
                                           uint32_t& bbMin, uint32_t& bbMax) {
-    float rw0 = fdiv(1.0f, v0.w), rw1 = fdiv(1.0f, v1.w), rw2 = fdiv(1.0f, v2.w);
+    // 1.0f / w (perspective_div, SIMD.h:473-476): the correctly rounded reciprocal is the same value
+    float rw0 = __frcp_rn(v0.w), rw1 = __frcp_rn(v1.w), rw2 = __frcp_rn(v2.w);
     float x0 = fmul(v0.x, rw0), y0 = fmul(v0.y, rw0);
     float x1 = fmul(v1.x, rw1), y1 = fmul(v1.y, rw1);
     float x2 = fmul(v2.x, rw2), y2 = fmul(v2.y, rw2);
@@ -114,7 +116,8 @@ __device__ __forceinline__ void edge_setup(const Setup& t, int halfW, int halfH,
     r.E1 = compute_edge(A20, sx - x2, B20, sy - y2);
     r.E2 = compute_edge(A01, sx - x0, B01, sy - y0);
     r.A12 = A12, r.B12 = B12, r.A20 = A20, r.B20 = B20, r.A01 = A01, r.B01 = B01;
-    float rcpArea = fdiv(16.0f, __int2float_rn(det));
+    // 16.0f / det: scaling the correctly rounded reciprocal by 16 is exact (|det| >= 1 or 0)
+    float rcpArea = fmul(16.0f, __frcp_rn(__int2float_rn(det)));
     r.Z0 = t.Z0;
     r.Z10 = fmul(fsub(t.Z1, t.Z0), rcpArea);
     r.Z20 = fmul(fsub(t.Z2, t.Z0), rcpArea);
@@ -237,7 +240,7 @@ struct TexCoord { float u, v; };
 __device__ __forceinline__ TexCoord alpha_texcoord(const AlphaExt& x, float u, float v) {
     const float pw0 = ffma(fadd(u, v), -x.W0S, x.W0);
     const float w = ffma(u, x.W1S, ffma(v, x.W2S, pw0));
-    float rcpW = fdiv(1.0f, w);
+    float rcpW = __frcp_rn(w);  // 1/w (rcp14 modelled as IEEE)
     rcpW = fmul(rcpW, ffma(-w, rcpW, 2.0f));  // Newton-Raphson step
     float bu = fmul(u, fmul(x.W1S, rcpW)), bv = fmul(v, fmul(x.W2S, rcpW));
     if (x.material & kTriAlpha) {  // clipped: barycentrics of the source triangle
