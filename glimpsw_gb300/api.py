@@ -45,6 +45,12 @@ class SwrLight(C.Structure):
                 ("spot_scale", C.c_float), ("spot_offset", C.c_float)]
 
 
+class SwrMeshDesc(C.Structure):
+    _fields_ = [("positions", C.c_void_p), ("texcoords", C.c_void_p), ("normal_tangents", C.c_void_p),
+                ("tangent_signs", C.c_void_p), ("num_vertices", C.c_uint32), ("indices", C.c_void_p),
+                ("num_triangles", C.c_uint32), ("material_id", C.c_uint32), ("alpha_cutoff", C.c_uint8)]
+
+
 class SwrShadingContext(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("meshlet_offset", C.c_uint32), ("cull_bitmap", C.c_void_p),
                 ("world_to_clip", C.c_float * 16), ("object_to_clip", C.c_float * 16),
@@ -118,13 +124,16 @@ _SIGS = {
     "swr_neural_set_latents": [C.c_void_p, C.c_uint32, C.c_void_p],
     "swr_neural_decode": [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p],
     "swr_resolve_neural": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+    "swr_meshlet_bound": [C.c_uint32],
+    "swr_build_meshlets": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p],
 }
 
 
 class SwrViewDesc(C.Structure):
     _fields_ = [("fb", C.c_void_p), ("proj", C.c_float * 16), ("view", C.c_float * 16), ("model", C.c_float * 16),
                 ("depth_only", C.c_uint32)]
-_RESTYPES = {"swr_last_error": C.c_char_p, "swr_get_stream": C.c_void_p, "swr_launch_count": C.c_uint64}
+_RESTYPES = {"swr_last_error": C.c_char_p, "swr_get_stream": C.c_void_p, "swr_launch_count": C.c_uint64,
+             "swr_meshlet_bound": C.c_uint32}
 
 
 def load_library(path: str = LIB_PATH):

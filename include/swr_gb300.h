@@ -207,6 +207,29 @@ swr_status swr_framebuffer_invalidate(swr_framebuffer fb);
 swr_status swr_framebuffer_size(swr_framebuffer fb, uint32_t* width, uint32_t* height, uint32_t* layer_stride,
                                 uint32_t* num_layers);
 
+/* ---- Meshlet building for imported meshes (Scene::ImportGltf, Scene.cpp:196-276) ----
+ * One primitive's triangles grouped into Meshlet records of at most 64 vertices and 128
+ * triangles, with bounds (sphere and normal cone). The reference uses meshoptimizer here; the
+ * grouping of this library is its own (greedy growth over shared vertices in Morton order), so
+ * the meshlets differ from the reference's for the same mesh. Per-vertex words are copied as
+ * given: texcoords as packed half2 (glm::packHalf2x16), normal/tangent as
+ * packUnorm4x8(oct(normal), oct(tangent)) (Scene.cpp:262-272). */
+typedef struct {
+    const float* positions;           /* x, y, z per vertex (mesh space) */
+    const uint32_t* texcoords;        /* per vertex, or NULL */
+    const uint32_t* normal_tangents;  /* per vertex, or NULL */
+    const uint8_t* tangent_signs;     /* per vertex, 1 where the tangent's w < 0, or NULL */
+    uint32_t num_vertices;
+    const uint32_t* indices;          /* 3 per triangle */
+    uint32_t num_triangles;
+    uint32_t material_id;             /* UINT32_MAX: none */
+    uint8_t alpha_cutoff;             /* Meshlet::AlphaCutoff */
+} swr_mesh_desc;
+/* An upper bound of the meshlets swr_build_meshlets makes for num_triangles triangles. */
+uint32_t swr_meshlet_bound(uint32_t num_triangles);
+/* Writes *count SWR_MESHLET_SIZE-byte records to host memory out (capacity records). */
+swr_status swr_build_meshlets(const swr_mesh_desc* mesh, void* out, uint32_t capacity, uint32_t* count);
+
 /* ---- Scene: Meshlet and Material pools (Scene.h:117-128) ---- */
 swr_status swr_scene_create(swr_scene* out);
 swr_status swr_scene_destroy(swr_scene s);
