@@ -1,5 +1,5 @@
 """Generates the golden fixtures of tests/golden/ from the CPU oracle (run from the repository root:
-`python tests/golden/make_golden.py`).
+`python tests/golden/make_golden.py [fixture names]`).
 
 The reference ships no golden vectors for this path and cannot be built here, so these fixtures
 are frozen outputs of the oracle on small seeded scenes. They pin the oracle against drift
@@ -15,6 +15,9 @@ Fixtures (all at 160x96 unless noted):
                       RGBA8, the Hi-Z pyramid of the frame, and the cull bitmap of the next camera
   neural_fwd_bwd.npz  learned decoder: forward outputs and parameter / input gradients for fixed
                       parameters, inputs and targets (oracle/neural.py)
+  alpha_debug.npz     camera inside a volume whose every second material is alpha-tested: the
+                      vis-buffer, the OverdrawShader's counters and depth, and the ResolveDebug
+                      layers base colour, meshlet id and overdraw-quad
 """
 from __future__ import annotations
 
@@ -105,6 +108,35 @@ def make_resolve_volume(O):
             "color": fb.get_pixels(0), "hiz": hiz.data.copy(), "cull_bitmap": bm, "cull_visible": np.uint32(visible)}
 
 
+def alpha_scene():
+    sc = scenes.volume_scene(n=3000, width=W, height=H, n_materials=4, extent=12.0, texture_size=32, env_size=32,
+                             alpha_every=2)
+    view = scenes.make_view(W, H, eye=(0.0, 0.0, 0.0), target=(0.3, 0.1, 1.0))
+    return sc, view
+
+
+def make_alpha_debug(O):
+    from tests.helpers import TexturePair, render_oracle
+    sc, view = alpha_scene()
+    texs = [TexturePair([sc.texture_pixels(i, 0), sc.texture_pixels(i, 1)], sc.texture_size, gpu=False) for i in range(4)]
+    tex = [t.o for t in texs]
+    out = {"scene_hash": scene_hash(sc.meshlets, sc.materials, view.world_to_clip, *[t.data for t in tex])}
+    fb, counters = render_oracle(sc.meshlets, sc.materials, view.world_to_clip, W, H, textures=tex)
+    out["alpha_ids"], out["alpha_depth"] = fb.get_pixels(0), fb.get_pixels(1)
+    out["alpha_counters"] = np.asarray(counters[:3], np.uint64)
+    ctx = O.Context(sc.meshlets, sc.materials, view.world_to_clip, textures=tex)
+    for layer in (1, 4):
+        fb, _ = render_oracle(sc.meshlets, sc.materials, view.world_to_clip, W, H, textures=tex)
+        O.resolve_debug(fb, ctx, layer)
+        out[f"debug{layer}"] = fb.get_pixels(0)
+    fb, _ = render_oracle(sc.meshlets, sc.materials, view.world_to_clip, W, H, textures=tex, clear=(0, 0.0),
+                          shader=O.SHADER_OVERDRAW)
+    out["overdraw_counts"], out["overdraw_depth"] = fb.get_pixels(0), fb.get_pixels(1)
+    O.resolve_debug(fb, ctx, 7)
+    out["debug7"] = fb.get_pixels(0)
+    return out
+
+
 def neural_case():
     """Fixed parameters, inputs, levels and targets of the decoder check."""
     rng = np.random.default_rng(2024)
@@ -132,15 +164,16 @@ def make_neural(O):
 
 
 MAKERS = {"raster_grid": make_raster_grid, "raster_inside": make_raster_inside, "resolve_volume": make_resolve_volume,
-          "neural_fwd_bwd": make_neural}
+          "neural_fwd_bwd": make_neural, "alpha_debug": make_alpha_debug}
 
 
 def main():
     from oracle import oracle as O
     O.lib()
     O.set_approx_mode(0)  # the portable rcp14/rsqrt14 model, as on the GPU
-    for name, fn in MAKERS.items():
-        out = fn(O)
+    names = sys.argv[1:] or list(MAKERS)  # regenerate the named fixtures (default: all)
+    for name in names:
+        out = MAKERS[name](O)
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **out)
         print(name, {k: (v.shape if hasattr(v, "shape") else v) for k, v in out.items()})
 

@@ -23,7 +23,7 @@ def O():
     return O
 
 
-@pytest.mark.parametrize("name", ["raster_grid", "raster_inside", "resolve_volume"])
+@pytest.mark.parametrize("name", ["raster_grid", "raster_inside", "resolve_volume", "alpha_debug"])
 def test_oracle_matches_golden(O, name):
     gold = load(name)
     out = G.MAKERS[name](O)

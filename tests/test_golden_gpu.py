@@ -76,3 +76,26 @@ def test_resolve_hiz_cull_match_golden():
     a = fb.get_pixels(0).view(np.uint8).astype(np.int32)
     b = gold["color"].view(np.uint8).astype(np.int32)
     assert np.abs(a - b).max() <= 1
+
+
+def test_alpha_overdraw_debug_match_golden():
+    from glimpsw_gb300 import api
+    gold = load("alpha_debug")
+    sc, view = G.alpha_scene()
+    texs = [TexturePair([sc.texture_pixels(i, 0), sc.texture_pixels(i, 1)], sc.texture_size) for i in range(4)]
+    check_hash(gold, sc.meshlets, sc.materials, view.world_to_clip, *[t.o.data for t in texs])
+    g = GpuRenderer(sc.meshlets, sc.materials, [t.g for t in texs])
+    fb, counters = g.render(view.world_to_clip, W, H)
+    assert np.array_equal(fb.get_pixels(0), gold["alpha_ids"])
+    assert np.array_equal(fb.get_pixels(1), gold["alpha_depth"])
+    assert list(counters[:3]) == list(gold["alpha_counters"])
+    ctx = api.ShadingContext(g.scene, view.world_to_clip)
+    for layer in (1, 4):
+        fb, _ = g.render(view.world_to_clip, W, H)
+        ctx.resolve_debug(g.rast, fb, layer)
+        assert np.array_equal(fb.get_pixels(0), gold[f"debug{layer}"]), layer
+    fb, _ = g.render(view.world_to_clip, W, H, clear=(0, 0.0), shader=api.OverdrawShader)
+    assert np.array_equal(fb.get_pixels(0), gold["overdraw_counts"])
+    assert np.array_equal(fb.get_pixels(1), gold["overdraw_depth"])
+    ctx.resolve_debug(g.rast, fb, 7)
+    assert np.array_equal(fb.get_pixels(0), gold["debug7"])
