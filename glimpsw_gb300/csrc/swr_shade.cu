@@ -128,34 +128,89 @@ __global__ void __launch_bounds__(256) k_cull(CullArgs a) {
 // texutil::DownsampleDepth (ImageHelpers.cpp:150-247). Mip m texels hold the min of the frame
 // depths they cover (FLT_MAX where they cover none). The reference writes mip m (m <= root-4) in
 // 8x8-texel blocks of 2^(m+4)-pixel regions whose origin lies inside the frame, and mip root-3
-// as one 4x4 tile; this kernel writes exactly those texels, level by level, reading mip m-1.
-__global__ void k_hiz_level(const float* __restrict__ depth, uint32_t fbW, uint32_t fbH, uint32_t* tex,
-                            uint32_t dstOff, uint32_t srcOff, int32_t rowShift, uint32_t m, uint32_t regionsX,
-                            uint32_t numTexels, uint32_t blockTexels) {
-    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= numTexels) return;
-    const uint32_t bs = blockTexels == 64 ? 8 : 4;
-    const uint32_t blk = t / blockTexels, within = t - blk * blockTexels;
-    const uint32_t by = blk / regionsX, bx = blk - by * regionsX;
-    const uint32_t tx = bx * bs + within % bs, ty = by * bs + within / bs;
-    float v;
-    if (m == 0) {
-        auto d = [&](uint32_t x, uint32_t y) -> float {
-            return (x < fbW && y < fbH) ? depth[pixel_offset(x, y, fbW)] : FLT_MAX;
-        };
-        uint32_t x = tx * 2, y = ty * 2;
-        v = vmin(vmin(d(x, y), d(x, y + 1)), vmin(d(x + 1, y), d(x + 1, y + 1)));
-    } else {
-        // children at mip m-1 cover 2^m pixels; one whose origin is outside the frame covers none
-        const int32_t sstride = rowShift - (int32_t)(m - 1);
-        auto c = [&](uint32_t x, uint32_t y) -> float {
-            if ((x << m) >= fbW || (y << m) >= fbH) return FLT_MAX;
-            return __uint_as_float(tex[srcOff + texel_offset(x, y, sstride)]);
-        };
-        uint32_t x = tx * 2, y = ty * 2;
-        v = vmin(vmin(c(x, y), c(x, y + 1)), vmin(c(x + 1, y), c(x + 1, y + 1)));
+// as one 4x4 tile. Two launches write exactly those texels: k_hiz_local makes levels 0-3 of one
+// 128x128-pixel region per block in shared memory, k_hiz_tail the levels above in one block,
+// level by level. A texel is the min of its four children in the order vmin(vmin(00, 01),
+// vmin(10, 11)); a child whose origin lies outside the frame counts as FLT_MAX.
+struct HizOffsets { uint32_t off[16]; };  // MipOffsets of the levels written (0 for levels the texture lacks)
+constexpr uint32_t kHizRegion = 128;      // pixels per side of a k_hiz_local block (level 3's 8x8 texels)
+
+__global__ void __launch_bounds__(256) k_hiz_local(const float* __restrict__ depth, uint32_t fbW, uint32_t fbH,
+                                                   uint32_t* __restrict__ tex, HizOffsets offs, int32_t rowShift,
+                                                   uint32_t nLocal) {
+    __shared__ float s0[64 * 64], s1[32 * 32], s2[16 * 16], s3[8 * 8];
+#pragma unroll
+    for (uint32_t m = 0; m < 4; m++) {
+        if (m >= nLocal) break;
+        float* dst = m == 0 ? s0 : (m == 1 ? s1 : (m == 2 ? s2 : s3));
+        const float* src = m == 1 ? s0 : (m == 2 ? s1 : s2);
+        const uint32_t side = 64u >> m, gx0 = blockIdx.x * side, gy0 = blockIdx.y * side;
+        for (uint32_t i = threadIdx.x; i < side * side; i += blockDim.x) {
+            const uint32_t lx = i % side, ly = i / side, gx = gx0 + lx, gy = gy0 + ly;
+            const uint32_t x = gx * 2, y = gy * 2;
+            float v;
+            if (m == 0) {
+                auto d = [&](uint32_t px, uint32_t py) -> float {
+                    return (px < fbW && py < fbH) ? depth[pixel_offset(px, py, fbW)] : FLT_MAX;
+                };
+                v = vmin(vmin(d(x, y), d(x, y + 1)), vmin(d(x + 1, y), d(x + 1, y + 1)));
+            } else {
+                // children at mip m-1 cover 2^m pixels; one whose origin is outside the frame covers none
+                auto c = [&](uint32_t cx, uint32_t cy) -> float {
+                    if ((cx << m) >= fbW || (cy << m) >= fbH) return FLT_MAX;
+                    return src[(cy - gy0 * 2) * (side * 2) + (cx - gx0 * 2)];
+                };
+                v = vmin(vmin(c(x, y), c(x, y + 1)), vmin(c(x + 1, y), c(x + 1, y + 1)));
+            }
+            dst[ly * side + lx] = v;
+            if (((gx & ~7u) << (m + 1)) < fbW && ((gy & ~7u) << (m + 1)) < fbH)  // the 8x8 block's region is in the frame
+                tex[offs.off[m] + texel_offset(gx, gy, rowShift - (int32_t)m)] = __float_as_uint(v);
+        }
+        __syncthreads();
     }
-    tex[dstOff + texel_offset(tx, ty, rowShift - (int32_t)m)] = __float_as_uint(v);
+}
+
+// The levels above k_hiz_local's (first = 4 .. last = root-3) in one block, out of shared memory:
+// the texels of level first-1 whose origin lies in the frame are read once (the others count as
+// FLT_MAX), then each level is computed from the previous one in shared memory and written out.
+// lvl[k] holds level first-1+k as a (fbW >> (first+k) rounded up) x (fbH >> ...) array.
+__host__ __device__ inline uint32_t hiz_extent(uint32_t n, uint32_t level) { return (n + (2u << level) - 1) >> (level + 1); }
+
+__global__ void __launch_bounds__(1024) k_hiz_tail(uint32_t fbW, uint32_t fbH, uint32_t* tex, HizOffsets offs,
+                                                   int32_t rowShift, uint32_t first, uint32_t last, uint32_t root) {
+    extern __shared__ float lvl[];
+    {  // level first-1 from the texture
+        const uint32_t m = first - 1, w = hiz_extent(fbW, m), h = hiz_extent(fbH, m);
+        const int32_t stride = rowShift - (int32_t)m;
+        for (uint32_t t = threadIdx.x; t < w * h; t += blockDim.x)
+            lvl[t] = __uint_as_float(tex[offs.off[m] + texel_offset(t % w, t / w, stride)]);
+    }
+    __syncthreads();
+    float* src = lvl;
+    for (uint32_t m = first; m <= last; m++) {
+        const uint32_t sw = hiz_extent(fbW, m - 1), sh = hiz_extent(fbH, m - 1);
+        const uint32_t dw = hiz_extent(fbW, m), dh = hiz_extent(fbH, m);
+        float* dst = src + sw * sh;
+        uint32_t regionsX = 1, regionsY = 1, blockTexels = 16;
+        if (m + 4 <= root) {
+            const uint32_t region = 1u << (m + 4);
+            regionsX = (fbW + region - 1) / region, regionsY = (fbH + region - 1) / region, blockTexels = 64;
+        }
+        const uint32_t bs = blockTexels == 64 ? 8 : 4, n = regionsX * regionsY * blockTexels;
+        for (uint32_t t = threadIdx.x; t < n; t += blockDim.x) {
+            const uint32_t blk = t / blockTexels, within = t - blk * blockTexels;
+            const uint32_t by = blk / regionsX, bx = blk - by * regionsX;
+            const uint32_t tx = bx * bs + within % bs, ty = by * bs + within / bs;
+            // children at mip m-1 cover 2^m pixels; one whose origin is outside the frame covers none
+            auto c = [&](uint32_t x, uint32_t y) -> float { return (x < sw && y < sh) ? src[y * sw + x] : FLT_MAX; };
+            const uint32_t x = tx * 2, y = ty * 2;
+            const float v = vmin(vmin(c(x, y), c(x, y + 1)), vmin(c(x + 1, y), c(x + 1, y + 1)));
+            tex[offs.off[m] + texel_offset(tx, ty, rowShift - (int32_t)m)] = __float_as_uint(v);
+            if (tx < dw && ty < dh) dst[ty * dw + tx] = v;
+        }
+        __syncthreads();
+        src = dst;
+    }
 }
 
 // =========================================================================== resolve
@@ -670,13 +725,22 @@ swr_status swr_downsample_depth(swr_framebuffer fb, swr_texture dest) {
         if (stride < 0 || mipOff(m) + 7 + (maxX << 3) + (maxY << stride) >= dest->words)
             return swr_internal_fail(SWR_EINVAL, "swr_downsample_depth: destination too small for this framebuffer");
     }
-    for (uint32_t m = 0; m + 3 <= root; m++) {
-        uint32_t regionsX, regionsY, blockTexels;
-        blocks(m, regionsX, regionsY, blockTexels);
-        const uint32_t n = regionsX * regionsY * blockTexels;
-        LaunchScope ls("k_hiz_level", st);
-        k_hiz_level<<<(n + 255) / 256, 256, 0, st>>>(depth, fb->width, fb->height, tex, mipOff(m), m ? mipOff(m - 1) : 0,
-                                                      (int32_t)dest->d.row_shift, m, regionsX, n, blockTexels);
+    HizOffsets offs = {};
+    for (uint32_t m = 0; m + 3 <= root && m < 16; m++) offs.off[m] = mipOff(m);
+    const uint32_t nLocal = std::min(4u, root - 3);  // levels with 8x8-texel blocks inside 128-pixel regions
+    {
+        LaunchScope ls("k_hiz_local", st);
+        const dim3 grid((fb->width + kHizRegion - 1) / kHizRegion, (fb->height + kHizRegion - 1) / kHizRegion);
+        k_hiz_local<<<grid, 256, 0, st>>>(depth, fb->width, fb->height, tex, offs, (int32_t)dest->d.row_shift, nLocal);
+    }
+    if (root - 3 >= nLocal) {
+        size_t smem = 0;  // levels nLocal-1 .. root-3, texels whose origin lies in the frame
+        for (uint32_t m = nLocal - 1; m <= root - 3; m++)
+            smem += (size_t)hiz_extent(fb->width, m) * hiz_extent(fb->height, m) * sizeof(float);
+        if (smem > 48 * 1024) cudaFuncSetAttribute(k_hiz_tail, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        LaunchScope ls("k_hiz_tail", st);
+        k_hiz_tail<<<1, 1024, smem, st>>>(fb->width, fb->height, tex, offs, (int32_t)dest->d.row_shift, nLocal, root - 3,
+                                           root);
     }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_downsample_depth");
