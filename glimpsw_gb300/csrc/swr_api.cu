@@ -289,8 +289,21 @@ swr_status swr_framebuffer_destroy(swr_framebuffer fb) {
     return SWR_OK;
 }
 
+}  // extern "C"
+
+swr_status swr_internal_finalize(swr_framebuffer fb) {
+    if (!fb->layers_stale) return SWR_OK;
+    launch_finalize(fb->keys, fb->layers, fb->layers + fb->layer_stride, fb->width * fb->height, t_stream);
+    SWR_CHECK_LAUNCH("finalize the vis-buffer layers");
+    fb->layers_stale = false;
+    return SWR_OK;
+}
+
+extern "C" {
+
 swr_status swr_framebuffer_clear(swr_framebuffer fb, uint32_t color, float depth) {
     if (!fb) return fail(SWR_EINVAL, "swr_framebuffer_clear: NULL framebuffer");
+    fb->layers_stale = false;  // every layer word is overwritten
     uint32_t d;
     memcpy(&d, &depth, 4);
     launch_clear(fb->layers, fb->layers + fb->layer_stride, fb->keys, fb->tileMin, fb->width * fb->height, color, d,
@@ -302,6 +315,8 @@ swr_status swr_framebuffer_clear(swr_framebuffer fb, uint32_t color, float depth
 
 swr_status swr_framebuffer_clear_layer(swr_framebuffer fb, uint32_t layer, uint32_t value) {
     if (!fb || layer >= fb->num_layers) return fail(SWR_EINVAL, "swr_framebuffer_clear_layer: bad framebuffer or layer");
+    swr_status st = swr_internal_finalize(fb);
+    if (st != SWR_OK) return st;
     launch_fill(fb->layers + (size_t)layer * fb->layer_stride, fb->width * fb->height, value, t_stream);
     SWR_CHECK_LAUNCH("swr_framebuffer_clear_layer");
     if (layer <= 1) fb->keys_valid = false;
@@ -311,6 +326,8 @@ swr_status swr_framebuffer_clear_layer(swr_framebuffer fb, uint32_t layer, uint3
 swr_status swr_framebuffer_get_pixels_device(swr_framebuffer fb, uint32_t layer, uint32_t* dest_device) {
     if (!fb || layer >= fb->num_layers || !dest_device)
         return fail(SWR_EINVAL, "swr_framebuffer_get_pixels_device: bad argument");
+    swr_status st = swr_internal_finalize(fb);
+    if (st != SWR_OK) return st;
     launch_detile(fb->layers + (size_t)layer * fb->layer_stride, dest_device, fb->width, fb->height, t_stream);
     SWR_CHECK_LAUNCH("swr_framebuffer_get_pixels_device");
     return SWR_OK;
@@ -319,6 +336,8 @@ swr_status swr_framebuffer_get_pixels_device(swr_framebuffer fb, uint32_t layer,
 swr_status swr_framebuffer_get_pixels(swr_framebuffer fb, uint32_t layer, uint32_t* dest, uint32_t stride) {
     if (!fb || layer >= fb->num_layers || !dest || stride < fb->width)
         return fail(SWR_EINVAL, "swr_framebuffer_get_pixels: bad argument");
+    swr_status st = swr_internal_finalize(fb);
+    if (st != SWR_OK) return st;
     uint32_t* tmp = nullptr;
     SWR_CUDA(cudaMallocAsync(&tmp, (size_t)fb->width * fb->height * 4, t_stream));
     launch_detile(fb->layers + (size_t)layer * fb->layer_stride, tmp, fb->width, fb->height, t_stream);
@@ -334,6 +353,8 @@ swr_status swr_framebuffer_get_pixels(swr_framebuffer fb, uint32_t layer, uint32
 
 swr_status swr_framebuffer_layer_data(swr_framebuffer fb, uint32_t layer, void** out_device_ptr) {
     if (!fb || layer >= fb->num_layers || !out_device_ptr) return fail(SWR_EINVAL, "swr_framebuffer_layer_data: bad argument");
+    swr_status st = swr_internal_finalize(fb);
+    if (st != SWR_OK) return st;
     *out_device_ptr = fb->layers + (size_t)layer * fb->layer_stride;
     return SWR_OK;
 }
@@ -451,6 +472,7 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
     if (st == SWR_OK && sc->hasAlpha && !overdraw) st = size_alpha_list(r, count);
     if (st != SWR_OK) return st;
     if (overdraw && !fb->counts) SWR_CUDA(cudaMalloc(&fb->counts, (size_t)fb->layer_stride * 8));
+    if (overdraw && (st = swr_internal_finalize(fb)) != SWR_OK) return st;  // its counters add to layer 0
     if (!fb->keys_valid) {
         launch_init_keys(fb->layers + fb->layer_stride, fb->keys, fb->tileMin, fb->width * fb->height, t_stream);
         SWR_CHECK_LAUNCH("swr_draw_meshlets: init keys");
@@ -494,10 +516,10 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
         launch_finalize_overdraw(fb->keys, fb->counts, fb->layers, fb->layers + fb->layer_stride, fb->width * fb->height,
                                  t_stream);
         fb->keys_valid = false;  // the keys hold the maximum depth of all samples, not vis-buffer keys
+        SWR_CHECK_LAUNCH("swr_draw_meshlets: finalize");
     } else {
-        launch_finalize(fb->keys, fb->layers, fb->layers + fb->layer_stride, fb->width * fb->height, t_stream);
+        fb->layers_stale = true;  // written by the next reader of the layers
     }
-    SWR_CHECK_LAUNCH("swr_draw_meshlets: finalize");
     return SWR_OK;
 }
 

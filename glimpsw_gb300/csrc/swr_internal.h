@@ -164,7 +164,11 @@ struct swr_framebuffer_t {
     uint32_t* tileMin;             // per 4x4 tile: lower bound of its keys' depth words
     unsigned long long* counts;    // OverdrawShader counters, allocated by its first draw
     bool keys_valid;               // keys and tileMin reflect the depth layer
+    bool layers_stale;             // the keys hold draws not yet written to layers 0 and 1
 };
+// Writes pending vis-buffer draws from the keys to layers 0 and 1 (k_finalize); every reader or
+// writer of the layers calls it first, so consecutive draws into one framebuffer finalize once.
+swr_status swr_internal_finalize(swr_framebuffer fb);
 
 struct swr_scene_t {
     uint8_t* meshlets;

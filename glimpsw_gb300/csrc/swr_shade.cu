@@ -606,6 +606,8 @@ swr_status build_resolve_args(swr_framebuffer fb, const swr_shading_context* ctx
     if (ctx->num_lights && !ctx->lights) return swr_internal_fail(SWR_EINVAL, (std::string(fn) + ": lights is NULL").c_str());
     if (ctx->skybox && ctx->skybox->format != SWR_FORMAT_R11G11B10F)
         return swr_internal_fail(SWR_EINVAL, (std::string(fn) + ": the skybox must be R11G11B10f").c_str());
+    swr_status fst = swr_internal_finalize(fb);  // pending draws reach layers 0 and 1 first
+    if (fst != SWR_OK) return fst;
     cudaStream_t st = swr_internal_stream();
     a = {};
     a.meshlets = ctx->scene->meshlets;
@@ -699,6 +701,8 @@ swr_status swr_cull_meshlets(swr_scene s, uint32_t first, uint32_t count, uint16
 swr_status swr_downsample_depth(swr_framebuffer fb, swr_texture dest) {
     if (!fb || !dest) return swr_internal_fail(SWR_EINVAL, "swr_downsample_depth: NULL argument");
     if (dest->format != SWR_FORMAT_R32F) return swr_internal_fail(SWR_EINVAL, "swr_downsample_depth: destination must be R32f");
+    swr_status fst = swr_internal_finalize(fb);
+    if (fst != SWR_OK) return fst;
     const uint32_t root = 32 - __builtin_clz(std::max(fb->width, fb->height));
     if (root < 4) return swr_internal_fail(SWR_EINVAL, "swr_downsample_depth: framebuffer smaller than 16 pixels");
     cudaStream_t st = swr_internal_stream();
