@@ -131,6 +131,7 @@ swr_status upload_views(swr_batch b, const swr_view_desc* views) {
         if (!b->rast->enable_binning && !b->rast->enable_guardband) v.bx = v.by = 1.0f;
         v.meshletOffset = b->first;
         v.count = b->count;
+        v.orderStride = order_stride(b->count);
         v.keys = fb->keys;
         v.tileMin = fb->tileMin;
         v.cullBitmap = b->frustumCull ? b->dBitmaps + (size_t)i * words : nullptr;
@@ -230,7 +231,8 @@ swr_status swr_batch_create(swr_rasterizer r, swr_scene s, uint32_t first, uint3
     if (num_views > 4096) return swr_internal_fail(SWR_EINVAL, "swr_batch_create: at most 4096 views");
     for (uint32_t i = 0; i < num_views; i++)
         if (!views[i].fb) return swr_internal_fail(SWR_EINVAL, "swr_batch_create: view without framebuffer");
-    if ((uint64_t)count * num_views >= (1ull << 32)) return swr_internal_fail(SWR_EINVAL, "swr_batch_create: too many work items");
+    const uint64_t padded = ((uint64_t)count + kBatchGroup - 1) / kBatchGroup * kBatchGroup;  // a view's work positions
+    if (padded * num_views >= (1ull << 32)) return swr_internal_fail(SWR_EINVAL, "swr_batch_create: too many work items");
     swr_batch b = new (std::nothrow) swr_batch_t();
     if (!b) return swr_internal_fail(SWR_ENOMEM, "swr_batch_create: host allocation failed");
     b->rast = r, b->scene = s, b->first = first, b->count = count, b->numViews = num_views, b->frustumCull = frustum_cull != 0;
@@ -242,7 +244,7 @@ swr_status swr_batch_create(swr_rasterizer r, swr_scene s, uint32_t first, uint3
     }
     const uint32_t words = (count + 15) / 16;
     std::vector<uint32_t> start(num_views + 1);
-    for (uint32_t i = 0; i <= num_views; i++) start[i] = i * count;
+    for (uint32_t i = 0; i <= num_views; i++) start[i] = i * (uint32_t)padded;
     cudaError_t e = cudaMalloc(&b->dViews, num_views * sizeof(ViewParams));
     if (e == cudaSuccess) e = cudaMalloc(&b->dBatch, num_views * sizeof(BatchView));
     if (e == cudaSuccess) e = cudaMalloc(&b->dViewStart, (num_views + 1) * sizeof(uint32_t));

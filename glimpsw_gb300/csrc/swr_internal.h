@@ -92,7 +92,8 @@ struct ViewParams {
     unsigned long long* keys;
     const uint16_t* cullBitmap;
     uint32_t* tileMin;      // per 4x4 tile: lower bound of its keys' depth words (nullptr: no tile culling)
-    uint32_t pad[2];
+    uint32_t orderStride;   // draw order: position p draws meshlet (p * orderStride) mod count (order_stride)
+    uint32_t pad;
 };
 static_assert(sizeof(ViewParams) == 128, "ViewParams");
 
@@ -123,7 +124,20 @@ struct DrawArgs {
     // OverdrawShader draws (single view): per-pixel counters (covered << 32 | other samples of
     // covered tiles), keys hold the maximum depth; nullptr for vis-buffer draws
     unsigned long long* counts;
+    // single view: order_stride(count), set by launch_draw
+    uint32_t orderStride;
 };
+
+// The mesh stage draws a view's meshlets in the order p -> (p * stride) mod count: a Weyl sequence
+// with stride near count / golden ratio (coprime to count), so neighbouring positions, fetched
+// together or by warps running at the same time, hold meshlets far apart in the record order. In a
+// spatially coherent order (meshlets built from a mesh, a grid) a fetch of 32 positions can
+// otherwise be 32 visible neighbours close to the camera, all for one warp, and concurrent warps
+// contend for the same pixels' keys. Keys are order-independent, so the image is the same for
+// every order. Work is fetched kDrawGroup positions at a time in single-view draws, kBatchGroup in
+// batches (whose views' position ranges are padded to multiples of it).
+constexpr uint32_t kDrawGroup = 4, kBatchGroup = 32;
+uint32_t order_stride(uint32_t count);
 
 void launch_draw(const DrawArgs& a, cudaStream_t st, int numSMs);
 void launch_init_keys(const uint32_t* depthLayer, unsigned long long* keys, uint32_t* tileMin, uint32_t n, cudaStream_t st);

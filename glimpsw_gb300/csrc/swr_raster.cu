@@ -24,6 +24,7 @@
 // the triangle cannot win anywhere is skipped. The vis-buffer is unchanged (only fragments that
 // would fail the depth test are skipped), while the dense scenes' overdraw mostly disappears.
 #include <cfloat>
+#include <numeric>
 #include <type_traits>
 
 #include "swr_device.cuh"
@@ -98,8 +99,9 @@ __device__ __forceinline__ int32_t compute_edge(int32_t a, int32_t x, int32_t b,
 
 // TriangleEdgeVars::Setup (Rasterizer.cpp:296-329), depth terms (the opaque vis-buffer shader
 // does not read the perspective-correct barycentrics; alpha_ext adds them from *rcpAreaOut).
-__device__ __forceinline__ void edge_setup(const Setup& t, int halfW, int halfH, uint32_t bbMin, uint32_t bbMax,
-                                           uint32_t rank, TriRec& r, float* rcpAreaOut = nullptr) {
+// Returns the fixed-point determinant (> 0, or 0 for a triangle degenerate in fixed point).
+__device__ __forceinline__ int32_t edge_setup(const Setup& t, int halfW, int halfH, uint32_t bbMin, uint32_t bbMax,
+                                              uint32_t rank, TriRec& r, float* rcpAreaOut = nullptr) {
     int32_t x0 = lo16(t.Pos0), y0 = hi16(t.Pos0);
     int32_t x1 = lo16(t.Pos1), y1 = hi16(t.Pos1);
     int32_t x2 = lo16(t.Pos2), y2 = hi16(t.Pos2);
@@ -125,7 +127,9 @@ __device__ __forceinline__ void edge_setup(const Setup& t, int halfW, int halfH,
     r.lowword = 0xFFFFFFFEu - rank;
     r.pad = 0;
     if (rcpAreaOut) *rcpAreaOut = rcpArea;
+    return det;
 }
+
 
 // ------------------------------------------------------------------ fragments
 // DrawTriangle inner loop (Rasterizer.h:287-323) + FS_EncodeSurfaceId<false> (Shading.cpp:309-331)
@@ -141,6 +145,43 @@ __device__ __forceinline__ void shade_fragment(const TriRec& r, uint32_t px, uin
     unsigned long long key = ((unsigned long long)float_order(depth) << 32) | r.lowword;
     unsigned long long* p = keys + pixel_offset(px, py, width);
     if (key > *(volatile unsigned long long*)p) atomicMax(p, key);
+}
+
+// Tiny triangles, drawn by their own lane. A sample passes the edge tests only inside the closed
+// fixed-point triangle (the tests are exact: floor(F / 16) >= 0 iff F >= 0, and the top-left
+// biases only remove boundary samples), so its pixel p satisfies 16 (p - half) + 8 in
+// [min, max] of the vertices, i.e. p in [(min + 7) >> 4, (max - 8) >> 4] + half, computed per
+// 16-bit half (the render box's single 32-bit add can carry from x into y). The tile walk visits
+// [bbMin, bbMax). The lane evaluates the pixels of both ranges' intersection: exactly the walk's
+// covered pixels. A triangle degenerate in fixed point (det 0) can pass samples on its whole line
+// and keeps the walk.
+constexpr uint32_t kTinyPixels = 2;
+struct TinyBox { uint32_t x0, y0, x1, y1; };  // inclusive pixel range
+__device__ __forceinline__ bool tiny_box(const Setup& t, int halfW, int halfH, uint32_t bbMin, uint32_t bbMax,
+                                         TinyBox& b) {
+    const uint32_t vp = (uint32_t)halfW | ((uint32_t)halfH << 16);
+    const uint32_t lo = srai16_4(__vadd2(__vmins2(__vmins2(t.Pos0, t.Pos1), t.Pos2), 0x00070007u));
+    const uint32_t hi = srai16_4(__vsub2(__vmaxs2(__vmaxs2(t.Pos0, t.Pos1), t.Pos2), 0x00080008u));
+    const uint32_t x = __vmaxs2(__vadd2(lo, vp), bbMin);
+    const uint32_t y = __vmins2(__vadd2(hi, vp), bbMax - 0x00010001u);
+    b.x0 = x & 0xFFFF, b.y0 = x >> 16, b.x1 = y & 0xFFFF, b.y1 = y >> 16;
+    const int w = (int)(int16_t)(y & 0xFFFF) - (int)(int16_t)(x & 0xFFFF) + 1;
+    const int h = (int)(int16_t)(y >> 16) - (int)(int16_t)(x >> 16) + 1;
+    return w <= 0 || h <= 0 || w * h <= (int)kTinyPixels;
+}
+
+__device__ __forceinline__ void shade_tiny(const TriRec& r, const TinyBox& b, unsigned long long* keys, uint32_t width) {
+    for (int y = (int16_t)b.y0; y <= (int16_t)b.y1; y++)
+        for (int x = (int16_t)b.x0; x <= (int16_t)b.x1; x++) {
+            const uint32_t px = (uint32_t)x, py = (uint32_t)y;
+            const int32_t e0 = (int32_t)((uint32_t)r.E0 + (uint32_t)r.A12 * px + (uint32_t)r.B12 * py);
+            const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
+            const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
+            if ((e0 | e1 | e2) < 0) continue;
+            const float depth = ffma(__int2float_rn(e1), r.Z10, ffma(__int2float_rn(e2), r.Z20, r.Z0));
+            if (depth != depth) continue;
+            atomicMax(keys + pixel_offset(px, py, width), ((unsigned long long)float_order(depth) << 32) | r.lowword);
+        }
 }
 
 // Upper bound of the depth tile_pixel_key computes for any sample of the 4x4 tile at (px, py).
@@ -737,6 +778,21 @@ struct WarpSmemAlpha : WarpSmem {
 // work items of alpha-tested meshlets to alphaList; the alpha pass draws those with
 // FS_EncodeSurfaceId<true>. The order of the passes does not change the keys. OverdrawShader draws
 // take one pass over every meshlet.
+// View of batched work position p: the largest v with viewStart[v] <= p.
+__device__ __forceinline__ uint32_t view_of(const uint32_t* viewStart, uint32_t numViews, uint32_t p) {
+    uint32_t lo = 0, hi = numViews - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (viewStart[mid] <= p) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Meshlet drawn at position p of a view of count meshlets (order_stride).
+__device__ __forceinline__ uint32_t draw_order(uint32_t p, uint32_t count, uint32_t stride) {
+    return (uint32_t)(((unsigned long long)p * stride) % count);
+}
+
 enum : int { kPassOpaque = 0, kPassAlpha = 1, kPassOverdraw = 2 };
 template <int kPass>
 __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
@@ -751,6 +807,9 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     const ViewParams& vp = S.view;
     const uint32_t chunk = a.chunkTiles ? a.chunkTiles : kChunkTiles;
     const bool multi = a.views != nullptr;
+    // Work positions. Position p of a view draws its meshlet draw_order(p) (order_stride); a batched
+    // draw concatenates its views' positions, padded to multiples of kBatchGroup (viewStart); the
+    // alpha pass walks its list of work items.
     const uint32_t totalItems = kAlpha ? (uint32_t)a.s.control[9] : (multi ? a.viewStart[a.numViews] : a.count);
     unsigned long long* const cursor = &a.s.control[kAlpha ? 10 : 0];
     unsigned long long* const idleWarps = &a.s.control[kAlpha ? 12 : 11];  // warps past their last item
@@ -771,64 +830,76 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     unsigned long long nProcessed = 0, nRaster = 0, nClipped = 0;
     if (!kAlpha && blockIdx.x == 0 && threadIdx.x == 0) a.s.control[8] = 0;  // the chunk stage's cursor (runs later)
 
-    // Work items are fetched kFetch at a time: one contended atomic per kFetch items. Batched
-    // draws, most of whose (view, meshlet) items are culled, fetch 32 at a time and test the 32
-    // cull bits at once (one item per lane), then walk the visible ones.
-    constexpr uint32_t kFetch = 4;
-    uint32_t fetchBase = 0, fetchLeft = 0;
-    unsigned fetchMask = 0;  // batched draws: visible items of the current fetch (bit j: item fetchBase + j)
+    // Work items are fetched a group at a time: one contended atomic per group. Batched draws,
+    // most of whose (view, meshlet) items are culled, fetch groups of 32 and test the 32 cull bits
+    // at once (one item per lane), then walk the visible ones. A work item is viewStart[view] + m
+    // (m alone in single-view draws), as the alpha list records it.
+    uint32_t fetchPos = 0, fetchLeft = 0;  // single view and alpha pass: next position, positions left
+    uint32_t laneMeshlet = 0;              // batched draws: the meshlet of this lane's position in the group
+    uint32_t fetchView = 0;
+    unsigned fetchMask = 0;                // batched draws: lanes whose meshlet is visible
     while (true) {
-        uint32_t idx;
-        if (multi && !kAlpha) {
-            if (fetchMask == 0) {
-                uint32_t b = 0;
-                if (lane == 0) b = (uint32_t)atomicAdd(cursor, 32ull);
-                fetchBase = __shfl_sync(0xFFFFFFFFu, b, 0);
-                if (fetchBase >= totalItems) break;
-                const uint32_t it = fetchBase + lane;
-                bool vis = false;
-                if (it < totalItems) {
-                    uint32_t lo = 0, hi = a.numViews - 1;  // largest view with viewStart <= it
-                    while (lo < hi) {
-                        uint32_t mid = (lo + hi + 1) >> 1;
-                        if (a.viewStart[mid] <= it) lo = mid; else hi = mid - 1;
-                    }
-                    const uint32_t mm = it - a.viewStart[lo];
-                    const uint16_t* bm = a.views[lo].cullBitmap;
-                    vis = bm == nullptr || ((bm[mm >> 4] >> (mm & 15)) & 1);
-                }
-                fetchMask = __ballot_sync(0xFFFFFFFFu, vis);
-                if (fetchMask == 0) continue;
-            }
-            idx = fetchBase + (__ffs(fetchMask) - 1);
-            fetchMask &= fetchMask - 1;
-        } else {
+        uint32_t m, view = 0, item;
+        if constexpr (kAlpha) {
             if (fetchLeft == 0) {
                 uint32_t b = 0;
-                if (lane == 0) b = (uint32_t)atomicAdd(cursor, (unsigned long long)kFetch);
-                fetchBase = __shfl_sync(0xFFFFFFFFu, b, 0);
-                fetchLeft = kFetch;
+                if (lane == 0) b = (uint32_t)atomicAdd(cursor, (unsigned long long)kDrawGroup);
+                fetchPos = __shfl_sync(0xFFFFFFFFu, b, 0);
+                fetchLeft = kDrawGroup;
             }
-            idx = fetchBase++;
+            const uint32_t idx = fetchPos++;
             fetchLeft--;
             if (idx >= totalItems) break;
+            item = a.s.alphaList[idx];
+            m = item;
+            if (multi) {
+                view = view_of(a.viewStart, a.numViews, item);
+                m = item - a.viewStart[view];
+            }
+        } else {
+            if (multi) {
+                if (fetchMask == 0) {
+                    uint32_t b = 0;
+                    if (lane == 0) b = (uint32_t)atomicAdd(cursor, (unsigned long long)kBatchGroup);
+                    const uint32_t base = __shfl_sync(0xFFFFFFFFu, b, 0);
+                    if (base >= totalItems) break;
+                    // groups interleave the views: group G is group G / numViews of view G % numViews
+                    const uint32_t G = base / kBatchGroup;
+                    fetchView = G % a.numViews;
+                    const ViewParams& fv = a.views[fetchView];
+                    const uint32_t q = (G / a.numViews) * kBatchGroup + lane;
+                    bool vis = false;
+                    if (q < fv.count) {
+                        laneMeshlet = draw_order(q, fv.count, fv.orderStride);
+                        const uint16_t* bm = fv.cullBitmap;
+                        vis = bm == nullptr || ((bm[laneMeshlet >> 4] >> (laneMeshlet & 15)) & 1);
+                    }
+                    fetchMask = __ballot_sync(0xFFFFFFFFu, vis);
+                    if (fetchMask == 0) continue;
+                }
+                view = fetchView;
+                m = __shfl_sync(0xFFFFFFFFu, laneMeshlet, __ffs(fetchMask) - 1);
+                fetchMask &= fetchMask - 1;
+                item = a.viewStart[view] + m;
+            } else {
+                if (fetchLeft == 0) {
+                    uint32_t b = 0;
+                    if (lane == 0) b = (uint32_t)atomicAdd(cursor, (unsigned long long)kDrawGroup);
+                    fetchPos = __shfl_sync(0xFFFFFFFFu, b, 0);
+                    fetchLeft = kDrawGroup;
+                }
+                const uint32_t p = fetchPos++;
+                fetchLeft--;
+                if (p >= totalItems) break;
+                m = draw_order(p, a.count, a.orderStride);
+                item = m;
+            }
         }
-        const uint32_t item = kAlpha ? a.s.alphaList[idx] : idx;
-        uint32_t m = item, view = 0;
-        if (multi) {
-            uint32_t lo = 0, hi = a.numViews - 1;  // largest view with viewStart <= item
-            while (lo < hi) {
-                uint32_t mid = (lo + hi + 1) >> 1;
-                if (a.viewStart[mid] <= item) lo = mid; else hi = mid - 1;
-            }
-            view = lo;
-            m = item - a.viewStart[lo];
-            if (view != curView) {
-                __syncwarp();
-                ((uint32_t*)&S.view)[lane] = ((const uint32_t*)&a.views[view])[lane];
-                __syncwarp();
-                curView = view;
-            }
+        if (multi && view != curView) {
+            __syncwarp();
+            ((uint32_t*)&S.view)[lane] = ((const uint32_t*)&a.views[view])[lane];
+            __syncwarp();
+            curView = view;
         }
         if (vp.cullBitmap != nullptr && !((vp.cullBitmap[m >> 4] >> (m & 15)) & 1)) continue;  // Shading.cpp:282-289
 
@@ -890,7 +961,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                 if (tri_setup(v0, v1, v2, vp.halfW, vp.halfH, cullMode, t, bbMin, bbMax)) {
                     TriRec r;
                     float rcpArea;
-                    edge_setup(t, vp.halfW, vp.halfH, bbMin, bbMax, make_rank(g, p, 0, 0), r, &rcpArea);
+                    const int32_t det = edge_setup(t, vp.halfW, vp.halfH, bbMin, bbMax, make_rank(g, p, 0, 0), r, &rcpArea);
                     nRaster++;
                     AlphaExt x;
                     if constexpr (kAlpha)
@@ -898,7 +969,10 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                                       texcoord_word(mp, idxBytes[256 + p]), matId);
                     const int tilesX = ((bbMax & 0xFFFF) - (bbMin & 0xFFFF)) >> 2;
                     const int tilesY = ((bbMax >> 16) - (bbMin >> 16)) >> 2;
-                    if (tilesX * tilesY <= kSmallTiles) {
+                    TinyBox tb;
+                    if (kPass == kPassOpaque && det > 0 && tiny_box(t, vp.halfW, vp.halfH, bbMin, bbMax, tb)) {
+                        shade_tiny(r, tb, vp.keys, vp.width);
+                    } else if (tilesX * tilesY <= kSmallTiles) {
                         // tile index -> row by a multiply-shift (exact for tile < 16, tilesX <= 16)
                         r.pad = (uint32_t)tilesX | ((uint32_t)((256 + tilesX - 1) / tilesX) << 8);
                         tris[lane] = r;
@@ -1193,7 +1267,16 @@ static int grid_for(uint32_t n, int perThread, int block) {
     return (int)max(1ll, min(g, 152ll * 16));
 }
 
-void launch_draw(const DrawArgs& a, cudaStream_t st, int numSMs) {
+uint32_t order_stride(uint32_t count) {
+    if (count <= 2) return 1;
+    uint32_t s = (uint32_t)((double)count * 0.6180339887498949) | 1u;
+    while (std::gcd(s, count) != 1u) s += 2;
+    return s % count;
+}
+
+void launch_draw(const DrawArgs& args, cudaStream_t st, int numSMs) {
+    DrawArgs a = args;
+    if (!a.views) a.orderStride = order_stride(a.count);
     const uint32_t warps = a.warpsPerBlock ? a.warpsPerBlock : kWarpsPerBlock;
     const size_t smem = warps * sizeof(WarpSmem), smemAlpha = warps * sizeof(WarpSmemAlpha);
     static size_t s_smemSet = 0, s_smemSetAlpha = 0;
