@@ -292,10 +292,11 @@ swr_status swr_framebuffer_destroy(swr_framebuffer fb) {
 }  // extern "C"
 
 swr_status swr_internal_finalize(swr_framebuffer fb) {
-    if (!fb->layers_stale) return SWR_OK;
-    launch_finalize(fb->keys, fb->layers, fb->layers + fb->layer_stride, fb->width * fb->height, t_stream);
+    if (fb->layers_stale == kStaleNone) return SWR_OK;
+    launch_finalize(fb->keys, fb->layers_stale == kStaleDepth ? nullptr : fb->layers, fb->layers + fb->layer_stride,
+                    fb->width * fb->height, t_stream);
     SWR_CHECK_LAUNCH("finalize the vis-buffer layers");
-    fb->layers_stale = false;
+    fb->layers_stale = kStaleNone;
     return SWR_OK;
 }
 
@@ -303,7 +304,7 @@ extern "C" {
 
 swr_status swr_framebuffer_clear(swr_framebuffer fb, uint32_t color, float depth) {
     if (!fb) return fail(SWR_EINVAL, "swr_framebuffer_clear: NULL framebuffer");
-    fb->layers_stale = false;  // every layer word is overwritten
+    fb->layers_stale = kStaleNone;  // every layer word is overwritten
     uint32_t d;
     memcpy(&d, &depth, 4);
     launch_clear(fb->layers, fb->layers + fb->layer_stride, fb->keys, fb->tileMin, fb->width * fb->height, color, d,
@@ -361,6 +362,8 @@ swr_status swr_framebuffer_layer_data(swr_framebuffer fb, uint32_t layer, void**
 
 swr_status swr_framebuffer_invalidate(swr_framebuffer fb) {
     if (!fb) return fail(SWR_EINVAL, "swr_framebuffer_invalidate: NULL framebuffer");
+    swr_status st = swr_internal_finalize(fb);
+    if (st != SWR_OK) return st;
     fb->keys_valid = false;
     return SWR_OK;
 }
@@ -518,7 +521,7 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
         fb->keys_valid = false;  // the keys hold the maximum depth of all samples, not vis-buffer keys
         SWR_CHECK_LAUNCH("swr_draw_meshlets: finalize");
     } else {
-        fb->layers_stale = true;  // written by the next reader of the layers
+        fb->layers_stale = kStaleAll;  // written by the next reader of the layers
     }
     return SWR_OK;
 }

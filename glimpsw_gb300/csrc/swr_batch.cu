@@ -1,6 +1,8 @@
 // Batched multi-view rendering: many views of different resolutions and meshlet ranges drawn by one
-// persistent launch of the mesh stage, the whole frame (clear, frustum culling, draw, chunk raster,
-// finalize) captured once into a CUDA graph and replayed. The reference renders one view per
+// persistent launch of the mesh stage, the whole frame (clear, frustum culling, draw, chunk raster)
+// captured once into a CUDA graph and replayed; each view's layers are written from its keys by
+// their next reader, as after a single draw (depth-only views: the depth layer alone). The
+// reference renders one view per
 // DrawMeshlets call (Main.cpp:216-245); each view of a batch gives exactly the vis-buffer of that
 // call sequence (clear, CullMeshlets without depth map, DrawMeshlets), since keys stay per view.
 #include <cuda_runtime.h>
@@ -17,14 +19,13 @@
 namespace swr {
 namespace {
 
-struct BatchView {              // device table for the batched clear / cull / finalize kernels
+struct BatchView {              // device table for the batched clear and cull kernels
     float planes[5][4];         // CullMeshlets frustum planes 0..4 (Shading.cpp:806)
     uint32_t* layer0;
     uint32_t* layer1;
     unsigned long long* keys;
     uint16_t* bitmap;
     uint32_t pixels;            // width * height
-    uint32_t depthOnly;
     uint32_t* tileMin;          // per 4x4 tile depth bound
 };
 
@@ -64,18 +65,6 @@ __global__ void k_cull_views(const BatchView* __restrict__ views, const uint8_t*
     }
 }
 
-// Keys to the reference's layers for every view; depth-only views keep only the depth layer.
-__global__ void k_finalize_views(const BatchView* __restrict__ views) {
-    const BatchView& v = views[blockIdx.y];
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < v.pixels; i += gridDim.x * blockDim.x) {
-        const unsigned long long k = v.keys[i];
-        const uint32_t low = (uint32_t)k;
-        if (low == kKeyEmptyLow) continue;
-        v.layer1[i] = __float_as_uint(float_unorder((uint32_t)(k >> 32)));
-        if (!v.depthOnly) v.layer0[i] = rank_surface_id(0xFFFFFFFEu - low);
-    }
-}
-
 }  // namespace
 }  // namespace swr
 
@@ -88,6 +77,7 @@ struct swr_batch_t {
     int frustumCull;
     uint32_t maxPixels;
     std::vector<swr_framebuffer> fbs;
+    std::vector<uint8_t> depthOnly;  // per view: only the depth layer is written
     ViewParams* dViews = nullptr;
     BatchView* dBatch = nullptr;
     uint32_t* dViewStart = nullptr;
@@ -144,7 +134,7 @@ swr_status upload_views(swr_batch b, const swr_view_desc* views) {
         w.tileMin = fb->tileMin;
         w.bitmap = b->dBitmaps + (size_t)i * words;
         w.pixels = fb->width * fb->height;
-        w.depthOnly = d.depth_only != 0;
+        b->depthOnly[i] = d.depth_only != 0;
     }
     cudaStream_t st = swr_internal_stream();
     cudaError_t e = cudaMemcpyAsync(b->dViews, vp.data(), vp.size() * sizeof(ViewParams), cudaMemcpyHostToDevice, st);
@@ -193,7 +183,6 @@ swr_status capture(swr_batch b) {
         a.chunkTiles = b->chunkTiles;
         a.warpsPerBlock = b->warpsPerBlock;
         launch_draw(a, cs, sm_count());
-        k_finalize_views<<<dim3(blocksX, nv), 256, 0, cs>>>(b->dBatch);
         e = cudaStreamEndCapture(cs, &b->graph);
     }
     swr_internal_set_profiling(prof);
@@ -239,6 +228,7 @@ swr_status swr_batch_create(swr_rasterizer r, swr_scene s, uint32_t first, uint3
     uint64_t totalTris = 0;
     for (uint32_t i = 0; i < num_views; i++) {
         b->fbs.push_back(views[i].fb);
+        b->depthOnly.push_back(views[i].depth_only != 0);
         b->maxPixels = std::max(b->maxPixels, views[i].fb->width * views[i].fb->height);
         totalTris += (uint64_t)count * 32;
     }
@@ -302,7 +292,10 @@ swr_status swr_batch_render(swr_batch b) {
     }
     if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_batch_render");
     if (b->kernelNodes > 1) swr_internal_count_launches(b->kernelNodes - 1);
-    for (swr_framebuffer fb : b->fbs) fb->keys_valid = true;
+    for (uint32_t i = 0; i < b->numViews; i++) {  // the layers are written by their next reader
+        b->fbs[i]->keys_valid = true;
+        b->fbs[i]->layers_stale = b->depthOnly[i] ? kStaleDepth : kStaleAll;
+    }
     return SWR_OK;
 }
 

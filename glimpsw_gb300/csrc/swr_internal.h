@@ -178,8 +178,9 @@ struct swr_framebuffer_t {
     uint32_t* tileMin;             // per 4x4 tile: lower bound of its keys' depth words
     unsigned long long* counts;    // OverdrawShader counters, allocated by its first draw
     bool keys_valid;               // keys and tileMin reflect the depth layer
-    bool layers_stale;             // the keys hold draws not yet written to layers 0 and 1
+    uint8_t layers_stale;          // the keys hold draws not yet written to the layers: kStale*
 };
+enum : uint8_t { kStaleNone = 0, kStaleDepth = 1, kStaleAll = 2 };  // kStaleDepth: depth-only views of a batch
 // Writes pending vis-buffer draws from the keys to layers 0 and 1 (k_finalize); every reader or
 // writer of the layers calls it first, so consecutive draws into one framebuffer finalize once.
 swr_status swr_internal_finalize(swr_framebuffer fb);

@@ -1233,7 +1233,7 @@ __global__ void k_finalize(const unsigned long long* __restrict__ keys, uint32_t
             const uint32_t low = (uint32_t)kk[j];
             if (low == kKeyEmptyLow) continue;
             l1[i + j] = __float_as_uint(float_unorder((uint32_t)(kk[j] >> 32)));
-            l0[i + j] = rank_surface_id(0xFFFFFFFEu - low);
+            if (l0) l0[i + j] = rank_surface_id(0xFFFFFFFEu - low);  // l0 null: depth only
         }
     }
 }

@@ -200,8 +200,10 @@ swr_status swr_framebuffer_clear_layer(swr_framebuffer fb, uint32_t layer, uint3
 swr_status swr_framebuffer_get_pixels(swr_framebuffer fb, uint32_t layer, uint32_t* dest, uint32_t stride);
 /* Device copy of a de-tiled layer (row-major, width*height words); no host synchronisation. */
 swr_status swr_framebuffer_get_pixels_device(swr_framebuffer fb, uint32_t layer, uint32_t* dest_device);
-/* Raw tiled layer storage (GetLayerData, Rasterizer.h:24-33), device pointer. Writing through it
- * must be followed by swr_framebuffer_invalidate. */
+/* Raw tiled layer storage (GetLayerData, Rasterizer.h:24-33), device pointer. Draws write layers 0
+ * and 1 when they are next read, so the storage holds the draws made before this call: call it again
+ * after later draws before reading or writing through the pointer. Writing through it must be
+ * followed by swr_framebuffer_invalidate (which first writes any draws still pending). */
 swr_status swr_framebuffer_layer_data(swr_framebuffer fb, uint32_t layer, void** out_device_ptr);
 swr_status swr_framebuffer_invalidate(swr_framebuffer fb);
 swr_status swr_framebuffer_size(swr_framebuffer fb, uint32_t* width, uint32_t* height, uint32_t* layer_stride,

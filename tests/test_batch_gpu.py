@@ -87,5 +87,17 @@ def test_batch_counts_kernels_and_autotunes(setup, tmp_path, monkeypatch):
     assert best2 == best
     n0 = api.launch_count()
     batch.render()
-    assert api.launch_count() - n0 >= 5  # clear, cull, mesh stage, chunk stage, finalize
+    assert api.launch_count() - n0 >= 4  # clear, cull, mesh stage, chunk stage
     check_all(api, sc, scene, rast, fbs)
+
+
+def test_depth_only_views_keep_layer0(setup):
+    """Depth-only views write only the depth layer when their layers are next read; layer 0 keeps
+    the clear colour while the depth layer matches a full per-view draw."""
+    from glimpsw_gb300 import api
+    sc, scene, rast, fbs, views, batch = setup
+    batch.render()
+    for fb, v in zip(fbs, sc.views):
+        if v.depth_only:
+            assert np.all(fb.get_pixels(0) == 0xFF000000)
+            assert np.array_equal(fb.get_pixels(1), per_view(api, sc, scene, rast, v).get_pixels(1))
