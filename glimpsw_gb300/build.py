@@ -37,7 +37,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
     deps = srcs + [os.path.join(CSRC, h) for h in HEADERS]
     inc = os.path.join(HERE, "..", "include")
-    deps += [os.path.join(inc, "swr_gb300.h"), os.path.join(inc, "swr", "hostmath.h")]
+    deps += [os.path.join(inc, "swr_gb300.h"), os.path.join(inc, "swr", "hostmath.h"), os.path.join(inc, "swr", "approx14.h")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
     os.makedirs(BUILD_DIR, exist_ok=True)

@@ -27,6 +27,7 @@
 #include <numeric>
 #include <type_traits>
 
+#include "../../include/swr/approx14.h"
 #include "swr_device.cuh"
 #include "swr_internal.h"
 #include "swr_sample.cuh"
@@ -247,7 +248,7 @@ __device__ __forceinline__ bool enqueue_big(const TriRec& r, const DrawArgs& a, 
 
 // ------------------------------------------------------------------ alpha test
 // FS_EncodeSurfaceId<true> (Shading.cpp:309-331): after the depth test, the fragment's
-// perspective-correct barycentrics (Rasterizer.h:300-317, rcp14 modelled as 1/w) interpolate the
+// perspective-correct barycentrics (Rasterizer.h:300-317, rcp14 reproduced exactly) interpolate the
 // vertices' texcoords (FragmentVars::Interpolate = BaryLerp, Rasterizer.h:101-104), the material's
 // texture is sampled at the implicit LOD of the 4x4 tile (SampleImplicitLod, Texture.h:403-410,
 // with the 2x2 finite differences texutil::dFdx/dFdy, Texture.h:258-275) and the fragment survives
@@ -281,7 +282,7 @@ struct TexCoord { float u, v; };
 __device__ __forceinline__ TexCoord alpha_texcoord(const AlphaExt& x, float u, float v) {
     const float pw0 = ffma(fadd(u, v), -x.W0S, x.W0);
     const float w = ffma(u, x.W1S, ffma(v, x.W2S, pw0));
-    float rcpW = __frcp_rn(w);  // 1/w (rcp14 modelled as IEEE)
+    float rcpW = swr_rcp14(w);  // simd::approx_rcp (VRCP14PS, bit-exact)
     rcpW = fmul(rcpW, ffma(-w, rcpW, 2.0f));  // Newton-Raphson step
     float bu = fmul(u, fmul(x.W1S, rcpW)), bv = fmul(v, fmul(x.W2S, rcpW));
     if (x.material & kTriAlpha) {  // clipped: barycentrics of the source triangle

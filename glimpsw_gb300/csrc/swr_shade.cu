@@ -3,8 +3,9 @@
 //
 // The translation unit is compiled with -fmad=false, so every float expression below is evaluated
 // in source order with one rounding per operation, as the reference's C++ is written; fmaf()
-// stands for the reference's explicit simd::fma. rcp14/rsqrt14 are modelled as 1/x and
-// 1/sqrtf(x) (IEEE), matching the oracle's portable model.
+// stands for the reference's explicit simd::fma. simd::approx_rcp / approx_rsqrt / approx_sqrt
+// (the AVX-512 instructions VRCP14PS and VRSQRT14PS) are reproduced bit for bit by the integer
+// segment tables of include/swr/approx14.h.
 //
 // Resolve layout: a half-warp shades one 4x4 tile (lane = pixel), so the reference's tile-wide
 // decisions (`any(mipLevel > 0)` filter choice, normal-map enable, light skipping, sky branch)
@@ -18,6 +19,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/swr/approx14.h"
 #include "../../include/swr/hostmath.h"
 #include "swr_device.cuh"
 #include "swr_internal.h"
@@ -29,9 +31,9 @@ namespace {
 
 struct F3 { float x, y, z; };
 
-__device__ __forceinline__ float approx_rcp(float x) { return 1.0f / x; }
-__device__ __forceinline__ float approx_rsqrt(float x) { return 1.0f / sqrtf(x); }
-__device__ __forceinline__ float approx_sqrt(float x) { return approx_rsqrt(x) * x; }
+__device__ __forceinline__ float approx_rcp(float x) { return swr_rcp14(x); }
+__device__ __forceinline__ float approx_rsqrt(float x) { return swr_rsqrt14(x); }
+__device__ __forceinline__ float approx_sqrt(float x) { return swr_sqrt14(x); }
 __device__ __forceinline__ float mulsign(float x, float y) {
     return __uint_as_float(__float_as_uint(x) ^ (__float_as_uint(y) & 0x80000000u));
 }

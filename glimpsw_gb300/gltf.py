@@ -12,7 +12,8 @@ Differences from the reference, all forced by absent libraries or undefined refe
 * a material without a base colour image has no texture (the reference creates an uninitialised
   4x4 texture);
 * a zero tangent packs as octahedral (0.5, 0.5) (the reference's MapOctahedron divides by zero);
-* ``MapOctahedron``'s rcp14 is the IEEE reciprocal, as everywhere in this project.
+* ``MapOctahedron`` runs the reference's rcp14 bit for bit (``approx14.rcp14``) and its fused
+  multiply-adds (``approx14.fma32``).
 
 Skins and animations (Scene.cpp:102-153, 304-319) are outside the raster path and not imported.
 """
@@ -30,6 +31,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import scenes
+from .approx14 import fma32, rcp14
 
 _COMPONENT = {5120: np.int8, 5121: np.uint8, 5122: np.int16, 5123: np.uint16, 5125: np.uint32, 5126: np.float32}
 _NUM = {"SCALAR": 1, "VEC2": 2, "VEC3": 3, "VEC4": 4, "MAT2": 4, "MAT3": 9, "MAT4": 16}
@@ -270,15 +272,16 @@ def pack_half2(uv: np.ndarray) -> np.ndarray:
 
 
 def map_octahedron(n: np.ndarray) -> np.ndarray:
-    """texutil::MapOctahedron (Texture.h:282-288), float32, rcp14 as the IEEE reciprocal; a zero
-    vector maps to (0.5, 0.5)."""
+    """texutil::MapOctahedron (Texture.h:282-288) in float32: w = rcp14(|x| + |y| + |z|),
+    t = max(-z * w, 0), u = fma(x, w, mulsign(t, x)), v likewise, then * 0.5 + 0.5; a zero vector
+    maps to (0.5, 0.5)."""
     n = n.astype(np.float32)
     s = np.abs(n[:, 0]) + np.abs(n[:, 1]) + np.abs(n[:, 2])
-    with np.errstate(divide="ignore", invalid="ignore"):
-        w = np.float32(1.0) / s
+    with np.errstate(divide="ignore", invalid="ignore", over="ignore"):
+        w = rcp14(s)
         t = np.maximum(-n[:, 2] * w, np.float32(0.0))
-        u = n[:, 0] * w + np.copysign(t, n[:, 0])
-        v = n[:, 1] * w + np.copysign(t, n[:, 1])
+        u = fma32(n[:, 0], w, np.copysign(t, n[:, 0]))
+        v = fma32(n[:, 1], w, np.copysign(t, n[:, 1]))
     out = np.stack([u, v], axis=1) * np.float32(0.5) + np.float32(0.5)
     return np.where(np.isfinite(out), out, np.float32(0.5)).astype(np.float32)
 

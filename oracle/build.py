@@ -18,7 +18,7 @@ LIB = os.path.join(OUT_DIR, "liborc.so")
 def build(force: bool = False) -> str:
     srcs = [os.path.join(HERE, s) for s in SOURCES]
     deps = srcs + [os.path.join(HERE, h) for h in ("swr_oracle.h", "swr_oracle_common.h")]
-    deps.append(os.path.join(HERE, "..", "include", "swr", "hostmath.h"))
+    deps += [os.path.join(HERE, "..", "include", "swr", h) for h in ("hostmath.h", "approx14.h")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)

@@ -71,6 +71,8 @@ def lib():
         L.orc_cull_meshlets.restype = C.c_uint32
         L.orc_texture_storage_words.restype = C.c_uint64
         L.orc_approx_mode_available.restype = C.c_int
+        L.orc_approx14_mismatches.restype = C.c_int64
+        L.orc_approx14_mismatches.argtypes = [C.c_int, C.c_uint64, C.c_uint64]
         L.orc_fb_clear.argtypes = [C.c_void_p, C.c_uint32, C.c_float]
         L.orc_cull_meshlets.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_void_p]
@@ -205,10 +207,27 @@ def resolve_debug(fb: Framebuffer, ctx: Context, layer: int, threads: int = 1):
 
 
 def set_approx_mode(mode: int) -> bool:
+    """simd::approx_rcp/approx_rsqrt: 0 = exact tables (default), 1 = the AVX-512 instructions
+    (x86 hosts with AVX-512 only), 2 = correctly rounded IEEE 1/x and 1/sqrt(x)."""
     if not lib().orc_approx_mode_available(mode):
         return False
     lib().orc_set_approx_mode(mode)
     return True
+
+
+def approx14_mismatches(which: int, first: int, count: int) -> int:
+    """Inputs in [first, first + count) where the tables differ from VRCP14PS (which=0) or
+    VRSQRT14PS (which=1); -1 without AVX-512."""
+    return int(lib().orc_approx14_mismatches(which, first, count))
+
+
+def approx_eval(which: int, x: np.ndarray) -> np.ndarray:
+    """approx_rcp (which=0) / approx_rsqrt (which=1) of a float32 array in the current mode."""
+    a = np.ascontiguousarray(x, dtype=np.float32).view(np.uint32)
+    out = np.empty_like(a)
+    lib().orc_approx_eval(C.c_int(which), a.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p),
+                          C.c_uint64(a.size))
+    return out.view(np.float32)
 
 
 def hiz_texture_size(width: int, height: int) -> tuple[int, int]:
@@ -220,6 +239,6 @@ def hiz_texture_size(width: int, height: int) -> tuple[int, int]:
 
 
 __all__ = ["Framebuffer", "Texture", "Context", "draw_meshlets", "cull_meshlets", "downsample_depth",
-           "resolve", "resolve_debug", "set_approx_mode", "hiz_texture_size", "lib", "SHADER_VISBUFFER",
+           "resolve", "resolve_debug", "set_approx_mode", "approx14_mismatches", "approx_eval", "hiz_texture_size", "lib", "SHADER_VISBUFFER",
            "SHADER_OVERDRAW"]
 _ = os

@@ -13,9 +13,10 @@
 //
 // Float semantics: source order, IEEE round-to-nearest, no contraction
 // (built with -ffp-contract=off); only the reference's explicit simd::fma calls
-// are fused (std::fma). AVX-512 rcp14/rsqrt14 (SIMD.h:294-296) are modelled by
-// correctly rounded 1/x and 1/sqrt(x) unless the x86 hardware path is selected
-// with orc_set_approx_mode(1) on an AVX-512 host.
+// are fused (std::fma). AVX-512 rcp14/rsqrt14 (SIMD.h:294-296) are reproduced
+// bit for bit by the integer tables of include/swr/approx14.h (mode 0, every
+// host); mode 1 runs the instructions on an AVX-512 host, mode 2 substitutes the
+// correctly rounded 1/x and 1/sqrt(x).
 #pragma once
 #include <stdint.h>
 
@@ -85,8 +86,10 @@ enum { ORC_SHADER_VISBUFFER = 0, ORC_SHADER_OVERDRAW = 2 };
 enum { ORC_TRIS_PROCESSED = 0, ORC_TRIS_RASTERIZED = 1, ORC_TRIS_CLIPPED = 2, ORC_BIN_FLUSHES = 3 };
 
 uint32_t orc_meshlet_size(void);
-void orc_set_approx_mode(int mode);  // 0: IEEE model, 1: AVX-512 hardware (x86 only)
+void orc_set_approx_mode(int mode);  // 0: exact tables, 1: AVX-512 hardware (x86 only), 2: IEEE
 int orc_approx_mode_available(int mode);
+int64_t orc_approx14_mismatches(int which, uint64_t first, uint64_t count);
+void orc_approx_eval(int which, const uint32_t* in, uint32_t* out, uint64_t n);
 
 void orc_fb_init(orc_framebuffer* fb, uint32_t width, uint32_t height, uint32_t num_layers, uint32_t* storage);
 uint32_t orc_fb_layer_stride(uint32_t width, uint32_t height);

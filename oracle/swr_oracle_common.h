@@ -73,7 +73,7 @@ static inline int32_t ilog2_x86(float x) {
     return ilog2(x);
 }
 
-// AVX-512 rcp14/rsqrt14 (SIMD.h:294-296) or their correctly rounded model.
+// AVX-512 rcp14/rsqrt14 (SIMD.h:294-296): exact tables, the instructions or IEEE (approx mode).
 float approx_rcp(float x);
 float approx_rsqrt(float x);
 static inline float approx_sqrt(float x) { return approx_rsqrt(x) * x; }

@@ -1,6 +1,7 @@
 // Oracle (test infrastructure, see swr_oracle.h): approximation model, textures and mips,
 // the Hi-Z depth pyramid and meshlet culling.
 #include "swr_oracle_common.h"
+#include "../include/swr/approx14.h"
 #include "../include/swr/hostmath.h"
 
 #include <algorithm>
@@ -25,17 +26,31 @@ __attribute__((target("avx512f"))) static float hw_rcp14(float x) {
 __attribute__((target("avx512f"))) static float hw_rsqrt14(float x) {
     return _mm_cvtss_f32(_mm512_castps512_ps128(_mm512_rsqrt14_ps(_mm512_set1_ps(x))));
 }
+// 16 inputs per instruction, for the exhaustive comparison with the tables.
+__attribute__((target("avx512f"))) static void hw_approx16(int which, const uint32_t* in, uint32_t* out) {
+    __m512 v;
+    memcpy(&v, in, 64);
+    __m512 r = which ? _mm512_rsqrt14_ps(v) : _mm512_rcp14_ps(v);
+    memcpy(out, &r, 64);
+}
 static bool hw_available() { return __builtin_cpu_supports("avx512f"); }
 #else
-static float hw_rcp14(float x) { return 1.0f / x; }
-static float hw_rsqrt14(float x) { return 1.0f / std::sqrt(x); }
+static float hw_rcp14(float x) { return swr_rcp14(x); }
+static float hw_rsqrt14(float x) { return swr_rsqrt14(x); }
+static void hw_approx16(int, const uint32_t*, uint32_t*) {}
 static bool hw_available() { return false; }
 #endif
 
-// rcp14/rsqrt14 model: correctly rounded IEEE reciprocal and 1/sqrtf (two IEEE roundings).
-// Mode 1 runs the hardware instructions on an AVX-512 host.
-float approx_rcp(float x) { return g_approxMode == 1 ? hw_rcp14(x) : 1.0f / x; }
-float approx_rsqrt(float x) { return g_approxMode == 1 ? hw_rsqrt14(x) : 1.0f / std::sqrt(x); }
+// simd::approx_rcp / approx_rsqrt (SIMD.h:294-295). Mode 0: the exact integer restatement of
+// VRCP14PS/VRSQRT14PS (include/swr/approx14.h, the same functions the GPU kernels run); mode 1:
+// the instructions themselves on an AVX-512 host; mode 2: the correctly rounded IEEE 1/x and
+// 1/sqrtf(x), kept to measure what the approximation changes.
+float approx_rcp(float x) {
+    return g_approxMode == 0 ? swr_rcp14(x) : g_approxMode == 1 ? hw_rcp14(x) : 1.0f / x;
+}
+float approx_rsqrt(float x) {
+    return g_approxMode == 0 ? swr_rsqrt14(x) : g_approxMode == 1 ? hw_rsqrt14(x) : 1.0f / std::sqrt(x);
+}
 
 // Texture2D::GetTexelOffset for TiledY8, Texture.h:493-501.
 static inline uint32_t texel_offset(uint32_t x, uint32_t y, uint32_t stride) {
@@ -81,8 +96,31 @@ using namespace orc;
 
 extern "C" {
 
-void orc_set_approx_mode(int mode) { g_approxMode = (mode == 1 && hw_available()) ? 1 : 0; }
-int orc_approx_mode_available(int mode) { return mode == 0 || (mode == 1 && hw_available()); }
+void orc_set_approx_mode(int mode) { g_approxMode = (mode == 2 || (mode == 1 && hw_available())) ? mode : 0; }
+int orc_approx_mode_available(int mode) { return mode == 0 || mode == 2 || (mode == 1 && hw_available()); }
+
+// approx_rcp (which = 0) or approx_rsqrt (which = 1) of n float bit patterns in the current mode.
+void orc_approx_eval(int which, const uint32_t* in, uint32_t* out, uint64_t n) {
+    for (uint64_t i = 0; i < n; i++) out[i] = f2u(which ? approx_rsqrt(u2f(in[i])) : approx_rcp(u2f(in[i])));
+}
+
+// Number of inputs among `count` consecutive 32-bit patterns from `first` (a multiple of 16) for
+// which the table restatement differs from the instruction (which: 0 rcp14, 1 rsqrt14); -1 when
+// the host has no AVX-512.
+int64_t orc_approx14_mismatches(int which, uint64_t first, uint64_t count) {
+    if (!hw_available() || (first & 15)) return -1;
+    int64_t bad = 0;
+    for (uint64_t b = first; b < first + count; b += 16) {
+        uint32_t in[16], hw[16];
+        for (int j = 0; j < 16; j++) in[j] = (uint32_t)(b + j);
+        hw_approx16(which, in, hw);
+        for (int j = 0; j < 16 && b + j < first + count; j++) {
+            const float f = u2f(in[j]);
+            if (f2u(which ? swr_rsqrt14(f) : swr_rcp14(f)) != hw[j]) bad++;
+        }
+    }
+    return bad;
+}
 
 // CreateTexture2D, Texture.h:599-636 (mips stop below 4 texels; levels 64-word aligned).
 static void texture_layout(uint32_t width, uint32_t height, uint32_t maxLevels, uint32_t* mipOffsets,

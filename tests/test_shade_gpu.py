@@ -1,5 +1,5 @@
 """GPU parity of textures, the Hi-Z pyramid, meshlet culling and the vis-buffer resolve against
-the CPU oracle (same rcp14/rsqrt14 model on both sides: IEEE 1/x and 1/sqrtf).
+the CPU oracle (both sides run rcp14/rsqrt14 through the exact tables of include/swr/approx14.h).
 
 Mips, Hi-Z texels and cull bitmaps must be bit-exact; the resolved RGBA8 colour must be within
 1/255 per channel (the contract), and the test also reports how many pixels match exactly.
@@ -110,3 +110,36 @@ def test_resolve_within_one_lsb(shaded):
     print(f"resolve: max abs {diff.max()} / 255, exact pixels {exact:.6f}")
     assert diff.max() <= 1
     assert exact > 0.999
+
+
+def test_resolve_follows_rcp14_tables(shaded):
+    """On the pixels where the reference's rcp14/rsqrt14 give a different colour than correctly
+    rounded IEEE reciprocals would, the GPU gives the reference's colour exactly: the device runs
+    the instructions' tables, not an IEEE stand-in."""
+    from glimpsw_gb300 import api
+    from oracle import oracle as O
+    sc, texs, env, g = shaded
+    v = sc.views[0]
+    w, h = v.width, v.height
+    lights = default_lights()
+    gfb, _ = g.render(v.world_to_clip, w, h)
+    gctx = api.ShadingContext(g.scene, v.world_to_clip, world_to_clip=v.world_to_clip, skybox=env.g, view_pos=v.eye,
+                              lights=gpu_lights(lights))
+    gctx.resolve(g.rast, gfb)
+    got = gfb.get_pixels(0).view(np.uint8).reshape(h, w, 4).astype(np.int32)
+    out = {}
+    for mode in (0, 2):
+        ofb, _ = render_oracle(sc.meshlets, sc.materials, v.world_to_clip, w, h)
+        octx = O.Context(sc.meshlets, sc.materials, v.world_to_clip, world_to_clip=v.world_to_clip,
+                         textures=[t.o for t in texs], lights=lights, skybox=env.o, view_pos=v.eye)
+        assert O.set_approx_mode(mode)
+        try:
+            O.resolve(ofb, octx)
+        finally:
+            O.set_approx_mode(0)
+        out[mode] = ofb.get_pixels(0).view(np.uint8).reshape(h, w, 4).astype(np.int32)
+    sensitive = (out[0] != out[2]).any(axis=2)
+    print(f"pixels whose colour depends on rcp14/rsqrt14: {int(sensitive.sum())}")
+    assert sensitive.sum() > 0
+    assert np.array_equal(got[sensitive], out[0][sensitive])
+
