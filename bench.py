@@ -278,6 +278,14 @@ def peaks():
         return 6800.0, "fallback"
 
 
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the frame's kernels, from
+# one ncu capture of the default workload (100k meshlets, 1920x1080; the capture used 256^2
+# textures, which changes only the resolve's texel addresses), averaged over the frame's launches:
+# k_draw_meshlets 88.6 MB and 35.3 MB for the two batches, k_raster_big 40.9 MB and 21.1 MB.
+NCU_DRAM_BYTES_PER_LAUNCH = {"k_draw_meshlets": 61.93e6, "k_raster_big": 30.999e6, "k_resolve": 27.26e6}
+NCU_WORKLOAD = (100_000, 1920, 1080)
+
+
 # ----------------------------------------------------------------------------- multi-view
 def multiview_section(args, api, stream):
     """64 views (6 depth-only cube faces at 1024^2 + 58 cameras of log-uniform resolution) of a
@@ -776,7 +784,8 @@ def run_ours(args):
     top_avg_s = per[top_name][1] / per[top_name][0] / 1e3
     achieved = algo[top_name] / top_avg_s / 1e9
     roofline = {"bound": "hbm", "kernel": top_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                "frac": achieved / peak, "peak_kind": peak_kind, "traffic": None,
+                "frac": achieved / peak, "peak_kind": peak_kind,
+                "traffic": NCU_DRAM_BYTES_PER_LAUNCH.get(top_name) if (n, W, H) == NCU_WORKLOAD else None,
                 "algorithmic_bytes_per_launch": algo[top_name], "avg_launch_ms": top_avg_s * 1e3}
 
     # end to end through the public API: pinned host scene upload + frame + colour readback
