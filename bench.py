@@ -63,8 +63,10 @@ def parse():
     p.add_argument("--neural-width", type=int, default=2560)
     p.add_argument("--neural-height", type=int, default=1440)
     p.add_argument("--no-alpha", action="store_true")
-    p.add_argument("--only", default="all", choices=["all", "neural"],
-                   help="neural: only the learned-decoder section (for profiling runs; prints that section)")
+    p.add_argument("--multiview-cameras", type=int, default=58,
+                   help="cameras besides the 6 cube faces of the multi-view workload")
+    p.add_argument("--only", default="all", choices=["all", "neural", "multiview"],
+                   help="neural / multiview: only that section (for profiling runs; prints that section)")
     return p.parse_args()
 
 
@@ -294,7 +296,7 @@ def multiview_section(args, api, stream):
     import torch
 
     from glimpsw_gb300 import autotune, scenes
-    sc = scenes.multiview_scene(n=args.multiview_meshlets)
+    sc = scenes.multiview_scene(n=args.multiview_meshlets, n_cameras=args.multiview_cameras)
     scene = api.Scene()
     scene.upload_meshlets(sc.meshlets)
     scene.set_materials(sc.materials)
@@ -670,6 +672,13 @@ def run_ours(args):
     torch.cuda.set_device(local)
     from glimpsw_gb300 import api, scenes
     api.load_library()
+    if args.only == "multiview":  # the multi-view section alone (profiling runs)
+        stream = torch.cuda.current_stream()
+        api.set_stream(stream.cuda_stream)
+        out = multiview_section(args, api, stream)
+        if rank == 0:
+            print(json.dumps({"multiview": out}), flush=True)
+        return
 
     sc = build_scene(args)
     v0, v1 = sc.views

@@ -63,14 +63,31 @@ __device__ __forceinline__ void render_bbox(const Setup& t, int halfW, int halfH
     bbMax = (y + 0x00030003u) & ~0x00030003u;
 }
 
-// TrianglePacket::Setup (Rasterizer.cpp:257-289); returns the lane's keep bit.
-__device__ __forceinline__ bool tri_setup(Vtx v0, Vtx v1, Vtx v2, int halfW, int halfH, int cullMode, Setup& t,
-                                          uint32_t& bbMin, uint32_t& bbMax) {
-    // 1.0f / w (perspective_div, SIMD.h:473-476): the correctly rounded reciprocal is the same value
-    float rw0 = __frcp_rn(v0.w), rw1 = __frcp_rn(v1.w), rw2 = __frcp_rn(v2.w);
-    float x0 = fmul(v0.x, rw0), y0 = fmul(v0.y, rw0);
-    float x1 = fmul(v1.x, rw1), y1 = fmul(v1.y, rw1);
-    float x2 = fmul(v2.x, rw2), y2 = fmul(v2.y, rw2);
+// ShadeMeshlet's vertex transform (Shading.cpp:295-298, simd::mul with w = 1, SIMD.h:457-464): the
+// clip position of a vertex slot; slots past the 16-vertex chunks up to NumVertices are zero.
+__device__ __forceinline__ float4 clip_position(float x, float y, float z, bool live, const ViewParams& vp) {
+    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (live) {
+        c.x = ffma(x, vp.m[0], ffma(y, vp.m[4], ffma(z, vp.m[8], vp.m[12])));
+        c.y = ffma(x, vp.m[1], ffma(y, vp.m[5], ffma(z, vp.m[9], vp.m[13])));
+        c.z = ffma(x, vp.m[2], ffma(y, vp.m[6], ffma(z, vp.m[10], vp.m[14])));
+        c.w = ffma(x, vp.m[3], ffma(y, vp.m[7], ffma(z, vp.m[11], vp.m[15])));
+    }
+    return c;
+}
+
+// A vertex after simd::perspective_div (SIMD.h:473-476): x/w, y/w, z/w and 1/w. The correctly
+// rounded reciprocal is the same value as 1.0f / w.
+struct Ndc { float x, y, z, rw; };
+__device__ __forceinline__ Ndc project(float x, float y, float z, float w) {
+    const float rw = __frcp_rn(w);
+    return { fmul(x, rw), fmul(y, rw), fmul(z, rw), rw };
+}
+
+// TrianglePacket::Setup (Rasterizer.cpp:257-289) from projected vertices; returns the lane's keep bit.
+__device__ __forceinline__ bool tri_setup_ndc(const Ndc& n0, const Ndc& n1, const Ndc& n2, int halfW, int halfH,
+                                              int cullMode, Setup& t, uint32_t& bbMin, uint32_t& bbMax) {
+    const float x0 = n0.x, y0 = n0.y, x1 = n1.x, y1 = n1.y, x2 = n2.x, y2 = n2.y;
     float det = fsub(fmul(fsub(x2, x0), fsub(y1, y0)), fmul(fsub(x0, x1), fsub(y0, y2)));
     if (cullMode != kCullFrontCCW) {
         bool flip = (cullMode == kCullFrontCW) ? true : (det < 0);
@@ -86,9 +103,16 @@ __device__ __forceinline__ bool tri_setup(Vtx v0, Vtx v1, Vtx v2, int halfW, int
     t.Pos2 = ((uint32_t)ix2 & 0xFFFF) | ((uint32_t)iy2 << 16);
     render_bbox(t, halfW, halfH, bbMin, bbMax);
     if (lo16(bbMin) >= lo16(bbMax) || hi16(bbMin) >= hi16(bbMax)) keep = false;
-    t.Z0 = fmul(v0.z, rw0), t.Z1 = fmul(v1.z, rw1), t.Z2 = fmul(v2.z, rw2);
-    t.W0 = rw0, t.W1 = rw1, t.W2 = rw2;
+    t.Z0 = n0.z, t.Z1 = n1.z, t.Z2 = n2.z;
+    t.W0 = n0.rw, t.W1 = n1.rw, t.W2 = n2.rw;
     return keep;
+}
+
+// TrianglePacket::Setup from clip-space vertices (the clipper's output triangles).
+__device__ __forceinline__ bool tri_setup(Vtx v0, Vtx v1, Vtx v2, int halfW, int halfH, int cullMode, Setup& t,
+                                          uint32_t& bbMin, uint32_t& bbMax) {
+    return tri_setup_ndc(project(v0.x, v0.y, v0.z, v0.w), project(v1.x, v1.y, v1.z, v1.w),
+                         project(v2.x, v2.y, v2.z, v2.w), halfW, halfH, cullMode, t, bbMin, bbMax);
 }
 
 // ComputeEdge (Rasterizer.cpp:291-295), wrapping int32.
@@ -718,38 +742,43 @@ __device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t out
     }
 }
 
-// Triangle p of a meshlet for one lane of a 32-triangle step: its clip-space vertices (the
-// meshlet's transformed vertices pos, gathered as simd::gather_preload64 does) and
-// Clipper::ComputeClipCodes (Rasterizer.cpp:353-397) per lane.
+// Triangle p of a meshlet for one lane of a 32-triangle step: its projected vertices (gathered
+// from the meshlet's per-vertex arrays as simd::gather_preload64 does) and its clip codes
+// (Clipper::ComputeClipCodes, Rasterizer.cpp:353-397). The transform step computes each vertex's
+// perspective division and codes once; a vertex is shared by about six triangles.
 struct LaneTri {
-    Vtx v0, v1, v2;
+    Ndc n0, n1, n2;     // projected vertices
+    uint32_t i0, i1, i2;  // their slots in the meshlet's vertex arrays
     uint32_t partial;   // OR of the vertices' out codes
     bool acc, nontriv;  // trivially accepted / accepted but needs clipping
 };
-__device__ __forceinline__ LaneTri lane_triangle(const float4* pos, const uint8_t* idxBytes, uint32_t p, bool valid,
-                                                 const ViewParams& vp) {
+
+// Per-vertex part of Clipper::ComputeClipCodes (Rasterizer.cpp:353-397): the six out-code bits and,
+// in bit 6, the guard-band test |x| < w bx and |y| < w by. A triangle's codes combine its vertices'.
+constexpr uint32_t kCodeInBand = 0x40u;
+__device__ __forceinline__ uint32_t vertex_code(float4 q, const ViewParams& vp) {
+    uint32_t oc = 0;
+    oc |= (q.x < -q.w) ? 1u : 0u;
+    oc |= (q.x > q.w) ? 2u : 0u;
+    oc |= (q.y < -q.w) ? 4u : 0u;
+    oc |= (q.y > q.w) ? 8u : 0u;
+    oc |= (q.z < -q.w) ? 16u : 0u;
+    oc |= (q.z > q.w) ? 32u : 0u;
+    if (fabsf(q.x) < fmul(q.w, vp.bx) && fabsf(q.y) < fmul(q.w, vp.by)) oc |= kCodeInBand;
+    return oc;
+}
+
+__device__ __forceinline__ LaneTri lane_triangle(const float4* ndc, const uint8_t* codes, const uint8_t* idxBytes,
+                                                 uint32_t p, bool valid) {
     LaneTri lt;
-    const float4 q0 = pos[preload64_index(idxBytes[p & 127])];
-    const float4 q1 = pos[preload64_index(idxBytes[128 + (p & 127)])];
-    const float4 q2 = pos[preload64_index(idxBytes[256 + (p & 127)])];
-    lt.v0 = { q0.x, q0.y, q0.z, q0.w }, lt.v1 = { q1.x, q1.y, q1.z, q1.w }, lt.v2 = { q2.x, q2.y, q2.z, q2.w };
-    uint32_t partial = 0, combined = 0x3F;
-    bool trivial = true;
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        const Vtx& q = i == 0 ? lt.v0 : (i == 1 ? lt.v1 : lt.v2);
-        uint32_t oc = 0;
-        oc |= (q.x < -q.w) ? 1u : 0u;
-        oc |= (q.x > q.w) ? 2u : 0u;
-        oc |= (q.y < -q.w) ? 4u : 0u;
-        oc |= (q.y > q.w) ? 8u : 0u;
-        oc |= (q.z < -q.w) ? 16u : 0u;
-        oc |= (q.z > q.w) ? 32u : 0u;
-        partial |= oc;
-        combined &= oc;
-        trivial = trivial && (fabsf(q.x) < fmul(q.w, vp.bx) && fabsf(q.y) < fmul(q.w, vp.by));
-    }
-    if (partial & 0x30u) trivial = false;
+    lt.i0 = preload64_index(idxBytes[p & 127]);
+    lt.i1 = preload64_index(idxBytes[128 + (p & 127)]);
+    lt.i2 = preload64_index(idxBytes[256 + (p & 127)]);
+    const float4 q0 = ndc[lt.i0], q1 = ndc[lt.i1], q2 = ndc[lt.i2];
+    lt.n0 = { q0.x, q0.y, q0.z, q0.w }, lt.n1 = { q1.x, q1.y, q1.z, q1.w }, lt.n2 = { q2.x, q2.y, q2.z, q2.w };
+    const uint32_t c0 = codes[lt.i0], c1 = codes[lt.i1], c2 = codes[lt.i2];
+    const uint32_t partial = (c0 | c1 | c2) & 0x3Fu, combined = c0 & c1 & c2 & 0x3Fu;
+    const bool trivial = (c0 & c1 & c2 & kCodeInBand) != 0 && !(partial & 0x30u);
     const bool accept = valid && combined == 0;
     lt.partial = partial;
     lt.acc = accept && trivial;
@@ -762,11 +791,12 @@ __device__ __forceinline__ LaneTri lane_triangle(const float4* pos, const uint8_
 // owner lane of each tile in the concatenated tile list of the round's small triangles. The alpha
 // pass also keeps each small triangle's alpha terms.
 struct WarpSmem {
-    float4 pos[64];
+    float4 ndc[64];      // projected vertices: x/w, y/w, z/w, 1/w
     uint32_t idx[96];
     TriRec tris[32];
     ViewParams view;
     uint8_t owner[32 * kSmallTiles];
+    uint8_t code[64];    // vertex_code
 };
 struct WarpSmemAlpha : WarpSmem {
     AlphaExt exts[32];
@@ -802,7 +832,6 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     extern __shared__ __align__(16) unsigned char smemRaw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     Smem& S = ((Smem*)smemRaw)[warp];
-    float4* pos = S.pos;
     const uint8_t* idxBytes = (const uint8_t*)S.idx;
     TriRec* tris = S.tris;
     const ViewParams& vp = S.view;
@@ -934,14 +963,10 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
         // slots past them are zero.
         const uint32_t nvr = min((nv + 15) & ~15u, 64u);
         auto xform = [&](uint32_t v, float x, float y, float z) {
-            float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (v < nvr) {
-                c.x = ffma(x, vp.m[0], ffma(y, vp.m[4], ffma(z, vp.m[8], vp.m[12])));
-                c.y = ffma(x, vp.m[1], ffma(y, vp.m[5], ffma(z, vp.m[9], vp.m[13])));
-                c.z = ffma(x, vp.m[2], ffma(y, vp.m[6], ffma(z, vp.m[10], vp.m[14])));
-                c.w = ffma(x, vp.m[3], ffma(y, vp.m[7], ffma(z, vp.m[11], vp.m[15])));
-            }
-            pos[v] = c;
+            const float4 c = clip_position(x, y, z, v < nvr, vp);
+            const Ndc n = project(c.x, c.y, c.z, c.w);
+            S.ndc[v] = make_float4(n.x, n.y, n.z, n.rw);
+            S.code[v] = (uint8_t)vertex_code(c, vp);
         };
         xform(lane, px0, py0, pz0);
         xform(32 + lane, px1, py1, pz1);
@@ -950,8 +975,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
 
         for (uint32_t base = 0; base < nt; base += 32) {
             const uint32_t p = base + lane;
-            const LaneTri lt = lane_triangle(pos, idxBytes, p, p < nt, vp);
-            const Vtx &v0 = lt.v0, &v1 = lt.v1, &v2 = lt.v2;
+            const LaneTri lt = lane_triangle(S.ndc, S.code, idxBytes, p, p < nt);
             if (a.countClipped) nClipped += __popc(__ballot_sync(0xFFFFFFFFu, lt.nontriv)) * (lane == 0);
 
             int myTiles = 0;     // tiles of this lane's small triangle (0 if none)
@@ -959,7 +983,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
             if (lt.acc) {
                 Setup t;
                 uint32_t bbMin, bbMax;
-                if (tri_setup(v0, v1, v2, vp.halfW, vp.halfH, cullMode, t, bbMin, bbMax)) {
+                if (tri_setup_ndc(lt.n0, lt.n1, lt.n2, vp.halfW, vp.halfH, cullMode, t, bbMin, bbMax)) {
                     TriRec r;
                     float rcpArea;
                     const int32_t det = edge_setup(t, vp.halfW, vp.halfH, bbMin, bbMax, make_rank(g, p, 0, 0), r, &rcpArea);
@@ -996,9 +1020,15 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                     }
                 }
             }
-            if (lt.nontriv && a.clipMode)
-                clip_and_queue(v0, v1, v2, lt.partial, a, vp, view, chunk, cullMode, g, p, nRaster, kAlpha ? matId : ~0u, mp,
-                               idxBytes);
+            if (lt.nontriv && a.clipMode) {  // rare: the clip-space vertices are transformed again
+                const float* P = (const float*)(mp + kOffPositions);
+                auto clip_vertex = [&](uint32_t v) {
+                    const float4 c = clip_position(P[v], P[64 + v], P[128 + v], v < nvr, vp);
+                    return Vtx{ c.x, c.y, c.z, c.w };
+                };
+                clip_and_queue(clip_vertex(lt.i0), clip_vertex(lt.i1), clip_vertex(lt.i2), lt.partial, a, vp, view, chunk,
+                               cullMode, g, p, nRaster, kAlpha ? matId : ~0u, mp, idxBytes);
+            }
             __syncwarp();
 
             // Once half of the warps have run out of work items, the warps still busy are the
