@@ -84,16 +84,23 @@ __device__ __forceinline__ Ndc project(float x, float y, float z, float w) {
     return { fmul(x, rw), fmul(y, rw), fmul(z, rw), rw };
 }
 
-// TrianglePacket::Setup (Rasterizer.cpp:257-289) from projected vertices; returns the lane's keep bit.
-__device__ __forceinline__ bool tri_setup_ndc(const Ndc& n0, const Ndc& n1, const Ndc& n2, int halfW, int halfH,
-                                              int cullMode, Setup& t, uint32_t& bbMin, uint32_t& bbMax) {
+// The face test of TrianglePacket::Setup (Rasterizer.cpp:262-266): the float determinant of the
+// projected vertices, negated for FrontCW or made absolute for None; the triangle is kept if > 0.
+__device__ __forceinline__ bool front_facing(const Ndc& n0, const Ndc& n1, const Ndc& n2, int cullMode) {
     const float x0 = n0.x, y0 = n0.y, x1 = n1.x, y1 = n1.y, x2 = n2.x, y2 = n2.y;
     float det = fsub(fmul(fsub(x2, x0), fsub(y1, y0)), fmul(fsub(x0, x1), fsub(y0, y2)));
     if (cullMode != kCullFrontCCW) {
         bool flip = (cullMode == kCullFrontCW) ? true : (det < 0);
         det = flip ? -det : det;
     }
-    bool keep = det > 0;
+    return det > 0;
+}
+
+// TrianglePacket::Setup (Rasterizer.cpp:257-289) from projected vertices; returns the lane's keep bit.
+__device__ __forceinline__ bool tri_setup_ndc(const Ndc& n0, const Ndc& n1, const Ndc& n2, int halfW, int halfH,
+                                              int cullMode, Setup& t, uint32_t& bbMin, uint32_t& bbMax) {
+    const float x0 = n0.x, y0 = n0.y, x1 = n1.x, y1 = n1.y, x2 = n2.x, y2 = n2.y;
+    bool keep = front_facing(n0, n1, n2, cullMode);
     float fsx = (float)(halfW * 16), fsy = (float)(halfH * 16);
     int32_t ix0 = round2i(fmul(x0, fsx)), iy0 = round2i(fmul(y0, fsy));
     int32_t ix1 = round2i(fmul(x1, fsx)), iy1 = round2i(fmul(y1, fsy));
@@ -748,7 +755,6 @@ __device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t out
 // perspective division and codes once; a vertex is shared by about six triangles.
 struct LaneTri {
     Ndc n0, n1, n2;     // projected vertices
-    uint32_t i0, i1, i2;  // their slots in the meshlet's vertex arrays
     uint32_t partial;   // OR of the vertices' out codes
     bool acc, nontriv;  // trivially accepted / accepted but needs clipping
 };
@@ -771,12 +777,12 @@ __device__ __forceinline__ uint32_t vertex_code(float4 q, const ViewParams& vp) 
 __device__ __forceinline__ LaneTri lane_triangle(const float4* ndc, const uint8_t* codes, const uint8_t* idxBytes,
                                                  uint32_t p, bool valid) {
     LaneTri lt;
-    lt.i0 = preload64_index(idxBytes[p & 127]);
-    lt.i1 = preload64_index(idxBytes[128 + (p & 127)]);
-    lt.i2 = preload64_index(idxBytes[256 + (p & 127)]);
-    const float4 q0 = ndc[lt.i0], q1 = ndc[lt.i1], q2 = ndc[lt.i2];
+    const uint32_t i0 = preload64_index(idxBytes[p & 127]);
+    const uint32_t i1 = preload64_index(idxBytes[128 + (p & 127)]);
+    const uint32_t i2 = preload64_index(idxBytes[256 + (p & 127)]);
+    const float4 q0 = ndc[i0], q1 = ndc[i1], q2 = ndc[i2];
     lt.n0 = { q0.x, q0.y, q0.z, q0.w }, lt.n1 = { q1.x, q1.y, q1.z, q1.w }, lt.n2 = { q2.x, q2.y, q2.z, q2.w };
-    const uint32_t c0 = codes[lt.i0], c1 = codes[lt.i1], c2 = codes[lt.i2];
+    const uint32_t c0 = codes[i0], c1 = codes[i1], c2 = codes[i2];
     const uint32_t partial = (c0 | c1 | c2) & 0x3Fu, combined = c0 & c1 & c2 & 0x3Fu;
     const bool trivial = (c0 & c1 & c2 & kCodeInBand) != 0 && !(partial & 0x30u);
     const bool accept = valid && combined == 0;
@@ -797,6 +803,7 @@ struct WarpSmem {
     ViewParams view;
     uint8_t owner[32 * kSmallTiles];
     uint8_t code[64];    // vertex_code
+    uint8_t live[128];   // the meshlet's triangles that survive the face test or need clipping
 };
 struct WarpSmemAlpha : WarpSmem {
     AlphaExt exts[32];
@@ -973,10 +980,25 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
         S.idx[lane] = ix0, S.idx[32 + lane] = ix1, S.idx[64 + lane] = ix2;
         __syncwarp();
 
+        // About half of a closed meshlet's triangles face away. The face test runs first for all of
+        // them and compacts the rest into S.live, so the setup and binning below run on full
+        // 32-triangle steps. Each triangle keeps its index p (its rank), so the keys do not change.
+        uint32_t nLive = 0;
         for (uint32_t base = 0; base < nt; base += 32) {
             const uint32_t p = base + lane;
             const LaneTri lt = lane_triangle(S.ndc, S.code, idxBytes, p, p < nt);
             if (a.countClipped) nClipped += __popc(__ballot_sync(0xFFFFFFFFu, lt.nontriv)) * (lane == 0);
+            const bool live = (lt.nontriv && a.clipMode) || (lt.acc && front_facing(lt.n0, lt.n1, lt.n2, cullMode));
+            const unsigned liveMask = __ballot_sync(0xFFFFFFFFu, live);
+            if (live) S.live[nLive + __popc(liveMask & ((1u << lane) - 1u))] = (uint8_t)p;
+            nLive += __popc(liveMask);
+        }
+        __syncwarp();
+
+        for (uint32_t base = 0; base < nLive; base += 32) {
+            const bool valid = base + lane < nLive;
+            const uint32_t p = valid ? S.live[base + lane] : 0u;
+            const LaneTri lt = lane_triangle(S.ndc, S.code, idxBytes, p, valid);
 
             int myTiles = 0;     // tiles of this lane's small triangle (0 if none)
             bool overflow = false;
@@ -1026,8 +1048,9 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                     const float4 c = clip_position(P[v], P[64 + v], P[128 + v], v < nvr, vp);
                     return Vtx{ c.x, c.y, c.z, c.w };
                 };
-                clip_and_queue(clip_vertex(lt.i0), clip_vertex(lt.i1), clip_vertex(lt.i2), lt.partial, a, vp, view, chunk,
-                               cullMode, g, p, nRaster, kAlpha ? matId : ~0u, mp, idxBytes);
+                clip_and_queue(clip_vertex(preload64_index(idxBytes[p])), clip_vertex(preload64_index(idxBytes[128 + p])),
+                               clip_vertex(preload64_index(idxBytes[256 + p])), lt.partial, a, vp, view, chunk, cullMode, g, p,
+                               nRaster, kAlpha ? matId : ~0u, mp, idxBytes);
             }
             __syncwarp();
 
