@@ -283,8 +283,8 @@ def peaks():
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the frame's kernels, from
 # one ncu capture of the default workload (100k meshlets, 1920x1080; the capture used 256^2
 # textures, which changes only the resolve's texel addresses), averaged over the frame's launches:
-# k_draw_meshlets 88.6 MB and 35.3 MB for the two batches, k_raster_big 40.9 MB and 21.1 MB.
-NCU_DRAM_BYTES_PER_LAUNCH = {"k_draw_meshlets": 61.93e6, "k_raster_big": 30.999e6, "k_resolve": 27.26e6}
+# k_draw_meshlets 86.73 MB and 35.01 MB for the two batches, k_raster_big 41.93 MB and 22.11 MB.
+NCU_DRAM_BYTES_PER_LAUNCH = {"k_draw_meshlets": 60.87e6, "k_raster_big": 32.02e6, "k_resolve": 27.26e6}
 NCU_WORKLOAD = (100_000, 1920, 1080)
 
 
