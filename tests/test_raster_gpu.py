@@ -1,6 +1,7 @@
 """GPU parity of the vis-buffer rasterizer against the CPU oracle: bit-exact depth and surface ids.
 
-Cases: the small grid scene (BASELINE config 1 construction, reduced), a volume scene with the
+Cases: the small grid scene (the 1024-meshlet plain-path construction, at 640x360 and at its own
+1280x720), a volume scene with the
 camera inside it (near-plane clipping, guard band), both binned (Mode A) and unbinned (Mode B)
 semantics, guard band off, equal-depth ties, meshlet offsets with cull bitmaps, multi-draw frames.
 """
@@ -34,6 +35,18 @@ def test_grid_bit_exact(grid, binning):
     sc, g = grid
     v = sc.views[0]
     gfb, gc = g.render(v.world_to_clip, v.width, v.height, binning=binning)
+    ofb, oc = render_oracle(sc.meshlets, sc.materials, v.world_to_clip, v.width, v.height, binning=binning)
+    assert_visbuffer_equal(gfb, ofb)
+    assert list(gc[:3]) == list(oc[:3])
+
+
+@pytest.mark.parametrize("binning", [True, False])
+def test_config1_size_bit_exact(binning):
+    """The small plain-path configuration at its own size: 1024 grid meshlets at 1280x720."""
+    sc = scenes.grid_scene(n_side=32, width=1280, height=720)
+    v = sc.views[0]
+    assert len(sc.meshlets) == 1024 and (v.width, v.height) == (1280, 720)
+    gfb, gc = GpuRenderer(sc.meshlets, sc.materials).render(v.world_to_clip, v.width, v.height, binning=binning)
     ofb, oc = render_oracle(sc.meshlets, sc.materials, v.world_to_clip, v.width, v.height, binning=binning)
     assert_visbuffer_equal(gfb, ofb)
     assert list(gc[:3]) == list(oc[:3])
