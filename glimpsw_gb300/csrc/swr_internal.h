@@ -126,6 +126,9 @@ struct DrawArgs {
     unsigned long long* counts;
     // single view: order_stride(count), set by launch_draw
     uint32_t orderStride;
+    // the shading steps read a pixel's key before its atomicMax only for triangles of at most this
+    // many tiles (0: for all); set by launch_draw
+    uint32_t keyReadTiles;
 };
 
 // The mesh stage draws a view's meshlets in the order p -> (p * stride) mod count: a Weyl sequence
