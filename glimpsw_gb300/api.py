@@ -124,6 +124,8 @@ _SIGS = {
     "swr_neural_set_latents": [C.c_void_p, C.c_uint32, C.c_void_p],
     "swr_neural_decode": [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p],
     "swr_resolve_neural": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
+    "swr_neural_set_wait_limit": [C.c_void_p, C.c_uint64],
+    "swr_selftest_bounded_wait": [C.c_uint64],
     "swr_meshlet_bound": [C.c_uint32],
     "swr_build_meshlets": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p],
 }
@@ -555,6 +557,10 @@ class NeuralMaterials:
         i = self.info
         return {"latent_bytes": i.latent_bytes, "weight_bytes": i.weight_bytes, "fallback_bytes": i.fallback_bytes,
                 "plain_bytes": i.plain_bytes}
+
+    def set_wait_limit(self, limit_ns: int) -> None:
+        """Time limit of each bounded device-side wait of the model's kernels (default 1 s)."""
+        _check(_lib.swr_neural_set_wait_limit(self.h, C.c_uint64(limit_ns)))
 
     def train(self, steps: int, batch: int = 65536, materials_per_step: int = 8, lr: float = 1e-3,
               want_loss: bool = False, level_weighting: int = 1):

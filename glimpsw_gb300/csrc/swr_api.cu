@@ -48,16 +48,7 @@ swr_status cuda_fail(cudaError_t e, const char* what) {
         if (e_ != cudaSuccess) return cuda_fail(e_, what); \
     } while (0)
 
-int num_sms() {
-    static int n = 0;
-    if (n == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 148;
-    }
-    return n;
-}
+int num_sms() { return swr_internal_sm_count(); }
 
 constexpr uint32_t kDefaultBigCapacity = 1u << 18;
 
@@ -151,6 +142,31 @@ void swr_internal_count_launches(unsigned long long n) { g_launches.fetch_add(n,
 swr_status swr_internal_fail(swr_status code, const char* msg) { return fail(code, "%s", msg); }
 swr_status swr_internal_cuda_fail(cudaError_t e, const char* what) { return cuda_fail(e, what); }
 cudaStream_t swr_internal_stream() { return t_stream; }
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::atomic<int> g_smCount[kMaxDevices];  // 0: not queried yet
+}  // namespace
+
+swr_status swr_internal_device(int* dev, int* sms) {
+    cudaError_t e = cudaGetDevice(dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (*dev < 0 || *dev >= kMaxDevices) return fail(SWR_EINVAL, "device ordinal %d above %d", *dev, kMaxDevices - 1);
+    int n = g_smCount[*dev].load(std::memory_order_relaxed);
+    if (n <= 0) {
+        e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, *dev);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute(MultiProcessorCount)");
+        if (n <= 0) return fail(SWR_ECUDA, "device %d reports %d SMs", *dev, n);
+        g_smCount[*dev].store(n, std::memory_order_relaxed);
+    }
+    *sms = n;
+    return SWR_OK;
+}
+
+int swr_internal_sm_count() {
+    int dev = 0, n = 0;
+    return swr_internal_device(&dev, &n) == SWR_OK ? n : 148;
+}
 
 extern "C" {
 

@@ -92,12 +92,7 @@ struct swr_batch_t {
 
 namespace {
 
-int sm_count() {
-    int dev = 0, n = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    return n > 0 ? n : 148;
-}
+int sm_count() { return swr_internal_sm_count(); }
 
 swr_status upload_views(swr_batch b, const swr_view_desc* views) {
     std::vector<ViewParams> vp(b->numViews);

@@ -158,6 +158,11 @@ void launch_detile(const uint32_t* src, uint32_t* dst, uint32_t width, uint32_t 
 swr_status swr_internal_fail(swr_status code, const char* msg);
 swr_status swr_internal_cuda_fail(cudaError_t e, const char* what);
 cudaStream_t swr_internal_stream();
+// The current device and its SM count (queried once per device, then cached). Returns SWR_ECUDA
+// with the message set if either query fails.
+swr_status swr_internal_device(int* dev, int* sms);
+// SM count of the current device, 148 if the query fails (launch sizing only).
+int swr_internal_sm_count();
 // Profiling on/off for this thread (returns the previous state) and extra launches to count
 // (kernels replayed inside a CUDA graph).
 bool swr_internal_set_profiling(bool on);

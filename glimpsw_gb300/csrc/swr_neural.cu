@@ -204,7 +204,7 @@ __device__ __forceinline__ void load_latent_f16(const uint16_t* L, const Taps& q
 // Synchronise the CTA (publishing its shared-memory operand writes to the tensor cores), let
 // thread 0 issue `issue()` and commit, and wait for completion. Returns the CTA-uniform status.
 template <class F>
-__device__ __forceinline__ bool tc_round(bool ok, uint64_t* bar, uint32_t& phase, F&& issue) {
+__device__ __forceinline__ bool tc_round(bool ok, uint64_t* bar, uint32_t& phase, uint64_t limitNs, F&& issue) {
     fence_proxy_async();
     fence_before_sync();
     ok = __syncthreads_and(ok);
@@ -214,7 +214,7 @@ __device__ __forceinline__ bool tc_round(bool ok, uint64_t* bar, uint32_t& phase
         issue();
         mma_commit(bar);
     }
-    ok = mbar_wait(bar, phase);
+    ok = mbar_wait_drained(bar, phase, limitNs);
     phase ^= 1;
     ok = __syncthreads_and(ok);  // every thread leaves with the same verdict
     fence_after_sync();
@@ -259,7 +259,7 @@ __global__ void __launch_bounds__(128) k_neural_train(const __grid_constant__ Ne
     const uint32_t tmem = *tmemSlot;
     const uint32_t tRow = tmem + ((warp * 32) << 16);
     const uint32_t sb = smem_u32(sm);
-    bool ok = mbar_wait(barLoad, 0);
+    bool ok = mbar_wait_drained(barLoad, 0, a.n.waitNs);
     uint32_t phase = 0;
     float lossAcc = 0.f;
     const float* b2 = (const float*)(sm + kIB2);
@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(128) k_neural_train(const __grid_constant__ Ne
             store_row8(sm + kSQ, 128, 9, t, li);  // X0 columns 8-15
         }
         // ---- layer 1
-        ok = tc_round(ok, barMma, phase, [&] {
+        ok = tc_round(ok, barMma, phase, a.n.waitNs, [&] {
             mma_bf16(tmem + kT0, desc_kmajor(sb + kSQ + 8 * kSlab, 128), desc_kmajor(sb + kIW1, 64), iFwd128x64, 0);
         });
         float z1[64];
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(128) k_neural_train(const __grid_constant__ Ne
             store_row8(sm + kSQ, 128, s, t, h);
         }
         // ---- layer 2
-        ok = tc_round(ok, barMma, phase, [&] {
+        ok = tc_round(ok, barMma, phase, a.n.waitNs, [&] {
 #pragma unroll
             for (uint32_t k = 0; k < 4; k++)
                 mma_bf16(tmem + kT0, desc_kmajor(sb + kSQ + 2 * k * kSlab, 128), desc_kmajor(sb + kIW2 + 2 * k * 1024, 64),
@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(128) k_neural_train(const __grid_constant__ Ne
             store_row8(sm + kSR, 128, s, t, h);
         }
         // ---- layer 3 and the loss gradient
-        ok = tc_round(ok, barMma, phase, [&] {
+        ok = tc_round(ok, barMma, phase, a.n.waitNs, [&] {
 #pragma unroll
             for (uint32_t k = 0; k < 4; k++)
                 mma_bf16(tmem + kT0, desc_kmajor(sb + kSR + 2 * k * kSlab, 128), desc_kmajor(sb + kIW3 + 2 * k * 256, 16),
@@ -340,7 +340,7 @@ __global__ void __launch_bounds__(128) k_neural_train(const __grid_constant__ Ne
             store_row8(sm + kSP, 128, 0, t, dy);
         }
         // ---- dh2 = (DY W3) * gelu'(z2)
-        ok = tc_round(ok, barMma, phase, [&] {
+        ok = tc_round(ok, barMma, phase, a.n.waitNs, [&] {
             mma_bf16(tmem + kT0, desc_kmajor(sb + kSP, 128), desc_kmajor(sb + kIW3t, 64), iFwd128x64, 0);
         });
 #pragma unroll
@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(128) k_neural_train(const __grid_constant__ Ne
             store_row8(sm + kSP, 128, 3 + 2 * c, t, v + 8);
         }
         // ---- dh1 = (DH2 W2) * gelu'(z1)
-        ok = tc_round(ok, barMma, phase, [&] {
+        ok = tc_round(ok, barMma, phase, a.n.waitNs, [&] {
 #pragma unroll
             for (uint32_t k = 0; k < 4; k++)
                 mma_bf16(tmem + kT0, desc_kmajor(sb + kSP + (2 + 2 * k) * kSlab, 128),
@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(128) k_neural_train(const __grid_constant__ Ne
         }
         // ---- dx0 = DH1 W1, and the weight-gradient accumulators
         const uint32_t acc = tile > tBegin ? 1u : 0u;
-        ok = tc_round(ok, barMma, phase, [&] {
+        ok = tc_round(ok, barMma, phase, a.n.waitNs, [&] {
 #pragma unroll
             for (uint32_t k = 0; k < 4; k++)
                 mma_bf16(tmem + kT0, desc_kmajor(sb + kSP + (10 + 2 * k) * kSlab, 128),
@@ -623,7 +623,7 @@ __global__ void __launch_bounds__(128) k_neural_decode(const __grid_constant__ N
                 mbar_arrive_expect_tx(barLoad, kNeuralFwdImage);
                 bulk_g2s(sm, a.n.image + (size_t)mat * kNeuralImage, kNeuralFwdImage, barLoad);
             }
-            ok = mbar_wait(barLoad, loadPhase) && ok;
+            ok = mbar_wait_drained(barLoad, loadPhase, a.n.waitNs) && ok;
             loadPhase ^= 1;
             loaded = mat;
         }
@@ -644,7 +644,7 @@ __global__ void __launch_bounds__(128) k_neural_decode(const __grid_constant__ N
             level_inputs(smp.level, li);
             store_row8(sm + kDX, 128, 1, t, li);
         }
-        ok = tc_round(ok, barMma, phase, [&] {
+        ok = tc_round(ok, barMma, phase, a.n.waitNs, [&] {
             mma_bf16(tmem, desc_kmajor(sb + kDX, 128), desc_kmajor(sb + kIW1, 64), i64, 0);
         });
 #pragma unroll
@@ -656,7 +656,7 @@ __global__ void __launch_bounds__(128) k_neural_decode(const __grid_constant__ N
             store_row8(sm + kDH1, 128, 2 * c, t, v);
             store_row8(sm + kDH1, 128, 2 * c + 1, t, v + 8);
         }
-        ok = tc_round(ok, barMma, phase, [&] {
+        ok = tc_round(ok, barMma, phase, a.n.waitNs, [&] {
 #pragma unroll
             for (uint32_t k = 0; k < 4; k++)
                 mma_bf16(tmem, desc_kmajor(sb + kDH1 + 2 * k * kSlab, 128), desc_kmajor(sb + kIW2 + 2 * k * 1024, 64), i64, k);
@@ -670,7 +670,7 @@ __global__ void __launch_bounds__(128) k_neural_decode(const __grid_constant__ N
             store_row8(sm + kDH2, 128, 2 * c, t, v);
             store_row8(sm + kDH2, 128, 2 * c + 1, t, v + 8);
         }
-        ok = tc_round(ok, barMma, phase, [&] {
+        ok = tc_round(ok, barMma, phase, a.n.waitNs, [&] {
 #pragma unroll
             for (uint32_t k = 0; k < 4; k++)
                 mma_bf16(tmem, desc_kmajor(sb + kDH2 + 2 * k * kSlab, 128), desc_kmajor(sb + kIW3 + 2 * k * 256, 16), i16, k);
@@ -787,6 +787,40 @@ void launch_neural_decode(const NeuralDecodeArgs& a, uint32_t blocks, cudaStream
     neural_decode_blocks_per_sm();
     k_neural_decode<<<blocks, 128, kDecodeSmem, st>>>(a);
 }
+// The bounded-wait path on demand (see launch_wait_selftest): an mbarrier armed with expect_tx for a
+// copy that is never issued, so only the time limit can end the wait. The CTA holds TMEM while it
+// waits, as the decoder's CTAs do, and frees it on the way out.
+__global__ void __launch_bounds__(128) k_wait_selftest(uint32_t* status, uint64_t limitNs) {
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ uint32_t tmemSlot;
+    const uint32_t warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    if (warp == 0) {
+        tmem_alloc(&tmemSlot, 32);
+        tmem_relinquish();
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    bool ok = true;
+    if (threadIdx.x == 0) {
+        mbar_arrive_expect_tx(&bar, 16);  // the one arrival, with 16 bytes that never come
+        ok = mbar_wait(&bar, 0, limitNs);
+        if (!ok) atomicOr(status, 1u);
+    }
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+    if (warp == 0) tmem_dealloc(tmemSlot, 32);
+}
+
+void launch_wait_selftest(uint32_t* status, uint64_t limitNs, cudaStream_t st) {
+    k_wait_selftest<<<1, 128, 0, st>>>(status, limitNs);
+}
+
 void launch_neural_image(float* params, uint8_t* image, uint32_t numMaterials, cudaStream_t st) {
     k_neural_image<<<numMaterials, 256, 0, st>>>(params, image);
 }

@@ -40,6 +40,7 @@ struct NeuralDev {
     const DevTexture* tex;                      // per material (layer 0 RGBA, layer 1 NX NY M R)
     const uint16_t* latentHalf;                 // FP16 [material][texel][8]
     const uint8_t* image;                       // [material][kNeuralImage]
+    uint64_t waitNs;                            // limit of each bounded tensor-core / copy wait
 };
 
 struct NeuralTrainArgs {
@@ -90,6 +91,9 @@ uint32_t neural_decode_blocks_per_sm();  // resident decode CTAs per SM (shared 
 void launch_neural_image(float* params, uint8_t* image, uint32_t numMaterials, cudaStream_t st);
 void launch_neural_latent_init(const NeuralDev& n, float* latent, cudaStream_t st);
 void launch_neural_export(const float* latent, uint16_t* half, size_t count, cudaStream_t st);
+// One CTA announces a 16-byte copy on an mbarrier and issues none, waits at most limitNs with TMEM
+// allocated, then frees the TMEM and sets status bit 0 if the wait gave up.
+void launch_wait_selftest(uint32_t* status, uint64_t limitNs, cudaStream_t st);
 void launch_neural_offsets(const uint32_t* counts, uint32_t* reqOffset, uint32_t* tileOffset, uint32_t numMaterials,
                            cudaStream_t st);
 void launch_neural_scatter(const unsigned long long* pixelReq, uint32_t slots, const uint32_t* reqOffset,

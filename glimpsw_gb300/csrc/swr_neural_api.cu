@@ -14,16 +14,9 @@ using namespace swr;
 
 namespace {
 
-int num_sms() {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 1;
-    }
-    return n;
-}
+int num_sms() { return swr_internal_sm_count(); }
+
+constexpr uint64_t kDefaultWaitNs = 1000000000ull;  // 1 s per bounded wait
 
 uint64_t splitmix64(uint64_t& s) {
     uint64_t z = (s += 0x9E3779B97F4A7C15ull);
@@ -195,6 +188,7 @@ swr_status swr_neural_create(const swr_texture* textures, uint32_t num_materials
     n->d.tex = n->tex;
     n->d.latentHalf = n->latentHalf;
     n->d.image = n->image;
+    n->d.waitNs = kDefaultWaitNs;
     if (e == cudaSuccess) {
         {
             LaunchScope ls("k_neural_image", st);
@@ -213,6 +207,36 @@ swr_status swr_neural_create(const swr_texture* textures, uint32_t num_materials
         return swr_internal_cuda_fail(e, "swr_neural_create");
     }
     *out = n;
+    return SWR_OK;
+}
+
+swr_status swr_neural_set_wait_limit(swr_neural n, uint64_t limit_ns) {
+    if (!n) return swr_internal_fail(SWR_EINVAL, "swr_neural_set_wait_limit: NULL handle");
+    if (limit_ns == 0 || limit_ns > 60000000000ull)
+        return swr_internal_fail(SWR_EINVAL, "swr_neural_set_wait_limit: the limit must be 1 ns to 60 s");
+    n->d.waitNs = limit_ns;
+    return SWR_OK;
+}
+
+swr_status swr_selftest_bounded_wait(uint64_t limit_ns) {
+    if (limit_ns == 0 || limit_ns > 1000000000ull)
+        return swr_internal_fail(SWR_EINVAL, "swr_selftest_bounded_wait: the limit must be 1 ns to 1 s");
+    cudaStream_t st = swr_internal_stream();
+    uint32_t* status = nullptr;
+    cudaError_t e = cudaMalloc(&status, sizeof(uint32_t));
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_selftest_bounded_wait: status word");
+    uint32_t s = 0;
+    e = cudaMemsetAsync(status, 0, sizeof(uint32_t), st);
+    if (e == cudaSuccess) {
+        LaunchScope ls("k_wait_selftest", st);
+        launch_wait_selftest(status, limit_ns, st);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&s, status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    cudaFree(status);
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_selftest_bounded_wait");
+    if (s & 1u) return swr_internal_fail(SWR_ETIMEOUT, "swr_selftest_bounded_wait: the wait gave up at its limit");
     return SWR_OK;
 }
 

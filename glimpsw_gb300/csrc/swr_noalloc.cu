@@ -7,6 +7,7 @@
 // outputs and keeps its working memory (vis-buffer keys, the large-triangle queue, control
 // words and expanded material records) in one file-scope device array of fixed size, so the
 // call itself allocates nothing. It reuses the regular draw kernels unchanged.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -35,27 +36,64 @@ constexpr size_t kNoAllocBytes = kOffKeys + (size_t)kNoAllocMaxPixels * sizeof(u
 static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocBytes];
 
 // In host code g_noallocScratch names a host-side stand-in, not device memory: the device address
-// is looked up once per device with that device current and cached here.
-std::mutex g_mu;
-unsigned char* g_scratch[64] = {};
+// is looked up with the device current and cached per device, together with the identity of the
+// context it was looked up in. A cudaDeviceReset ends that context; the next call sees a new
+// context and looks the address up again.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
 
-swr_status scratch_for_current_device(unsigned char** out) {
+// Identity of the calling thread's current context (0 if none is current or the driver does not
+// tell; the address is then looked up at every call).
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn getCurrent = nullptr;
+    static CtxGetIdFn getId = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            getCurrent = (CtxGetCurrentFn)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            getId = (CtxGetIdFn)f;
+    });
+    CUcontext c = nullptr;
+    unsigned long long id = 0;
+    if (!getCurrent || !getId || getCurrent(&c) != CUDA_SUCCESS || !c || getId(c, &id) != CUDA_SUCCESS) return 0;
+    return id + 1;
+}
+
+struct DeviceScratch {
+    unsigned char* ptr;
+    unsigned long long context;
+};
+std::mutex g_mu;
+DeviceScratch g_scratch[64] = {};
+
+// The working array's device address and the SM count of the current device.
+swr_status scratch_for_current_device(unsigned char** out, int* sms) {
     int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_draw_meshlets_noalloc: cudaGetDevice");
-    if (dev < 0 || dev >= 64) return swr_internal_fail(SWR_EINVAL, "swr_draw_meshlets_noalloc: device ordinal above 63");
+    swr_status st = swr_internal_device(&dev, sms);
+    if (st != SWR_OK) return st;
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_scratch[dev]) {
+    DeviceScratch& d = g_scratch[dev];
+    const unsigned long long ctx = current_context_id();
+    if (!d.ptr || ctx == 0 || ctx != d.context) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noallocScratch);
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
         if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_draw_meshlets_noalloc: cudaGetSymbolAddress");
-        g_scratch[dev] = (unsigned char*)p;
+        d.ptr = (unsigned char*)p;
+        d.context = current_context_id();  // the lookup made the context current if none was
     }
-    *out = g_scratch[dev];
+    *out = d.ptr;
     return SWR_OK;
 }
 
-// Material records for the draw kernel from one flag byte per material (bit 0: double-sided).
+// Material records for the draw kernel from one flag byte per material (bit 0: double-sided; the
+// other bits are reserved). The entry point takes no textures, so no material is alpha-tested: every
+// meshlet draws with the opaque shader, FragmentShaderId 0.
 __global__ void k_expand_material_flags(const uint8_t* __restrict__ flags, uint32_t n, DevMaterial* __restrict__ out) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         DevMaterial m = {};
@@ -89,7 +127,8 @@ extern "C" swr_status swr_draw_meshlets_noalloc(const void* meshlets, uint32_t m
     if (count == 0) return SWR_OK;
 
     unsigned char* base = nullptr;
-    swr_status st = scratch_for_current_device(&base);
+    int sms = 0;
+    swr_status st = scratch_for_current_device(&base, &sms);
     if (st != SWR_OK) return st;
     cudaStream_t stream = swr_internal_stream();
     const uint32_t n = width * height;
@@ -106,9 +145,6 @@ extern "C" swr_status swr_draw_meshlets_noalloc(const void* meshlets, uint32_t m
     }
     launch_init_keys((const uint32_t*)depth, keys, nullptr, n, stream);
 
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     DrawArgs a = {};
     a.meshlets = (const uint8_t*)meshlets;
     a.materials = mats;
@@ -129,7 +165,7 @@ extern "C" swr_status swr_draw_meshlets_noalloc(const void* meshlets, uint32_t m
     a.s.big = (TriRec*)(base + kOffQueue);
     a.s.bigBase = (unsigned long long*)(base + kOffBases);
     a.s.bigCapacity = kNoAllocQueue;
-    launch_draw(a, stream, sms > 0 ? sms : 148);
+    launch_draw(a, stream, sms);
     launch_finalize(keys, surface_ids, (uint32_t*)depth, n, stream);
     e = cudaGetLastError();
     if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_draw_meshlets_noalloc");

@@ -24,6 +24,7 @@
 // the triangle cannot win anywhere is skipped. The vis-buffer is unchanged (only fragments that
 // would fail the depth test are skipped), while the dense scenes' overdraw mostly disappears.
 #include <cfloat>
+#include <mutex>
 #include <numeric>
 #include <type_traits>
 
@@ -1337,6 +1338,20 @@ uint32_t order_stride(uint32_t count) {
     return s % count;
 }
 
+// The dynamic shared memory limit of a mesh-stage pass is an attribute of the kernel in one
+// device's context: it is raised per device (and only when a larger size is needed), under a lock
+// because draws may come from several host threads.
+static void raise_smem_limit(int pass, const void* kernel, size_t bytes) {
+    static std::mutex mu;
+    static size_t setSize[64][3] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+    std::lock_guard<std::mutex> lock(mu);
+    if (bytes <= setSize[dev][pass]) return;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) == cudaSuccess)
+        setSize[dev][pass] = bytes;
+}
+
 void launch_draw(const DrawArgs& args, cudaStream_t st, int numSMs) {
     DrawArgs a = args;
     if (!a.views) {
@@ -1348,20 +1363,11 @@ void launch_draw(const DrawArgs& args, cudaStream_t st, int numSMs) {
     }
     const uint32_t warps = a.warpsPerBlock ? a.warpsPerBlock : kWarpsPerBlock;
     const size_t smem = warps * sizeof(WarpSmem), smemAlpha = warps * sizeof(WarpSmemAlpha);
-    static size_t s_smemSet = 0, s_smemSetAlpha = 0;
-    static size_t s_smemSetOver = 0;
-    if (smem > 48 * 1024) {
-        size_t& set = a.counts ? s_smemSetOver : s_smemSet;
-        if (smem > set) {
-            cudaFuncSetAttribute(a.counts ? k_draw_meshlets<kPassOverdraw> : k_draw_meshlets<kPassOpaque>,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            set = smem;
-        }
-    }
-    if (a.s.alphaList && smemAlpha > s_smemSetAlpha && smemAlpha > 48 * 1024) {
-        cudaFuncSetAttribute(k_draw_meshlets<kPassAlpha>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smemAlpha);
-        s_smemSetAlpha = smemAlpha;
-    }
+    if (smem > 48 * 1024)
+        raise_smem_limit(a.counts ? kPassOverdraw : kPassOpaque,
+                         a.counts ? (const void*)k_draw_meshlets<kPassOverdraw> : (const void*)k_draw_meshlets<kPassOpaque>,
+                         smem);
+    if (a.s.alphaList && smemAlpha > 48 * 1024) raise_smem_limit(kPassAlpha, (const void*)k_draw_meshlets<kPassAlpha>, smemAlpha);
     const uint32_t chunk = a.chunkTiles ? a.chunkTiles : kChunkTiles;
     const int grid = numSMs * (32 / warps);  // 64 registers a thread leave room for 32 resident warps per SM
     if (a.counts) {  // OverdrawShader: one pass, every meshlet

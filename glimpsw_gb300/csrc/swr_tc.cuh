@@ -60,6 +60,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint64
     }
 }
 
+// The wait of a copy or MMA that was issued: when it gives up after limit_ns, the operation is still
+// in flight and would land in shared memory or TMEM the CTA is about to release, so this waits for
+// the phase once more (at most one further second) before returning false.
+__device__ __forceinline__ bool mbar_wait_drained(uint64_t* bar, uint32_t parity, uint64_t limit_ns) {
+    if (mbar_wait(bar, parity, limit_ns)) return true;
+    mbar_wait(bar, parity, 1000000000ull);
+    return false;
+}
+
 // ---------------------------------------------------------------------------- bulk copies
 // global -> shared, completion counted in bytes on `bar` (addresses 16-byte aligned, size % 16 == 0)
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {

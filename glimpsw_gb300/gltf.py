@@ -458,19 +458,22 @@ def load(path: str, lib=None) -> Model:
 
 
 def _light(ld, g):
-    """Light::SetRadius / SetSpotAngles (Scene.h:65-75) of a KHR_lights_punctual light."""
+    """Light::SetRadius / SetSpotAngles (Scene.h:65-75) of a KHR_lights_punctual light, in float32 as
+    the reference computes them."""
+    f = np.float32
     kind = {"directional": 0, "point": 1, "spot": 2}[ld["type"]]
-    radius = float(ld.get("range", 0.0))
-    radius = radius if radius > 0 else 1e6
+    radius = f(ld.get("range", 0.0))
+    radius = radius if radius > 0 else f(1e6)
     spot = ld.get("spot", {})
-    inner, outer = float(spot.get("innerConeAngle", 0.0)), float(spot.get("outerConeAngle", math.pi / 4))
-    scale = 1.0 / max(math.cos(inner) - math.cos(outer), 1e-4)
+    inner, outer = f(spot.get("innerConeAngle", 0.0)), f(spot.get("outerConeAngle", math.pi / 4))
+    scale = f(1.0) / max(np.cos(inner) - np.cos(outer), f(1e-4))
     d = -g[:3, 2]
     d = d / max(np.linalg.norm(d), 1e-30)
     return {"type": kind, "position": g[:3, 3].astype(np.float32), "direction": d.astype(np.float32),
             "color": np.array(ld.get("color", [1, 1, 1]), np.float32), "intensity": float(ld.get("intensity", 1.0)),
-            "radius": radius, "spot_inner": inner, "spot_outer": outer, "inv_radius_sq": 1.0 / (radius * radius),
-            "spot_scale": scale, "spot_offset": -math.cos(outer) * scale}
+            "radius": float(radius), "spot_inner": float(inner), "spot_outer": float(outer),
+            "inv_radius_sq": float(f(1.0) / (radius * radius)), "spot_scale": float(scale),
+            "spot_offset": float(-np.cos(outer) * scale)}
 
 
 # ----------------------------------------------------------------------------- device upload / draw

@@ -150,14 +150,18 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
  * cannot allocate device memory (their memory belongs to another allocator, or they run where
  * cudaMalloc is not allowed): every input and output is a caller-owned device pointer and the call
  * allocates nothing. meshlets: Meshlet records (device); material_flags: one byte per material,
- * bit 0 = double-sided (device, or NULL with num_materials 0); cull_bitmap as in
+ * bit 0 = double-sided, other bits reserved (device, or NULL with num_materials 0). It takes no
+ * textures, so materials are never alpha-tested: every meshlet draws with the opaque shader
+ * (FragmentShaderId 0), where swr_draw_meshlets would alpha-test the meshlets of a material with
+ * alpha_cutoff < 255 and a texture. cull_bitmap as in
  * swr_shading_context; object_to_clip: host. surface_ids and depth are the framebuffer's layers 0
  * and 1 in the 4x4-tiled layout (width*height words each, device): they are read for the depth
  * test and updated like the layers of a framebuffer. Limits: width*height <= 1048576 pixels and
  * at most 1024 materials, else SWR_ECAPACITY. Working memory is one fixed device array (about
  * 9.3 MiB, held by every GPU that loads the library until the process exits), shared by every
  * call: calls whose work overlaps on the GPU race, so serialise them (one stream). The first call
- * on each device looks up that array's device address; make it before any stream capture. */
+ * on each device (and the first after a cudaDeviceReset) looks up that array's device address; make
+ * it before any stream capture. */
 swr_status swr_draw_meshlets_noalloc(const void* meshlets, uint32_t meshlet_offset, uint32_t count,
                                      const uint8_t* material_flags, uint32_t num_materials,
                                      const uint16_t* cull_bitmap, const float object_to_clip[16],
@@ -332,6 +336,14 @@ swr_status swr_neural_set_latents(swr_neural n, uint32_t material, const float* 
  * (2 words per texel: layer-0 RGBA8 with AO in alpha, layer-1 RGBA8). */
 swr_status swr_neural_decode(swr_neural n, uint32_t material, const uint32_t* texels_device, uint32_t count,
                              uint32_t* out_device);
+/* Time limit of each bounded device-side wait of the model's kernels (copy and tensor-core
+ * completion; default 1 s, 1 ns to 60 s). A wait that reaches it makes the call return
+ * SWR_ETIMEOUT; the kernel first lets the operation it waited for land, then frees its TMEM. */
+swr_status swr_neural_set_wait_limit(swr_neural n, uint64_t limit_ns);
+/* Exercises the bounded-wait path on the device: one CTA allocates TMEM, arms an mbarrier for a
+ * 16-byte copy that is never issued and waits at most limit_ns (1 ns to 1 s); the wait gives up,
+ * the CTA frees its TMEM and exits, and the call returns SWR_ETIMEOUT. The context stays usable. */
+swr_status swr_selftest_bounded_wait(uint64_t limit_ns);
 /* swr_resolve with the texture levels below latent_levels decoded by the model (the scene's
  * material i must use the model's texture i); stats may be NULL (else the stream is synchronised). */
 swr_status swr_resolve_neural(swr_rasterizer r, swr_framebuffer fb, const swr_shading_context* ctx, swr_neural n,

@@ -1,6 +1,8 @@
 """Shared test helpers: render a scene with the CUDA library and with the CPU oracle."""
 from __future__ import annotations
 
+import math
+
 import numpy as np
 
 from glimpsw_gb300 import scenes
@@ -95,6 +97,37 @@ def default_lights() -> np.ndarray:
     lights["color"] = 1.0
     lights["intensity"] = 1500.0
     return lights
+
+
+def make_light(kind: int, position=(0.0, 0.0, 0.0), direction=(0.0, 0.0, 1.0), color=(1.0, 1.0, 1.0),
+               intensity: float = 1.0, radius: float = 0.0, inner: float = 0.0, outer: float = math.pi / 4) -> np.ndarray:
+    """One light record as the reference builds it (Scene.h:52-75): a normalised direction, then
+    Light::SetRadius (0 or less: 1e6) and Light::SetSpotAngles in float32."""
+    f = np.float32
+    li = np.zeros(1, dtype=LIGHT_DTYPE)
+    li["type"] = kind
+    li["position"] = np.asarray(position, f)
+    d = np.asarray(direction, f)
+    li["direction"] = (d * f(1.0 / np.sqrt(np.float64((d * d).sum())))).astype(f)
+    li["color"] = np.asarray(color, f)
+    li["intensity"] = f(intensity)
+    r = f(radius) if radius > 0 else f(1e6)
+    li["radius"] = r
+    li["inv_radius_sq"] = f(1.0) / (r * r)
+    li["spot_inner"], li["spot_outer"] = f(inner), f(outer)
+    scale = f(1.0) / max(np.cos(f(inner)) - np.cos(f(outer)), f(1e-4))
+    li["spot_scale"] = scale
+    li["spot_offset"] = -np.cos(f(outer)) * scale
+    return li
+
+
+def model_lights(model) -> np.ndarray:
+    """An imported glTF model's KHR_lights_punctual lights (gltf.Model.lights) as light records."""
+    out = np.zeros(len(model.lights), dtype=LIGHT_DTYPE)
+    for i, li in enumerate(model.lights):
+        for k in LIGHT_DTYPE.names:
+            out[k][i] = li[k]
+    return out
 
 
 def gpu_lights(lights: np.ndarray):

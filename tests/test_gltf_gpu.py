@@ -1,12 +1,13 @@
 """An imported glTF model drawn on the GPU through gltf.upload / gltf.draw against the oracle fed
 the same meshlets, instance by instance: the vis-buffer bit for bit (the plane's material is
-alpha-masked, so the alpha pass runs with the model's own texcoords) and the resolve within 1/255."""
+alpha-masked, so the alpha pass runs with the model's own texcoords) and the resolve within 1/255,
+lit by the frame driver's default light and the model's own point light."""
 import numpy as np
 import pytest
 
 from glimpsw_gb300 import gltf, scenes
 from tests import gltf_fixtures
-from tests.helpers import TexturePair, assert_visbuffer_equal, default_lights, gpu_lights
+from tests.helpers import TexturePair, assert_visbuffer_equal, default_lights, gpu_lights, model_lights
 
 pytestmark = pytest.mark.gpu
 
@@ -16,6 +17,8 @@ def test_imported_model_matches_oracle(tmp_path):
     from oracle import oracle as O
     m = gltf.load(gltf_fixtures.build(str(tmp_path))[1])
     assert not m.warnings
+    lights = np.concatenate([default_lights(), model_lights(m)])
+    assert len(m.lights) == 1 and int(lights["type"][1]) == 1
     scene, texs = gltf.upload(m)
     otex = [TexturePair(layers, layers[0].shape[0], gpu=False) for layers in m.textures]
     rast = api.Rasterizer()
@@ -39,10 +42,10 @@ def test_imported_model_matches_oracle(tmp_path):
         assert (ids != 0xFF000000).sum() > 3000
         # resolve (one instance's object transform is the reference frame driver's choice: identity)
         octx = O.Context(m.meshlets, m.materials, v.world_to_clip, world_to_clip=v.world_to_clip,
-                         textures=[t.o for t in otex], lights=default_lights(), view_pos=v.eye)
+                         textures=[t.o for t in otex], lights=lights, view_pos=v.eye)
         O.resolve(ofb, octx, threads=8)
         gctx = api.ShadingContext(scene, v.world_to_clip, world_to_clip=v.world_to_clip, view_pos=v.eye,
-                                  lights=gpu_lights(default_lights()))
+                                  lights=gpu_lights(lights))
         gctx.resolve(rast, fb)
         a = fb.get_pixels(0).view(np.uint8).astype(np.int32)
         b = ofb.get_pixels(0).view(np.uint8).astype(np.int32)

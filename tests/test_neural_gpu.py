@@ -4,10 +4,11 @@
   quantisation, within one step (BF16 activations may round differently when the FP32 tensor-core
   sums or tanh.approx differ from the oracle's float64 by a rounding boundary);
 * gradients: parameter and latent gradients of the training kernel for explicit samples within
-  1e-2 relative (L2) of the oracle's backward pass on the same BF16 operands;
+  2e-3 relative (L2) of the oracle's backward pass on the same BF16 operands;
 * training: the loss falls; the texture levels decoded 1:1 from their latent level come back
   within a few unorm8 steps, and the magnified levels 0 and 1 beat the plain texture at the
-  latent grid's resolution (texture level 2) magnified bilinearly in PSNR;
+  latent grid's resolution (texture level 2) magnified bilinearly by at least 2 dB of PSNR;
+* bounded waits: a wait that nothing completes returns SWR_ETIMEOUT and leaves the context usable;
 * resolve: with a model whose network outputs each material's constant texel the neural resolve
   equals the plain resolve bit for bit (every pixel finds its decoded texels), and with a trained
   model its colours stay close to the plain resolve.
@@ -108,10 +109,10 @@ def test_model_layout_and_memory(model):
     assert lat[5 * 32 + 3, 7] == 0
 
 
-def test_decode_matches_oracle(model):
-    m, _, _ = model
-    rng = np.random.default_rng(1)
-    mat = 2
+def _check_decode(m, seed=1, mat=2):
+    """Random latents and parameters for one material, then 3000 texels of every decoded level:
+    the inference kernel against the oracle's forward pass."""
+    rng = np.random.default_rng(seed)
     lat = rng.normal(0, 0.8, (m.texels_per_material, 8)).astype(np.float32)
     m.set_latents(mat, lat)
     params = m.get_params(mat)
@@ -128,6 +129,32 @@ def test_decode_matches_oracle(model):
     assert len(np.unique(exp[:, 0])) > 20  # the check is not vacuous
     for l in range(DECODED):
         assert (lvl == l).sum() > 10
+
+
+def test_decode_matches_oracle(model):
+    _check_decode(model[0])
+
+
+def test_bounded_wait_times_out_and_context_stays_usable(model):
+    """A device wait that nothing completes (an mbarrier armed for a copy that is never issued,
+    with TMEM held) gives up at its limit and the call returns SWR_ETIMEOUT; the CTA frees its
+    TMEM and exits, so the next kernels run normally: a decode with a host-set wait limit still
+    matches the oracle."""
+    api = _setup_stream()
+    lib = api.load_library()
+    for limit_ns in (1000, 1, 2_000_000):
+        st = lib.swr_selftest_bounded_wait(limit_ns)
+        assert st == api.SWR_ETIMEOUT, lib.swr_last_error().decode()
+        assert "gave up" in lib.swr_last_error().decode()
+    assert lib.swr_selftest_bounded_wait(0) == api.SWR_EINVAL
+    m = model[0]
+    with pytest.raises(Exception):
+        m.set_wait_limit(0)
+    m.set_wait_limit(50_000_000)  # 50 ms per wait
+    try:
+        _check_decode(m, seed=3)
+    finally:
+        m.set_wait_limit(1_000_000_000)
 
 
 def test_gradients_match_oracle(model):
@@ -160,11 +187,11 @@ def test_gradients_match_oracle(model):
             a, b = view(a), view(b)
         rel = np.linalg.norm(a - b) / np.linalg.norm(b)
         print(f"{name}: rel L2 error {rel:.2e}")
-        assert rel < 1e-2, name
+        assert rel < 2e-3, name
     assert np.all(pg[N.PW1:N.PW2].reshape(64, 16)[:, 11:] == 0)
     rel = np.linalg.norm(lg - lgo) / np.linalg.norm(lgo)
     print(f"latent: rel L2 error {rel:.2e}")
-    assert rel < 1e-2
+    assert rel < 2e-3
     assert np.count_nonzero(np.abs(lgo).sum(1)) == np.count_nonzero(np.abs(lg).sum(1))
 
 
@@ -210,7 +237,7 @@ def test_training_decodes_and_beats_plain_magnification():
           f"{one_to_one:.2f} dB, levels 0-1 {magnified:.2f} dB vs plain level 2 magnified {base:.2f} dB")
     assert loss1 < 0.25 * loss0
     assert one_to_one > 40.0
-    assert magnified > base + 0.5
+    assert magnified > base + 2.0
 
 
 def test_resolve_neural_constant_materials_equal_plain():

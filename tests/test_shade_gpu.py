@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from glimpsw_gb300 import scenes
-from tests.helpers import GpuRenderer, TexturePair, default_lights, gpu_lights, render_oracle
+from tests.helpers import LIGHT_DTYPE, GpuRenderer, TexturePair, default_lights, gpu_lights, make_light, render_oracle
 
 pytestmark = pytest.mark.gpu
 
@@ -108,6 +108,50 @@ def test_resolve_within_one_lsb(shaded):
     diff = np.abs(a - b)
     exact = (diff.max(axis=2) == 0).mean()
     print(f"resolve: max abs {diff.max()} / 255, exact pixels {exact:.6f}")
+    assert diff.max() <= 1
+    assert exact > 0.999
+
+
+def test_resolve_point_and_spot_lights_within_one_lsb(shaded):
+    """EvalLighting's loop over several lights with GetLightAttenuation's three branches
+    (Shading.cpp:581-645): one directional, two point and two spot lights with their own colours,
+    ranges and cone angles. Each light alone visibly changes the oracle's image (so every branch is
+    exercised), and the GPU resolve with all five is within 1/255 of the oracle's."""
+    from glimpsw_gb300 import api
+    from oracle import oracle as O
+    sc, texs, env, g = shaded
+    v = sc.views[0]
+    w, h = v.width, v.height
+    lights = np.concatenate([
+        make_light(0, direction=(0.3, -0.8, 0.5), color=(1.0, 0.85, 0.6), intensity=900.0),
+        make_light(1, position=(-8.0, 6.0, -30.0), color=(1.0, 0.45, 0.25), intensity=3.0e5, radius=45.0),
+        make_light(1, position=(12.0, -4.0, -18.0), color=(0.3, 0.6, 1.0), intensity=1.5e5, radius=30.0),
+        make_light(2, position=(0.0, 20.0, -50.0), direction=(0.0, -20.0, 20.0), color=(0.8, 1.0, 0.7),
+                   intensity=4.0e5, radius=100.0, inner=0.2, outer=0.6),
+        make_light(2, position=(5.0, -10.0, -50.0), direction=(-5.0, 10.0, 20.0), color=(1.0, 0.7, 0.9),
+                   intensity=4.0e5, radius=100.0, inner=0.25, outer=0.5),
+    ])
+
+    def oracle_image(ls):
+        ofb, _ = render_oracle(sc.meshlets, sc.materials, v.world_to_clip, w, h)
+        octx = O.Context(sc.meshlets, sc.materials, v.world_to_clip, world_to_clip=v.world_to_clip,
+                         textures=[t.o for t in texs], lights=ls, skybox=env.o, view_pos=v.eye)
+        O.resolve(ofb, octx, threads=8)
+        return ofb.get_pixels(0).view(np.uint8).reshape(h, w, 4).astype(np.int32)
+
+    ambient = oracle_image(np.zeros(0, dtype=LIGHT_DTYPE))
+    for i in range(len(lights)):
+        changed = (np.abs(oracle_image(lights[i:i + 1]) - ambient).max(axis=2) > 2).sum()
+        assert changed > 1000, f"light {i} changes only {changed} pixels"
+    ref = oracle_image(lights)
+    gfb, _ = g.render(v.world_to_clip, w, h)
+    gctx = api.ShadingContext(g.scene, v.world_to_clip, world_to_clip=v.world_to_clip, skybox=env.g, view_pos=v.eye,
+                              lights=gpu_lights(lights))
+    gctx.resolve(g.rast, gfb)
+    got = gfb.get_pixels(0).view(np.uint8).reshape(h, w, 4).astype(np.int32)
+    diff = np.abs(got - ref)
+    exact = (diff.max(axis=2) == 0).mean()
+    print(f"resolve, 5 lights: max abs {diff.max()} / 255, exact pixels {exact:.6f}")
     assert diff.max() <= 1
     assert exact > 0.999
 
