@@ -66,6 +66,7 @@ def parse():
     p.add_argument("--neural-width", type=int, default=2560)
     p.add_argument("--neural-height", type=int, default=1440)
     p.add_argument("--no-alpha", action="store_true")
+    p.add_argument("--no-cone", action="store_true")
     p.add_argument("--multiview-cameras", type=int, default=58,
                    help="cameras besides the 6 cube faces of the multi-view workload")
     p.add_argument("--only", default="all", choices=["all", "neural", "multiview"],
@@ -125,12 +126,20 @@ def make_gpu_textures(sc, api):
 
 # ----------------------------------------------------------------------------- CPU frame
 class OracleFrame:
-    """The same frame on the CPU oracle (test infrastructure, used here only as the timed baseline)."""
+    """The same frame on the CPU oracle (test infrastructure, used here only as the timed baseline),
+    in one of the reference's two rasterizer configurations:
+    - "binned": Rasterizer(threads) with binning (Rasterizer.cpp:493-820): meshlets strided over the
+      workers, 128x128 bins rasterized by their elected worker; the resolve's 4x4 tiles split over
+      the same threads (Rasterizer::Dispatch, Rasterizer.cpp:822-845);
+    - "unbinned1": Rasterizer(1) without binning (DrawMeshletsST, Rasterizer.cpp:153-254), the
+      shape of the reference's RasterBench (RasterBench.cpp:75-86): one thread does everything.
+    Culling and the Hi-Z build run on one thread, as the reference's frame driver calls them."""
 
-    def __init__(self, sc, tex_data, env_data, threads):
+    def __init__(self, sc, tex_data, env_data, threads, mode="binned"):
         from oracle import oracle as O
         from glimpsw_gb300 import scenes
-        self.O, self.sc, self.threads = O, sc, threads
+        self.O, self.sc, self.mode = O, sc, mode
+        self.threads = threads if mode == "binned" else 1
         v0, v1 = sc.views
         self.v0, self.v1 = v0, v1
         self.texs = []
@@ -150,7 +159,6 @@ class OracleFrame:
         lights["direction"], lights["color"], lights["intensity"] = default_lights(), 1.0, 1500.0
         self.lights = lights
         self.model = scenes.IDENTITY
-        self.frame(v0, v0, None, self.hiz_in)  # Hi-Z of the previous view
 
     def frame(self, view, prev, hiz_in, hiz_out):
         O, sc = self.O, self.sc
@@ -161,21 +169,52 @@ class OracleFrame:
             bm, _ = O.cull_meshlets(sc.meshlets[off:off + cnt], cnt, view.proj, view.view, self.model, prev.view,
                                     view.width, view.height, hiz_in)
             ctx = O.Context(sc.meshlets, sc.materials, view.world_to_clip, meshlet_offset=off, cull_bitmap=bm)
-            O.draw_meshlets(self.fb, ctx, cnt, binning=False, threads=self.threads)
+            if self.mode == "binned":
+                O.draw_meshlets_binned(self.fb, ctx, cnt, self.threads)
+            else:
+                O.draw_meshlets(self.fb, ctx, cnt, binning=False, threads=1)
         ctx = O.Context(sc.meshlets, sc.materials, view.world_to_clip, world_to_clip=view.world_to_clip,
                         textures=self.texs, lights=self.lights, skybox=self.env, view_pos=view.eye)
         O.resolve(self.fb, ctx, threads=self.threads)
         O.downsample_depth(self.fb, hiz_out)
 
-    def timed(self, budget_s, max_frames=50):
+    def timed(self, budget_s, max_frames=50, warmup=1):
+        """Median-ready frame times of the headline frame (no previous depth) after `warmup`
+        untimed frames, until budget_s seconds or max_frames frames."""
+        for _ in range(warmup):
+            self.frame(self.v0, self.v0, None, self.hiz_out)
         times = []
         t_end = time.perf_counter() + budget_s
         while True:
             t0 = time.perf_counter()
-            self.frame(self.v0, self.v0, None, self.hiz_out)  # the headline frame (no previous depth)
+            self.frame(self.v0, self.v0, None, self.hiz_out)
             times.append(time.perf_counter() - t0)
             if time.perf_counter() > t_end or len(times) >= max_frames:
                 return times
+
+
+def host_description():
+    import platform
+    try:
+        flags = open("/proc/cpuinfo").read()
+    except OSError:
+        flags = ""
+    return {"machine": platform.machine(), "cores": cpu_threads(), "avx512": "avx512f" in flags,
+            "note": "scalar C++ restatement of the reference's AVX-512 code (the reference needs clang vector "
+                    "extensions and cannot be built here)"}
+
+
+def cpu_baselines(sc, tex_data, env_data, steps, warmup, unbinned_seconds=10.0):
+    """Both reference configurations on this host's cores: the binned Rasterizer(threads) frame
+    (steps frames after warmup, the reported value) and a bounded sample of the one-thread
+    unbinned frame."""
+    threads = cpu_threads()
+    binned = OracleFrame(sc, tex_data, env_data, threads, "binned")
+    times = binned.timed(150.0, max_frames=steps, warmup=warmup)
+    single = OracleFrame(sc, tex_data, env_data, 1, "unbinned1")
+    t1 = single.timed(unbinned_seconds, max_frames=steps, warmup=0)
+    return {"binned_ms": float(np.median(times) * 1e3), "binned_frames": len(times), "threads": threads,
+            "unbinned_1_thread_ms": float(np.median(t1) * 1e3), "unbinned_frames": len(t1), "host": host_description()}
 
 
 def cpu_threads():
@@ -210,24 +249,31 @@ def run_reference(args):
     if rank != 0:
         return
     sc = build_scene(args)
-    threads = cpu_threads()
     tex_data, env_data = oracle_textures_from_host(sc)
-    of = OracleFrame(sc, tex_data, env_data, threads)
-    of.timed(0.0, 1)  # warm-up frame
-    times = []
-    for _ in range(args.steps):
-        times += of.timed(0.0, 1)
-        if sum(times) > 150:
-            break
-    ms = float(np.median(times) * 1e3)
-    line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": args.gpus, "steps": len(times),
-            "warmup": 1, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32+i32", "data": "synthetic (seeded)", "config": config_dict(args, sc),
-            "cpu_baseline": {"value": ms, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{len(times)} full frames (median); oracle restatement of the reference's CPU "
-                                       f"pipeline, draw and resolve rows split over {threads} threads"},
+    warmup = max(3, args.warmup)
+    b = cpu_baselines(sc, tex_data, env_data, args.steps, warmup)
+    ms = b["binned_ms"]
+    line = {"impl": "reference", "metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": b["binned_frames"], "warmup": warmup, "ms_per_step": ms, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+i32", "data": "synthetic (seeded)",
+            "config": config_dict(args, sc, {"parallelism": PARALLELISM}),
+            "cpu_baseline": cpu_baseline_entry(b),
             "e2e": {"value": ms, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+PARALLELISM = "replicas only (one GPU renders the frame)"
+
+
+def cpu_baseline_entry(b):
+    return {"value": b["binned_ms"], "unit": UNIT, "cores": b["threads"], "kind": "port",
+            "sample": f"{b['binned_frames']} full frames of the same workload (median) through the oracle's "
+                      f"restatement of Rasterizer({b['threads']}) with binning: meshlets strided over "
+                      f"{b['threads']} workers, 128x128 bins rasterized by their elected worker, resolve tiles "
+                      f"over the same threads",
+            "unbinned_1_thread": {"value": b["unbinned_1_thread_ms"], "unit": UNIT, "frames": b["unbinned_frames"],
+                                  "what": "Rasterizer(1) without binning (RasterBench's shape), one thread"},
+            "host": b["host"]}
 
 
 # ----------------------------------------------------------------------------- clocks
@@ -338,10 +384,18 @@ def multiview_section(args, api, stream):
 
     batched_ms = timed(batch.render, args.steps)
     per_view_ms = timed(per_view, args.steps)
+    # every view of the batch against its own per-view draw (the depth-only views hold depth alone)
     batch.reset_counters()
     batch.render()
     c = batch.counters()
+    batched_layers = [(fb.get_pixels(0) if not v.depth_only else None, fb.get_pixels(1)) for fb, v in zip(fbs, sc.views)]
+    per_view()
+    identical = 0
+    for (ids, depth), fb, v in zip(batched_layers, fbs, sc.views):
+        same = np.array_equal(depth, fb.get_pixels(1)) and (ids is None or np.array_equal(ids, fb.get_pixels(0)))
+        identical += int(same)
     return {"views": len(sc.views), "meshlets": n, "pixels": int(sum(v.width * v.height for v in sc.views)),
+            "views_bit_identical_to_per_view_draws": f"{identical}/{len(sc.views)}",
             "visible_meshlets_per_view": {"min": int(min(visible)), "max": int(max(visible)),
                                           "total": int(sum(visible))},
             "batched_ms": batched_ms, "per_view_ms": per_view_ms, "speedup": per_view_ms / batched_ms,
@@ -523,6 +577,77 @@ def alpha_section(args, api, stream, sc, texs, env, lights, flush):
             "alpha_materials": int((sca.materials["alpha_cutoff"] < 255).sum()), "materials": len(sca.materials),
             "cutoff": 128, "triangles_processed": int(c[0]), "triangles_rasterized": int(c[1]),
             "pixels_showing_alpha_materials": alpha_px, "pixels_covered": int(shown.sum())}
+
+
+# ----------------------------------------------------------------------------- backface-cone culling
+def cone_section(args, api, stream, texs, env, lights, flush):
+    """Backface-cone culling (swr_cull_meshlets_ex, SWR_CULL_BACKFACE_CONE) on the headline frame's
+    construction with open sphere patches instead of closed hulls (scenes.patch_scene: same count,
+    volume, scales, materials and camera; each patch carries its normal cone). The frame (cull,
+    draw, resolve, Hi-Z) is timed with frustum culling alone and with the cone test added; reports
+    both times, the meshlets each keeps and whether the two vis-buffers are identical. (The closed
+    meshlets of the headline scene have degenerate cones: the test culls none of them.)"""
+    import torch
+
+    from glimpsw_gb300 import scenes
+    sc = scenes.patch_scene(n=args.meshlets, width=args.width, height=args.height, texture_size=args.texture_size,
+                            n_materials=args.materials)
+    scene = api.Scene()
+    scene.upload_meshlets(sc.meshlets)
+    scene.set_materials(sc.materials, texs)
+    rast = api.Rasterizer()
+    rast.EnableBinning = False
+    v0 = sc.views[0]
+    W, H = v0.width, v0.height
+    fb = api.Framebuffer(W, H, 3)
+    n = len(sc.meshlets)
+    batches = [(off, min(BATCH, n - off)) for off in range(0, n, BATCH)]
+    bitmaps = [torch.zeros((cnt + 15) // 16, dtype=torch.int16, device="cuda") for _, cnt in batches]
+    hw, hh = api.hiz_texture_size(W, H)
+    hiz = api.Texture2D(api.FORMAT_R32F, hw, hh, 16, 1)
+    mats = (api.mat4(v0.proj), api.mat4(v0.view), api.mat4(scenes.IDENTITY), api.mat4(v0.view))
+    ctxs = [api.ShadingContext(scene, v0.world_to_clip, meshlet_offset=off, cull_bitmap=bm)
+            for (off, _), bm in zip(batches, bitmaps)]
+    rctx = api.ShadingContext(scene, v0.world_to_clip, world_to_clip=v0.world_to_clip, skybox=env, view_pos=v0.eye,
+                              lights=lights)
+
+    def draw(cone):
+        fb.clear(0xFF000000, 0.0)
+        for (off, cnt), bm, ctx in zip(batches, bitmaps, ctxs):
+            api.cull_meshlets(scene, off, cnt, bm, *mats, W, H, None, cone=cone)
+            rast.draw_meshlets(fb, cnt, ctx)
+
+    def frame(cone):
+        draw(cone)
+        rctx.resolve(rast, fb)
+        api.downsample_depth(fb, hiz)
+
+    out = {"meshlets": n, "scene": "open sphere patches (20-degree caps, 64 vertices, 113 triangles) with normal cones"}
+    layers = {}
+    for cone in (False, True):
+        for _ in range(max(3, args.warmup)):
+            frame(cone)
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            frame(cone)
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        kept = sum(api.cull_meshlets(scene, off, cnt, bm, *mats, W, H, None, want_count=True, cone=cone)
+                   for (off, cnt), bm in zip(batches, bitmaps))
+        draw(cone)
+        layers[cone] = (fb.get_pixels(0), fb.get_pixels(1))
+        key = "frustum_and_cone" if cone else "frustum_only"
+        out[key] = {"frame_ms": float(np.mean(ms)), "meshlets_kept": int(kept)}
+    out["cone_culled_share_of_frustum_visible"] = 1.0 - out["frustum_and_cone"]["meshlets_kept"] / max(
+        1, out["frustum_only"]["meshlets_kept"])
+    out["visbuffer_identical"] = bool(np.array_equal(layers[False][0], layers[True][0]) and
+                                      np.array_equal(layers[False][1], layers[True][1]))
+    return out
 
 
 # ----------------------------------------------------------------------------- learned decoder
@@ -838,6 +963,9 @@ def run_ours(args):
     alpha = None
     if not args.no_alpha:
         alpha = alpha_section(args, api, stream, sc, texs, env, lights, flush)
+    cone = None
+    if not args.no_cone:
+        cone = cone_section(args, api, stream, texs, env, lights, flush)
     neural = None
     if not args.no_neural:
         neural = neural_section(args, api, stream, sc, texs, env, scene, rast, lights)
@@ -850,18 +978,14 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        threads = cpu_threads()
-        of = OracleFrame(sc, [t.get_data() for t in texs], env.get_data(), threads)
-        times = of.timed(args.cpu_seconds)
-        cpu = {"value": float(np.median(times) * 1e3), "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"{len(times)} full frames of the same workload (median), oracle restatement, draw and "
-                         f"resolve rows split over {threads} threads"}
+        cpu = cpu_baseline_entry(cpu_baselines(sc, [t.get_data() for t in texs], env.get_data(), args.steps, 1,
+                                               unbinned_seconds=args.cpu_seconds))
 
     if rank == 0:
         line = {"metric": METRIC, "value": ms, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": max(3, args.warmup), "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32+i32", "data": "synthetic (seeded)",
-                "config": config_dict(args, sc, {"parallelism": "replicas only (one GPU renders the frame)"}),
+                "config": config_dict(args, sc, {"parallelism": PARALLELISM}),
                 "gtri_per_s": int(counters[0]) / (ms / 1e3) / 1e9,
                 "gpix_per_s": W * H / (ms / 1e3) / 1e9,
                 "counters": {"triangles_processed": int(counters[0]), "triangles_rasterized": int(counters[1]),
@@ -875,7 +999,7 @@ def run_ours(args):
                 "e2e": {"value": float(np.median(e2e_ms)), "unit": UNIT, "h2d_bytes_per_step": int(sc.meshlets.nbytes),
                         "d2h_bytes_per_step": int(W * H * 4)},
                 "gpu_launches": int(launches), "clocks": clocks.summary(), "cpu_baseline": cpu,
-                "alpha": alpha, "multiview": multiview, "neural": neural, "combined": combined}
+                "alpha": alpha, "cone": cone, "multiview": multiview, "neural": neural, "combined": combined}
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()

@@ -103,6 +103,8 @@ _SIGS = {
     "swr_texture_set_data": [C.c_void_p, C.c_void_p, C.c_size_t],
     "swr_cull_meshlets": [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                           C.c_void_p, C.c_float, C.c_float, C.c_void_p, C.c_void_p],
+    "swr_cull_meshlets_ex": [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                             C.c_void_p, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_uint32],
     "swr_downsample_depth": [C.c_void_p, C.c_void_p],
     "swr_resolve": [C.c_void_p, C.c_void_p, C.c_void_p],
     "swr_resolve_debug": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32],
@@ -372,14 +374,20 @@ class ShadingContext:
         return (st.requests, st.tiles, list(st.level_texels)) if want_stats else None
 
 
+CULL_FRUSTUM = 1
+CULL_BACKFACE_CONE = 2
+
+
 def cull_meshlets(scene: Scene, first: int, count: int, bitmap_device, proj, view, model, prev_view,
-                  frame_w: float, frame_h: float, depth_map: Texture2D | None = None, want_count: bool = False):
-    """ShadingContext::CullMeshlets (Shading.cpp:775-869) into a device bitmap (uint16 per 16)."""
+                  frame_w: float, frame_h: float, depth_map: Texture2D | None = None, want_count: bool = False,
+                  cone: bool = False):
+    """ShadingContext::CullMeshlets (Shading.cpp:775-869) into a device bitmap (uint16 per 16); with
+    cone, meshlets facing away from the camera as a whole are dropped too (swr_cull_meshlets_ex)."""
     cnt = C.c_uint32(0)
-    _check(_lib.swr_cull_meshlets(scene.h, first, count, _ptr(bitmap_device), _f16(proj), _f16(view), _f16(model),
-                                  _f16(prev_view), float(frame_w), float(frame_h),
-                                  depth_map.h if depth_map is not None else None,
-                                  C.byref(cnt) if want_count else None))
+    _check(_lib.swr_cull_meshlets_ex(scene.h, first, count, _ptr(bitmap_device), _f16(proj), _f16(view), _f16(model),
+                                     _f16(prev_view), float(frame_w), float(frame_h),
+                                     depth_map.h if depth_map is not None else None,
+                                     C.byref(cnt) if want_count else None, CULL_BACKFACE_CONE if cone else 0))
     return cnt.value if want_count else None
 
 
@@ -401,7 +409,7 @@ class Batch:
     views: list of (Framebuffer, proj, view, model, depth_only)."""
 
     def __init__(self, rast: "Rasterizer", scene: Scene, views, first: int = 0, count: int | None = None,
-                 frustum_cull: bool = True):
+                 frustum_cull: bool = True, cone: bool = False):
         L = load_library()
         if count is None:
             c = C.c_uint32()
@@ -410,7 +418,8 @@ class Batch:
         self._views = list(views)
         arr = self._descs(self._views)
         h = C.c_void_p()
-        _check(L.swr_batch_create(rast.h, scene.h, first, count, arr, len(self._views), int(frustum_cull), C.byref(h)))
+        flags = (CULL_FRUSTUM if frustum_cull else 0) | (CULL_BACKFACE_CONE if cone else 0)
+        _check(L.swr_batch_create(rast.h, scene.h, first, count, arr, len(self._views), flags, C.byref(h)))
         self.h = h
         self.count, self.rast, self.scene = count, rast, scene
 

@@ -27,6 +27,8 @@ struct BatchView {              // device table for the batched clear and cull k
     uint16_t* bitmap;
     uint32_t pixels;            // width * height
     uint32_t* tileMin;          // per 4x4 tile depth bound
+    uint32_t frustum, cone;     // tests of the batched cull: frustum planes, backface cone
+    float eye[3];               // camera centre in object space (cone_camera)
 };
 
 // Framebuffer::Clear(color, depth) for every view; keys and tile depth bounds restart from the
@@ -43,19 +45,24 @@ __global__ void k_clear_views(const BatchView* __restrict__ views, uint32_t colo
     }
 }
 
-// CullMeshlets without a depth map (Shading.cpp:797-809, 865): frustum planes 0..4, one meshlet per
-// thread, the view in blockIdx.y; a warp's ballot gives two 16-bit masks.
+// CullMeshlets without a depth map (Shading.cpp:797-809, 865): frustum planes 0..4 and, when enabled,
+// the backface-cone test (cone_culled), one meshlet per thread, the view in blockIdx.y; a warp's
+// ballot gives two 16-bit masks.
 __global__ void k_cull_views(const BatchView* __restrict__ views, const uint8_t* __restrict__ meshlets, uint32_t first,
-                             uint32_t count) {
+                             uint32_t count, const DevMaterial* __restrict__ materials, uint32_t numMaterials) {
     const BatchView& v = views[blockIdx.y];
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool visible = i < count;
     if (visible) {
-        const float4 s = *(const float4*)(meshlets + (size_t)(first + i) * kMeshletSize);
-        for (int k = 0; k < 5; k++) {
-            float dist = fadd(ffma(s.x, v.planes[k][0], ffma(s.y, v.planes[k][1], fmul(s.z, v.planes[k][2]))), v.planes[k][3]);
-            visible = visible && (dist > -s.w);
+        const uint8_t* rec = meshlets + (size_t)(first + i) * kMeshletSize;
+        const float4 s = *(const float4*)rec;
+        if (v.frustum) {
+            for (int k = 0; k < 5; k++) {
+                float dist = fadd(ffma(s.x, v.planes[k][0], ffma(s.y, v.planes[k][1], fmul(s.z, v.planes[k][2]))), v.planes[k][3]);
+                visible = visible && (dist > -s.w);
+            }
         }
+        if (v.cone && visible) visible = !cone_culled(rec, v.eye[0], v.eye[1], v.eye[2], materials, numMaterials);
     }
     const unsigned m = __ballot_sync(0xFFFFFFFFu, visible);
     const uint32_t w0 = i & ~31u;
@@ -74,7 +81,7 @@ struct swr_batch_t {
     swr_rasterizer rast;
     swr_scene scene;
     uint32_t first, count, numViews;
-    int frustumCull;
+    uint32_t cullFlags;  // SWR_CULL_FRUSTUM | SWR_CULL_BACKFACE_CONE
     uint32_t maxPixels;
     std::vector<swr_framebuffer> fbs;
     std::vector<uint8_t> depthOnly;  // per view: only the depth layer is written
@@ -119,7 +126,7 @@ swr_status upload_views(swr_batch b, const swr_view_desc* views) {
         v.orderStride = order_stride(b->count);
         v.keys = fb->keys;
         v.tileMin = fb->tileMin;
-        v.cullBitmap = b->frustumCull ? b->dBitmaps + (size_t)i * words : nullptr;
+        v.cullBitmap = b->cullFlags ? b->dBitmaps + (size_t)i * words : nullptr;
         BatchView& w = bv[i];
         memset(&w, 0, sizeof(w));
         memcpy(w.planes, planes, sizeof(w.planes));
@@ -129,6 +136,8 @@ swr_status upload_views(swr_batch b, const swr_view_desc* views) {
         w.tileMin = fb->tileMin;
         w.bitmap = b->dBitmaps + (size_t)i * words;
         w.pixels = fb->width * fb->height;
+        w.frustum = (b->cullFlags & SWR_CULL_FRUSTUM) ? 1u : 0u;
+        w.cone = ((b->cullFlags & SWR_CULL_BACKFACE_CONE) && swr_hostmath::cone_camera(objToClip, w.eye)) ? 1u : 0u;
         b->depthOnly[i] = d.depth_only != 0;
     }
     cudaStream_t st = swr_internal_stream();
@@ -161,8 +170,9 @@ swr_status capture(swr_batch b) {
         const uint32_t nv = b->numViews;
         const int blocksX = (int)std::min<uint32_t>((b->maxPixels + 255) / 256, 1024u);
         k_clear_views<<<dim3(blocksX, nv), 256, 0, cs>>>(b->dBatch, 0xFF000000u, 0u);
-        if (b->frustumCull && b->count)
-            k_cull_views<<<dim3((b->count + 255) / 256, nv), 256, 0, cs>>>(b->dBatch, b->scene->meshlets, b->first, b->count);
+        if (b->cullFlags && b->count)
+            k_cull_views<<<dim3((b->count + 255) / 256, nv), 256, 0, cs>>>(b->dBatch, b->scene->meshlets, b->first, b->count,
+                                                                          b->scene->materials, b->scene->num_materials);
         cudaMemsetAsync(b->scratch.control, 0, 3 * sizeof(unsigned long long), cs);
         DrawArgs a = {};
         a.meshlets = b->scene->meshlets;
@@ -219,7 +229,7 @@ swr_status swr_batch_create(swr_rasterizer r, swr_scene s, uint32_t first, uint3
     if (padded * num_views >= (1ull << 32)) return swr_internal_fail(SWR_EINVAL, "swr_batch_create: too many work items");
     swr_batch b = new (std::nothrow) swr_batch_t();
     if (!b) return swr_internal_fail(SWR_ENOMEM, "swr_batch_create: host allocation failed");
-    b->rast = r, b->scene = s, b->first = first, b->count = count, b->numViews = num_views, b->frustumCull = frustum_cull != 0;
+    b->rast = r, b->scene = s, b->first = first, b->count = count, b->numViews = num_views, b->cullFlags = (uint32_t)frustum_cull & (SWR_CULL_FRUSTUM | SWR_CULL_BACKFACE_CONE);
     uint64_t totalTris = 0;
     for (uint32_t i = 0; i < num_views; i++) {
         b->fbs.push_back(views[i].fb);

@@ -38,6 +38,35 @@ inline __host__ __device__ bool material_alpha_tested(const DevMaterial& m) {
     return m.alpha_cutoff - 1u < 254u && m.has_texture;
 }
 
+#ifdef __CUDACC__
+// Backface-cone culling of one meshlet record (no counterpart in the reference's CullMeshlets; the
+// records carry meshoptimizer's cone, Scene.h:18-19, Scene.cpp:240-244): every triangle faces away
+// from the camera at eye (object space) when dot(normalize(ConeApex - eye), ConeAxis) >= ConeCutoff.
+// The test here is conservative by a margin, so that no triangle the rasterizer would keep is
+// culled despite float rounding: the cosine must exceed the cutoff by kConeMargin (about 1.8
+// degrees of the view direction), and the camera must be at least four times the apex's reach
+// (|centre - apex| + radius) away, so that each triangle's plane is seen at more than a degree.
+// Double-sided materials draw both faces and are never culled. Degenerate cones (cutoff 1) never
+// pass.
+constexpr float kConeMargin = 1.0f / 32.0f;
+__device__ __forceinline__ bool cone_culled(const uint8_t* rec, float ex, float ey, float ez, const DevMaterial* materials,
+                                            uint32_t numMaterials) {
+    const float* f = (const float*)rec;  // BoundCenter, BoundRadius, ConeApex, ConeAxis, ConeCutoff
+    const float cm = f[10] + kConeMargin;
+    if (!(cm < 1.0f)) return false;
+    const uint32_t mat = *(const uint32_t*)(rec + 48);
+    if (mat < numMaterials && materials[mat].is_double_sided) return false;
+    const float dx = f[4] - ex, dy = f[5] - ey, dz = f[6] - ez;
+    const float l2 = dx * dx + dy * dy + dz * dz;
+    const float proj = dx * f[7] + dy * f[8] + dz * f[9];
+    const float a2 = f[7] * f[7] + f[8] * f[8] + f[9] * f[9];
+    if (!(proj > 0.0f) || !(a2 > 0.5f)) return false;
+    const float cx = f[0] - f[4], cy = f[1] - f[5], cz = f[2] - f[6];
+    const float reach = sqrtf(cx * cx + cy * cy + cz * cz) + f[3];
+    return proj * proj >= cm * cm * l2 * a2 && l2 >= 16.0f * reach * reach;
+}
+#endif
+
 // A triangle ready to rasterize: edge equations at pixel (0,0), depth plane and tie-break rank.
 struct TriRec {
     int32_t E0, E1, E2;

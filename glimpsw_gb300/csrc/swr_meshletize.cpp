@@ -12,9 +12,9 @@
 //
 // Bounds: a bounding sphere of the meshlet's vertices (Ritter's construction from the extreme
 // points along the axes, radius widened by a relative 1e-6 so that every vertex lies inside after
-// rounding) and a normal cone (axis = normalised mean of the triangle normals, cutoff = the least
-// cosine between a triangle normal and the axis, apex = the sphere centre). The rasterizer reads
-// only the sphere (CullMeshlets, Shading.cpp:797-809); the cone is carried in the record.
+// rounding) and a normal cone in meshoptimizer's convention (see below), which the backface-cone
+// test of swr_cull_meshlets_ex reads; the reference's CullMeshlets reads only the sphere
+// (Shading.cpp:797-809).
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -228,13 +228,32 @@ swr_status swr_build_meshlets(const swr_mesh_desc* mesh, void* out, uint32_t cap
             while ((double)rf < d) rf = std::nextafter(rf, INFINITY);
         }
         m.BoundRadius = rf;
+        // Normal cone in meshoptimizer's convention (every triangle faces away from a camera at e when
+        // dot(normalize(apex - e), axis) >= cutoff): axis = normalised mean normal; with m the least
+        // cosine between a normal and the axis, cutoff = sqrt(1 - m^2), and the apex is the point
+        // centre - t*axis behind every triangle's plane. m <= 0.1 gives the degenerate cone
+        // (cutoff 1, axis 0, apex = centre), which never culls.
         const double al = std::sqrt(axis.x * axis.x + axis.y * axis.y + axis.z * axis.z);
         if (al > 0) axis = { axis.x / al, axis.y / al, axis.z / al };
-        double cutoff = 1.0;
-        for (const Vec3& n : normals) cutoff = std::min(cutoff, n.x * axis.x + n.y * axis.y + n.z * axis.z);
+        double mindp = al > 0 ? 1.0 : -1.0;
+        for (const Vec3& n : normals) mindp = std::min(mindp, n.x * axis.x + n.y * axis.y + n.z * axis.z);
         m.ConeApex[0] = m.BoundCenter[0], m.ConeApex[1] = m.BoundCenter[1], m.ConeApex[2] = m.BoundCenter[2];
-        m.ConeAxis[0] = (float)axis.x, m.ConeAxis[1] = (float)axis.y, m.ConeAxis[2] = (float)axis.z;
-        m.ConeCutoff = (float)cutoff;
+        m.ConeCutoff = 1.0f;
+        if (mindp > 0.1) {
+            const Vec3 cc = { m.BoundCenter[0], m.BoundCenter[1], m.BoundCenter[2] };
+            double t = 0.0;
+            for (size_t i = 0; i < tris.size(); i++) {
+                const Vec3& n = normals[i];
+                const Vec3& a = pts[vertSlot[I[tris[i] * 3]]];
+                const double dn = n.x * axis.x + n.y * axis.y + n.z * axis.z;
+                const double dc = (cc.x - a.x) * n.x + (cc.y - a.y) * n.y + (cc.z - a.z) * n.z;
+                if (dn > 0) t = std::max(t, dc / dn);
+            }
+            m.ConeApex[0] = (float)(cc.x - axis.x * t), m.ConeApex[1] = (float)(cc.y - axis.y * t);
+            m.ConeApex[2] = (float)(cc.z - axis.z * t);
+            m.ConeAxis[0] = (float)axis.x, m.ConeAxis[1] = (float)axis.y, m.ConeAxis[2] = (float)axis.z;
+            m.ConeCutoff = (float)std::sqrt(std::max(0.0, 1.0 - mindp * mindp));
+        }
     }
     *count = made;
     return SWR_OK;

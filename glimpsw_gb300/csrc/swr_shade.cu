@@ -65,10 +65,16 @@ struct CullArgs {
     const uint32_t* depthData;  // R32f Hi-Z storage or null
     uint32_t mipOffsets[16];
     uint32_t mipLevels, rowShift;
+    // backface-cone culling (cone_culled): camera centre in object space, materials
+    uint32_t cone;
+    float eye[3];
+    const DevMaterial* materials;
+    uint32_t numMaterials;
 };
 
 // ShadingContext::CullMeshlets (Shading.cpp:775-869) + ProjectSphere (264-279), one meshlet per
-// thread; a warp's ballot gives two of the reference's 16-bit masks.
+// thread; a warp's ballot gives two of the reference's 16-bit masks. With a.cone, meshlets that
+// pass the frustum test and face away as a whole (cone_culled) are dropped before the Hi-Z test.
 __global__ void __launch_bounds__(256) k_cull(CullArgs a) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool visible = i < a.count;
@@ -81,6 +87,8 @@ __global__ void __launch_bounds__(256) k_cull(CullArgs a) {
             float dist = fmaf(c.x, a.planes[k][0], fmaf(c.y, a.planes[k][1], c.z * a.planes[k][2])) + a.planes[k][3];
             visible = visible && (dist > -r);
         }
+        if (a.cone && visible)
+            visible = !cone_culled((const uint8_t*)b, a.eye[0], a.eye[1], a.eye[2], a.materials, a.numMaterials);
         if (a.depthData != nullptr && visible) {
             float vw;
             F3 vs = xform4(a.objectToPrevView, c, vw);
@@ -643,8 +651,16 @@ extern "C" {
 swr_status swr_cull_meshlets(swr_scene s, uint32_t first, uint32_t count, uint16_t* bitmap_device, const float proj[16],
                              const float view[16], const float model[16], const float prev_view[16], float frame_width,
                              float frame_height, swr_texture depth_map, uint32_t* visible_count) {
+    return swr_cull_meshlets_ex(s, first, count, bitmap_device, proj, view, model, prev_view, frame_width, frame_height,
+                                depth_map, visible_count, 0u);
+}
+
+swr_status swr_cull_meshlets_ex(swr_scene s, uint32_t first, uint32_t count, uint16_t* bitmap_device, const float proj[16],
+                                const float view[16], const float model[16], const float prev_view[16], float frame_width,
+                                float frame_height, swr_texture depth_map, uint32_t* visible_count, uint32_t flags) {
     if (!s || !bitmap_device || !proj || !view || !model || !prev_view)
         return swr_internal_fail(SWR_EINVAL, "swr_cull_meshlets: NULL argument");
+    if (flags & ~(uint32_t)SWR_CULL_BACKFACE_CONE) return swr_internal_fail(SWR_EINVAL, "swr_cull_meshlets_ex: unknown flags");
     if ((uint64_t)first + count > s->count) return swr_internal_fail(SWR_EINVAL, "swr_cull_meshlets: range outside the scene");
     if (depth_map && depth_map->format != SWR_FORMAT_R32F)
         return swr_internal_fail(SWR_EINVAL, "swr_cull_meshlets: the depth map must be R32f");
@@ -666,6 +682,11 @@ swr_status swr_cull_meshlets(swr_scene s, uint32_t first, uint32_t count, uint16
     swr_hostmath::mat4_mul(pv, model, objToClip);
     swr_hostmath::frustum_planes(objToClip, planes);
     memcpy(a.planes, planes, sizeof(a.planes));  // planes 0..4 (the reference skips the last, Shading.cpp:806)
+    if (flags & SWR_CULL_BACKFACE_CONE) {
+        a.cone = swr_hostmath::cone_camera(objToClip, a.eye) ? 1u : 0u;
+        a.materials = s->materials;
+        a.numMaterials = s->num_materials;
+    }
     memcpy(a.objectToPrevView, objToPrev, sizeof(objToPrev));
     a.objectToWorldScale = swr_hostmath::column0_length(model);
     a.projFactors[0] = proj[3 * 4 + 2], a.projFactors[1] = proj[0], a.projFactors[2] = proj[1 * 4 + 1];

@@ -82,6 +82,114 @@ def meshlet_template() -> tuple[np.ndarray, np.ndarray]:
     return _TEMPLATE
 
 
+_PATCH: tuple[np.ndarray, np.ndarray] | None = None
+
+
+def patch_template(cap_degrees: float = 20.0) -> tuple[np.ndarray, np.ndarray]:
+    """An open patch of the unit sphere: the 64 points of a Fibonacci lattice on the cap within
+    cap_degrees of +y, triangulated by the cap's part of the convex hull of those points and a point
+    far below the cap (the hull's other triangles touch that point and are dropped), wound so
+    (b-a)x(c-a) points outward. Returns (64x3 positions, triangles)."""
+    global _PATCH
+    if _PATCH is None:
+        from scipy.spatial import ConvexHull
+
+        n = 64
+        i = np.arange(n, dtype=np.float64) + 0.5
+        ymin = math.cos(math.radians(cap_degrees))
+        y = 1.0 - (1.0 - ymin) * i / n
+        r = np.sqrt(1.0 - y * y)
+        th = math.pi * (1.0 + 5.0 ** 0.5) * i
+        p = np.stack([np.cos(th) * r, y, np.sin(th) * r], axis=1)
+        hull = ConvexHull(np.concatenate([p, [[0.0, -10.0, 0.0]]]))
+        tris = hull.simplices[(hull.simplices < n).all(axis=1)].astype(np.int64)
+        a, b, c = p[tris[:, 0]], p[tris[:, 1]], p[tris[:, 2]]
+        flip = np.einsum("ij,ij->i", np.cross(b - a, c - a), (a + b + c) / 3.0) < 0
+        tris[flip] = tris[flip][:, [0, 2, 1]]
+        cen = (a + b + c) / 3.0
+        tris = tris[np.lexsort((np.arctan2(cen[:, 2], cen[:, 0]), np.floor(cen[:, 1] * 8.0)))]
+        _PATCH = (p, tris)
+    return _PATCH
+
+
+def normal_cones(world: np.ndarray, tris: np.ndarray, centers: np.ndarray, min_dot: float = 0.1):
+    """Normal cones of meshlets in meshoptimizer's convention, as the reference stores them
+    (ConeApex, ConeAxis, ConeCutoff, Scene.cpp:240-244): every triangle faces away from a camera at e
+    when dot(normalize(apex - e), axis) >= cutoff. Axis = normalised mean of the unit triangle
+    normals; with m the least cosine between a normal and the axis, cutoff = sqrt(1 - m^2) and the
+    apex is the point centre - t*axis behind every triangle's plane (t = the largest distance along
+    the axis from the centre back to a plane). A cone with m <= min_dot is degenerate: cutoff 1,
+    axis 0, apex = centre. world: (n, verts, 3) float64 positions; returns float32 arrays."""
+    a, b, c = world[:, tris[:, 0]], world[:, tris[:, 1]], world[:, tris[:, 2]]
+    nrm = np.cross(b - a, c - a)
+    ln = np.linalg.norm(nrm, axis=2, keepdims=True)
+    nrm = np.where(ln > 0, nrm / np.where(ln > 0, ln, 1.0), 0.0)
+    axis = nrm.sum(axis=1)
+    al = np.linalg.norm(axis, axis=1, keepdims=True)
+    axis = np.where(al > 0, axis / np.where(al > 0, al, 1.0), 0.0)
+    m = np.einsum("ntk,nk->nt", nrm, axis).min(axis=1)
+    dn = np.einsum("ntk,nk->nt", nrm, axis)
+    dc = np.einsum("ntk,ntk->nt", centers[:, None, :] - a, nrm)
+    t = np.where(dn > 0, dc / np.where(dn > 0, dn, 1.0), 0.0).max(axis=1).clip(min=0.0)
+    ok = m > min_dot
+    apex = np.where(ok[:, None], centers - axis * t[:, None], centers)
+    cutoff = np.where(ok, np.sqrt(np.clip(1.0 - m * m, 0.0, 1.0)), 1.0)
+    return apex.astype(np.float32), np.where(ok[:, None], axis, 0.0).astype(np.float32), cutoff.astype(np.float32)
+
+
+def _random_rotations(rng: np.random.Generator, n: int) -> np.ndarray:
+    """Uniformly distributed rotation matrices from normalised Gaussian quaternions, (n, 3, 3)."""
+    q = rng.standard_normal((n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q.T
+    return np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], axis=1),
+                     np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], axis=1),
+                     np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], axis=1)], axis=1)
+
+
+def build_patch_meshlets(centers: np.ndarray, scales: np.ndarray, material_ids: np.ndarray, rng: np.random.Generator,
+                         sigma: float = 0.002, uv_repeat: float = 2.0) -> np.ndarray:
+    """Open sphere patches (patch_template), one per meshlet: radially displaced, randomly rotated,
+    scaled and translated, with bounding spheres and normal cones (normal_cones). The displacement
+    is smaller than the closed meshlets' (sigma 0.002 instead of 0.02): on triangles this small,
+    sigma 0.02 tilts some normals by 30 degrees or more, which widens every cone until it culls
+    almost nothing."""
+    n = len(centers)
+    base, tris = patch_template()
+    nv, nt = base.shape[0], tris.shape[0]
+    out = np.zeros(n, dtype=MESHLET_DTYPE)
+    disp = 1.0 + sigma * rng.standard_normal((n, nv))
+    local = base[None, :, :] * disp[:, :, None]
+    rot = _random_rotations(rng, n)
+    world = np.einsum("nij,nvj->nvi", rot, local) * scales[:, None, None] + centers[:, None, :]
+    world32 = world.astype(np.float32)
+    out["Positions"] = np.transpose(world32, (0, 2, 1))
+    out["NumVertices"] = nv
+    out["NumTriangles"] = nt
+    out["AlphaCutoff"] = 255
+    out["MaterialId"] = material_ids.astype(np.uint32)
+    out["BoundCenter"] = centers.astype(np.float32)
+    d = np.linalg.norm(world32.astype(np.float64) - centers[:, None, :], axis=2).max(axis=1)
+    out["BoundRadius"] = (d * (1.0 + 1e-6)).astype(np.float32)
+    out["ConeApex"], out["ConeAxis"], out["ConeCutoff"] = normal_cones(world32.astype(np.float64), tris,
+                                                                         centers.astype(np.float32).astype(np.float64))
+    idx = np.zeros((3, 128), dtype=np.uint8)
+    idx[:, :nt] = tris.T
+    out["Indices"] = idx[None]
+    uv = (base[:, [0, 2]] * 0.5 + 0.5) * uv_repeat
+    uv16 = uv.astype(np.float16).view(np.uint16).astype(np.uint32)
+    out["TexCoords"][:, :nv] = (uv16[:, 0] | (uv16[:, 1] << 16))[None]
+    normal = local / np.linalg.norm(local, axis=2, keepdims=True)
+    nrm = np.einsum("nij,nvj->nvi", rot, normal)
+    up = np.array([0.0, 1.0, 0.0])
+    tan = np.cross(up[None, None, :], nrm)
+    tl = np.linalg.norm(tan, axis=2, keepdims=True)
+    tan = np.where(tl > 1e-6, tan / np.maximum(tl, 1e-12), np.array([1.0, 0.0, 0.0]))
+    on, ot = _pack_unorm8(_oct_encode(nrm)), _pack_unorm8(_oct_encode(tan))
+    out["NormalTangents"][:, :nv] = on[..., 0] | (on[..., 1] << 8) | (ot[..., 0] << 16) | (ot[..., 1] << 24)
+    return out
+
+
 def _oct_encode(n: np.ndarray) -> np.ndarray:
     """Octahedral map of unit vectors to [0,1]^2 (the reference's MapOctahedron, Texture.h:282-288)."""
     w = 1.0 / (np.abs(n[..., 0]) + np.abs(n[..., 1]) + np.abs(n[..., 2]))
@@ -356,13 +464,38 @@ def _round4(v: float) -> int:
     return max(4, int(round(v / 4.0)) * 4)
 
 
+def frustum_visible_count(meshlets: np.ndarray, view: "View") -> int:
+    """Meshlets whose bounding sphere passes frustum planes 0..4 of the view (CullMeshlets'
+    frustum test, Shading.cpp:797-809, in float64; for choosing cameras, not for parity)."""
+    m = mat_mul(view.proj, view.view).astype(np.float64).reshape(4, 4)  # [column, row]
+    rows = m.T
+    c = meshlets["BoundCenter"].astype(np.float64)
+    r = meshlets["BoundRadius"].astype(np.float64)
+    vis = np.ones(len(meshlets), bool)
+    for i in range(3):
+        for sgn in (1.0, -1.0):
+            if i == 2 and sgn < 0:
+                continue  # the far plane is not tested
+            p = rows[3] + sgn * rows[i]
+            p = p / np.linalg.norm(p[:3])
+            vis &= c @ p[:3] + p[3] > -r
+    return int(vis.sum())
+
+
 def multiview_scene(n: int = 200_000, n_cameras: int = 58, seed: int = 3, cube_size: int = 1024,
-                    min_res=(256, 256), max_res=(2560, 1440)) -> Scene:
+                    min_res=(256, 256), max_res=(2560, 1440), min_visible: int | None = None,
+                    max_visible: int | None = None) -> Scene:
     """Batched multi-view workload: n meshlets of the grid construction (spacing 1, radius 1,
     random yaw) seen by 6 depth-only cube-face views (cube_size^2, 90 degrees) from a point above the
     grid's centre plus n_cameras cameras at random positions and heights whose resolutions are
-    drawn log-uniformly between min_res and max_res (rounded to multiples of 4)."""
+    drawn log-uniformly between min_res and max_res (rounded to multiples of 4). The cube is turned
+    so that its diagonal is vertical: every face then sees part of the grid (an axis-aligned cube's
+    upward face would see nothing). Cameras whose frustum holds fewer than min_visible or more than
+    max_visible meshlets (default n/200 and 3n/4: 1k and 150k for 200k meshlets) are drawn again, so
+    the views' loads range over that interval."""
     rng = np.random.default_rng(seed)
+    min_visible = max(1, n // 200) if min_visible is None else min_visible
+    max_visible = (3 * n) // 4 if max_visible is None else max_visible
     side = int(math.ceil(math.sqrt(n)))
     g = np.arange(side) - (side - 1) / 2.0
     gx, gz = np.meshgrid(g, g)
@@ -372,21 +505,35 @@ def multiview_scene(n: int = 200_000, n_cameras: int = 58, seed: int = 3, cube_s
     mats["alpha_cutoff"] = 255
     views = []
     eye = np.array([0.0, 3.0, 0.0])
+    # rotation taking the cube diagonal (1, 1, 1) / sqrt(3) to +y
+    d = np.array([1.0, 1.0, 1.0]) / math.sqrt(3.0)
+    axis = np.cross(d, [0.0, 1.0, 0.0])
+    ang = math.acos(d[1])
+    k = axis / np.linalg.norm(axis)
+    K = np.array([[0, -k[2], k[1]], [k[2], 0, -k[0]], [-k[1], k[0], 0]])
+    R = np.eye(3) + math.sin(ang) * K + (1 - math.cos(ang)) * K @ K
     faces = [((1, 0, 0), (0, 1, 0)), ((-1, 0, 0), (0, 1, 0)), ((0, 1, 0), (0, 0, 1)), ((0, -1, 0), (0, 0, 1)),
              ((0, 0, 1), (0, 1, 0)), ((0, 0, -1), (0, 1, 0))]
-    for d, up in faces:
-        v = View(cube_size, cube_size, look_at(eye, eye + np.array(d), up), proj_reversed_z(90.0, 1.0, 0.1),
+    for fd, up in faces:
+        fd, up = R @ np.array(fd, float), R @ np.array(up, float)
+        v = View(cube_size, cube_size, look_at(eye, eye + fd, up), proj_reversed_z(90.0, 1.0, 0.1),
                  eye.astype(np.float32), depth_only=True)
         views.append(v)
     half = side / 2.0
-    for _ in range(n_cameras):
+    tries = 0
+    while len(views) < 6 + n_cameras:
+        tries += 1
+        if tries > 100 * (n_cameras + 1):
+            raise ValueError("multiview_scene: no camera placement meets the visible-meshlet bounds")
         w = _round4(math.exp(rng.uniform(math.log(min_res[0]), math.log(max_res[0]))))
         h = _round4(math.exp(rng.uniform(math.log(min_res[1]), math.log(max_res[1]))))
         height = math.exp(rng.uniform(math.log(1.5), math.log(80.0)))
         e = np.array([rng.uniform(-half, half), height, rng.uniform(-half, half)])
         yaw, pitch = rng.uniform(0, 2 * math.pi), math.radians(rng.uniform(-70, -8))
-        d = np.array([math.cos(pitch) * math.cos(yaw), math.sin(pitch), math.cos(pitch) * math.sin(yaw)])
-        views.append(make_view(w, h, eye=e, target=e + d))
+        dv = np.array([math.cos(pitch) * math.cos(yaw), math.sin(pitch), math.cos(pitch) * math.sin(yaw)])
+        v = make_view(w, h, eye=e, target=e + dv)
+        if min_visible <= frustum_visible_count(m, v) <= max_visible:
+            views.append(v)
     return Scene(m, mats, 0, 1, views, name=f"multiview{n}x{len(views)}")
 
 
@@ -417,12 +564,34 @@ def volume_scene(n: int = 100_000, width: int = 1920, height: int = 1080, n_mate
                  name=f"volume{n}@{width}x{height}")
 
 
+def patch_scene(n: int = 100_000, width: int = 1920, height: int = 1080, n_materials: int = 64, seed: int = 2,
+                texture_size: int = 2048, extent: float = 100.0, env_size: int = 1024) -> Scene:
+    """The volume construction (volume_scene) with open sphere patches instead of closed hulls:
+    n randomly rotated patches (build_patch_meshlets) scattered in a (2*extent)^3 volume with
+    log-uniform scale 0.1-10, each carrying its normal cone, so that about half of them face away
+    from any camera as a whole (what backface-cone culling removes)."""
+    rng = np.random.default_rng(seed)
+    centers = rng.uniform(-extent, extent, size=(n, 3))
+    scales = np.exp(rng.uniform(math.log(0.1), math.log(10.0), n))
+    mat_ids = rng.integers(0, n_materials, n)
+    m = build_patch_meshlets(centers, scales, mat_ids, rng)
+    mats = np.zeros(n_materials, dtype=MATERIAL_DTYPE)
+    mats["texture"] = np.arange(n_materials)
+    mats["alpha_cutoff"] = 255
+    eye = np.array([0.0, 0.0, -1.3 * extent])
+    v0 = make_view(width, height, eye=eye, target=(0.0, 0.0, 0.0))
+    v1 = make_view(width, height, eye=eye + np.array([0.4, 0.2, 0.6]), target=(1.0, 0.5, 0.0))
+    return Scene(m, mats, texture_size, 2, [v0, v1], texture_seed=seed * 1000, env_size=env_size, texture_detail=True,
+                 name=f"patches{n}@{width}x{height}")
+
+
 def combined_scene(copies: int = 10, base_n: int = 100_000, n_materials: int = 256, n_views: int = 16, seed: int = 5,
                    texture_size: int = 2048, env_size: int = 1024, extent: float = 100.0) -> Scene:
     """Combined stress workload: `copies` translated copies of the volume construction (base_n
     meshlets in a (2*extent)^3 cube each) side by side on a grid in x and z, copy c using materials
     (m % 64) + 64 * (c % (n_materials / 64)), seen by n_views cameras above the field looking at
-    its centre, with 16:9 sizes log-uniform between 1280x720 and 2880x1620 (multiples of 4)."""
+    its centre, with 16:9 sizes log-uniform between 1280x720 and 2880x1620 (multiples of 4; the first two
+    views take the two ends)."""
     rng = np.random.default_rng(seed)
     base = volume_scene(n=base_n, width=1280, height=720, n_materials=64, seed=seed, extent=extent).meshlets
     cols = int(math.ceil(math.sqrt(copies)))
@@ -447,6 +616,8 @@ def combined_scene(copies: int = 10, base_n: int = 100_000, n_materials: int = 2
     views = []
     for i in range(n_views):
         s = math.exp(rng.uniform(0.0, math.log(2880.0 / 1280.0)))
+        if i < 2:  # the interval's two ends are always among the sizes
+            s = 1.0 if i == 0 else 2880.0 / 1280.0
         w, h = _round4(1280 * s), _round4(720 * s)
         ang = 2 * math.pi * i / n_views + rng.uniform(-0.2, 0.2)
         r = rng.uniform(0.6, 1.2) * max(half_x, half_z)

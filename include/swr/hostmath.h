@@ -105,6 +105,68 @@ inline void frustum_planes(const float* objectToClip, float planes[6][4]) {
     }
 }
 
+// Camera centre in object space for backface-cone culling: the point that objectToClip maps to
+// clip x = y = w = 0, i.e. the null vector of its x, y and w rows (solved in double). Returns false
+// when the cone test does not apply: an affine (orthographic) or singular projection, or one that
+// mirrors the screen so that FrontCCW keeps triangles whose (b-a)x(c-a) normal points away from
+// the camera. The orientation is read off a small triangle placed in front of the camera with its
+// normal towards it, projected and tested with TrianglePacket::Setup's determinant
+// (Rasterizer.cpp:262-266): it must come out front-facing (det > 0).
+inline bool cone_camera(const float* m, float eye[3]) {
+    const int rows[3] = { 0, 1, 3 };
+    double A[3][3], b[3];
+    for (int i = 0; i < 3; i++) {
+        for (int c = 0; c < 3; c++) A[i][c] = (double)m[c * 4 + rows[i]];
+        b[i] = -(double)m[3 * 4 + rows[i]];
+    }
+    auto det3 = [](double M[3][3]) {
+        return M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) - M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+               M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+    };
+    double scale = 0;
+    for (int i = 0; i < 3; i++)
+        for (int c = 0; c < 3; c++) scale = fmax(scale, fabs(A[i][c]));
+    const double d = det3(A);
+    if (!(fabs(d) > 1e-12 * scale * scale * scale)) return false;
+    double e[3];
+    for (int c = 0; c < 3; c++) {  // Cramer's rule
+        double M[3][3];
+        for (int i = 0; i < 3; i++)
+            for (int k = 0; k < 3; k++) M[i][k] = (k == c) ? b[i] : A[i][k];
+        e[c] = det3(M) / d;
+    }
+    // w grows along g (the w row); a triangle at e + g/|g| with normal -g faces the camera.
+    double g[3] = { A[2][0], A[2][1], A[2][2] };
+    const double gl = sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+    if (!(gl > 0)) return false;
+    for (int k = 0; k < 3; k++) g[k] /= gl;
+    const double h[3] = { fabs(g[0]) < 0.9 ? 1.0 : 0.0, fabs(g[0]) < 0.9 ? 0.0 : 1.0, 0.0 };
+    double u[3] = { h[1] * g[2] - h[2] * g[1], h[2] * g[0] - h[0] * g[2], h[0] * g[1] - h[1] * g[0] };
+    const double ul = sqrt(u[0] * u[0] + u[1] * u[1] + u[2] * u[2]);
+    for (int k = 0; k < 3; k++) u[k] /= ul;
+    const double v[3] = { g[1] * u[2] - g[2] * u[1], g[2] * u[0] - g[0] * u[2], g[0] * u[1] - g[1] * u[0] };  // g x u
+    // vertices q, q + v/100, q + u/100: (v x u) = -g, so the normal points at the camera
+    const double dist = 1.0 + sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) * 1e-3;
+    double P[3][3];
+    for (int k = 0; k < 3; k++) {
+        const double q = e[k] + g[k] * dist;
+        P[0][k] = q, P[1][k] = q + v[k] * dist * 0.01, P[2][k] = q + u[k] * dist * 0.01;
+    }
+    double nx[3], ny[3];
+    for (int i = 0; i < 3; i++) {
+        double c4[4];
+        for (int r = 0; r < 4; r++)
+            c4[r] = (double)m[0 * 4 + r] * P[i][0] + (double)m[1 * 4 + r] * P[i][1] + (double)m[2 * 4 + r] * P[i][2] +
+                    (double)m[3 * 4 + r];
+        if (!(c4[3] > 0)) return false;
+        nx[i] = c4[0] / c4[3], ny[i] = c4[1] / c4[3];
+    }
+    const double det = (nx[2] - nx[0]) * (ny[1] - ny[0]) - (nx[0] - nx[1]) * (ny[0] - ny[2]);
+    if (!(det > 0)) return false;
+    for (int k = 0; k < 3; k++) eye[k] = (float)e[k];
+    return true;
+}
+
 // glm::length(vec3(m[0])): uniform-scale estimate of a model matrix (Shading.cpp:793).
 inline float column0_length(const float* m) { return sqrtf(m[0] * m[0] + m[1] * m[1] + m[2] * m[2]); }
 

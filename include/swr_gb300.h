@@ -182,6 +182,9 @@ typedef struct {
     float proj[16], view[16], model[16];   /* object_to_clip = proj * view * model */
     uint32_t depth_only;                   /* keep only the depth layer (shadow-map style views) */
 } swr_view_desc;
+/* frustum_cull: bit 0 (SWR_CULL_FRUSTUM) culls each view's frustum as swr_cull_meshlets does; bit 1
+ * (SWR_CULL_BACKFACE_CONE) adds the backface-cone test of swr_cull_meshlets_ex. */
+#define SWR_CULL_FRUSTUM 1u
 swr_status swr_batch_create(swr_rasterizer r, swr_scene s, uint32_t first, uint32_t count, const swr_view_desc* views,
                             uint32_t num_views, int frustum_cull, swr_batch* out);
 /* New matrices for the same framebuffers (takes effect at the next render; no re-capture). */
@@ -269,6 +272,18 @@ swr_status swr_cull_meshlets(swr_scene s, uint32_t first, uint32_t count, uint16
                              const float proj[16], const float view[16], const float model[16],
                              const float prev_view[16], float frame_width, float frame_height,
                              swr_texture depth_map, uint32_t* visible_count);
+/* swr_cull_meshlets with options. SWR_CULL_BACKFACE_CONE (no counterpart in the reference, whose
+ * records carry the cone but whose CullMeshlets never reads it) also drops meshlets that face away
+ * from the camera as a whole: dot(normalize(ConeApex - eye), ConeAxis) >= ConeCutoff
+ * (meshoptimizer's cone, Scene.h:18-19), tested with a margin so that it never removes a triangle
+ * the rasterizer would draw; the vis-buffer is the same with and without it. Meshlets of
+ * double-sided materials are kept; a projection that mirrors the screen or has no camera centre
+ * (orthographic) turns the test off. */
+#define SWR_CULL_BACKFACE_CONE 2u
+swr_status swr_cull_meshlets_ex(swr_scene s, uint32_t first, uint32_t count, uint16_t* bitmap_device,
+                                const float proj[16], const float view[16], const float model[16],
+                                const float prev_view[16], float frame_width, float frame_height,
+                                swr_texture depth_map, uint32_t* visible_count, uint32_t flags);
 /* texutil::DownsampleDepth(Framebuffer&, Texture2D<R32f>&) (Texture.h:243, ImageHelpers.cpp:150-247). */
 swr_status swr_downsample_depth(swr_framebuffer fb, swr_texture dest);
 /* ShadingContext::Resolve(Rasterizer&, Framebuffer&) (Shading.cpp:658-690): shades the vis-buffer

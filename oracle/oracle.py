@@ -180,6 +180,15 @@ def draw_meshlets(fb: Framebuffer, ctx: Context, count: int, binning=False, clip
     return counters
 
 
+def draw_meshlets_binned(fb: Framebuffer, ctx: Context, count: int, threads: int) -> np.ndarray:
+    """Rasterizer(threads)::DrawMeshlets with binning on, threaded in the reference's shape (meshlets
+    strided over workers, 128x128 bins rasterized by their elected worker); returns the counters."""
+    counters = np.zeros(4, dtype=np.uint64)
+    lib().orc_draw_meshlets_binned(C.byref(fb.s), C.c_uint32(count), C.byref(ctx.s), C.c_uint32(threads),
+                                   _fptr(counters))
+    return counters
+
+
 def cull_meshlets(meshlets: np.ndarray, count: int, proj, view, model, prev_view, frame_w, frame_h,
                   depth_map: Texture | None = None):
     bitmap = np.zeros((count + 15) // 16, dtype=np.uint16)

@@ -112,6 +112,12 @@ void orc_draw_meshlets_rows(orc_framebuffer* fb, uint32_t count, const orc_shadi
 void orc_draw_meshlets_mt(orc_framebuffer* fb, uint32_t count, const orc_shading_context* ctx,
                           const orc_raster_flags* flags, uint32_t num_threads);
 
+// Rasterizer(num_threads)::DrawMeshlets with binning on (Rasterizer.cpp:493-820), threaded in the
+// reference's shape: meshlets strided over workers, 128x128 bins, each bin rasterized by its elected
+// worker. The timed CPU baseline; non-trivial triangles are dropped (binned semantics).
+void orc_draw_meshlets_binned(orc_framebuffer* fb, uint32_t count, const orc_shading_context* ctx, uint32_t num_threads,
+                              uint64_t counters[4]);
+
 // ShadingContext::CullMeshlets (Shading.cpp:775-869).
 uint32_t orc_cull_meshlets(uint16_t* bitmap, const void* meshlets, uint32_t count,
                            const float proj[16], const float view[16], const float model[16],

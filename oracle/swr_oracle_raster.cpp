@@ -4,6 +4,8 @@
 #include "swr_oracle_common.h"
 
 #include <algorithm>
+#include <array>
+#include <atomic>
 #include <thread>
 #include <vector>
 
@@ -552,11 +554,234 @@ static void draw_meshlets(DrawCtx& dc, uint32_t count, const orc_raster_flags* f
     }
 }
 
+// ---------------------------------------------------------------- binned, threaded draw
+// Rasterizer::DrawMeshlets with binning on (Rasterizer.cpp:493-644) and N worker threads, in the
+// reference's work split: worker w shades meshlets w, w+N, w+2N, ... and sets up their packets into
+// its own batch of at most MaxWorkerBatch packets, inserting each packet's accepted lanes into
+// per-(bin, worker) lists of at most MaxBinSize entries over 128x128-pixel bins
+// (DistributeToBins/InsertBin, Rasterizer.cpp:663-700, 759-768). When a worker's batch or one of its
+// bins is full, or it has nothing left, the workers meet at a barrier, worker 0 commits the batches
+// (BinQueue::Commit, 770-790), and each worker rasterizes the bins elected to it, bin b going to
+// worker (b % 64) % N (the elect mask of 505-508), every bin's lists in worker order with each
+// triangle clamped to the bin (RasterizeBin, 701-740). Non-trivial triangles are dropped. This is
+// the timed CPU baseline in the reference's own shape; with several workers, equal-depth ties
+// resolve in bin-list order, as in the reference.
+namespace {
+
+constexpr uint32_t kMaxWorkerBatch = 256, kMaxBinSize = 63, kBinShift = 7, kBinSize = 1u << kBinShift;
+
+struct Packet {  // TrianglePacket as committed to the rasterizer
+    TriSetup lane[16];
+    uint32_t meshletId, basePrim, fsId;
+};
+struct Bin {
+    uint32_t count;
+    uint32_t ids[kMaxBinSize];  // packetIdx << 16 | lane mask
+};
+
+class SpinBarrier {  // a generation barrier (the reference's Barrier, SYNC_SPIN_ONLY)
+public:
+    explicit SpinBarrier(uint32_t n) : n_(n) {}
+    void wait() {
+        const uint32_t gen = gen_.load(std::memory_order_acquire);
+        if (count_.fetch_add(1, std::memory_order_acq_rel) + 1 == n_) {
+            count_.store(0, std::memory_order_relaxed);
+            gen_.fetch_add(1, std::memory_order_acq_rel);
+        } else {
+            while (gen_.load(std::memory_order_acquire) == gen) std::this_thread::yield();
+        }
+    }
+private:
+    uint32_t n_;
+    std::atomic<uint32_t> count_{ 0 }, gen_{ 0 };
+};
+
+}  // namespace
+
+static void draw_meshlets_binned(orc_framebuffer* fb, uint32_t meshCount, const orc_shading_context* sc,
+                                 uint32_t numWorkers, uint64_t counters[4]) {
+    const int halfW = (int)fb->width / 2, halfH = (int)fb->height / 2;
+    const float bx = 2896.0f / (float)fb->width, by = 2896.0f / (float)fb->height;  // guard band always on (509)
+    const uint32_t binsPerRow = (fb->width + kBinSize - 1) >> kBinShift;
+    const uint32_t binsPerFrame = ((fb->height + kBinSize - 1) >> kBinShift) * binsPerRow;
+    const uint32_t bitmapWords = (binsPerFrame + 63) / 64;
+    std::vector<Packet> batch((size_t)kMaxWorkerBatch * numWorkers), committedBatch(batch.size());
+    std::vector<Bin> bins((size_t)binsPerFrame * numWorkers), committedBins(bins.size());
+    for (Bin& b : bins) b.count = 0;
+    for (Bin& b : committedBins) b.count = 0;
+    std::vector<uint64_t> workerBitmap((size_t)bitmapWords * numWorkers, 0), frameBitmap(bitmapWords, 0);
+    uint64_t electMask = 0;
+    for (uint32_t i = 0; i < 64; i += numWorkers) electMask |= 1ull << i;
+    SpinBarrier ready(numWorkers);
+    std::atomic<uint32_t> doneMeshCount{ 0 };
+    std::vector<std::array<uint64_t, 4>> perWorker(numWorkers, std::array<uint64_t, 4>{ 0, 0, 0, 0 });
+
+    auto insert_bin = [&](uint32_t w, uint32_t binId, uint32_t packetIdx, uint32_t mask) {
+        Bin& b = bins[(size_t)binId * numWorkers + w];
+        b.ids[b.count++] = (packetIdx << 16) | mask;
+        workerBitmap[(size_t)w * bitmapWords + binId / 64] |= 1ull << (binId & 63);
+        return b.count < kMaxBinSize;
+    };
+    auto rasterize_bin = [&](uint32_t binId, uint32_t w) {
+        DrawCtx dc = {};
+        dc.fb = fb;
+        dc.sc = sc;
+        dc.halfW = halfW, dc.halfH = halfH;
+        dc.rowBegin = 0, dc.rowEnd = fb->height;
+        dc.counters = nullptr;
+        const uint32_t binX = (binId % binsPerRow) * kBinSize, binY = (binId / binsPerRow) * kBinSize;
+        const uint32_t binMin = binX | (binY << 16), binMax = binMin + kBinSize * 0x00010001u;
+        for (uint32_t wk = 0; wk < numWorkers; wk++) {
+            Bin& b = committedBins[(size_t)binId * numWorkers + wk];
+            for (uint32_t i = 0; i < b.count; i++) {
+                const Packet& pk = committedBatch[b.ids[i] >> 16];
+                const uint32_t mask = b.ids[i] & 0xFFFF;
+                const Meshlet& rec = ((const Meshlet*)sc->meshlets)[sc->meshlet_offset + pk.meshletId];
+                for (uint32_t l = 0; l < 16; l++) {
+                    if (!((mask >> l) & 1)) continue;
+                    uint32_t bbMin, bbMax;
+                    render_bbox(pk.lane[l], halfW, halfH, bbMin, bbMax);
+                    bbMin = max16(bbMin, binMin);
+                    bbMax = min16(bbMax, binMax);
+                    EdgeVars e;
+                    edge_setup(pk.lane[l], halfW, halfH, e);
+                    const uint32_t prim = pk.basePrim + l;
+                    if (pk.fsId != 0) {
+                        const orc_material& mat = sc->materials[rec.MaterialId];
+                        AlphaTri at = {};
+                        if (mat.texture != UINT32_MAX && sc->textures && sc->textures[mat.texture].data)
+                            at.tex = &sc->textures[mat.texture];
+                        at.cutoff = (uint32_t)mat.alpha_cutoff << 24;
+                        for (int k = 0; k < 3; k++) {
+                            const uint32_t tw = texcoord_word(rec, rec.Indices[k][prim]);
+                            at.uv[k][0] = half_to_float(tw & 0xFFFF), at.uv[k][1] = half_to_float(tw >> 16);
+                        }
+                        if (at.tex) {
+                            draw_triangle_alpha(dc, e, bbMin, bbMax, pk.meshletId, prim, at);
+                            continue;
+                        }
+                    }
+                    draw_triangle(dc, e, bbMin, bbMax, pk.meshletId, prim);
+                }
+            }
+            b.count = 0;
+        }
+    };
+
+    auto worker = [&](uint32_t w) {
+        Shaded mesh;
+        mesh.PrimCount = 0;
+        uint32_t meshJobs = 0, nextMeshIdx = w, meshIdx = w, primOffset = 0;
+        uint32_t nextPacketIdx = w * kMaxWorkerBatch;
+        const uint32_t maxPacketIdx = nextPacketIdx + kMaxWorkerBatch;
+        std::array<uint64_t, 4>& cnt = perWorker[w];
+        while (true) {
+            bool batchFull = false, isIdle = true;
+            if (nextMeshIdx < meshCount && primOffset >= mesh.PrimCount) {
+                isIdle = false;
+                meshIdx = nextMeshIdx;
+                nextMeshIdx += numWorkers;
+                meshJobs++;
+                shade_meshlet(sc, meshIdx, mesh);
+                if (mesh.PrimCount == 0) continue;
+                cnt[ORC_TRIS_PROCESSED] += mesh.PrimCount;
+                primOffset = 0;
+            }
+            for (; primOffset < mesh.PrimCount && !batchFull; primOffset += 16) {
+                isIdle = false;
+                Vtx v[3][16];
+                for (uint32_t l = 0; l < 16; l++)
+                    for (uint32_t k = 0; k < 3; k++) v[k][l] = mesh.Pos[preload64_index(mesh.Indices[k][primOffset + l])];
+                ClipCodes cc = compute_clip_codes(v, bx, by);
+                if (primOffset + 16 > mesh.PrimCount) {
+                    const uint16_t trail = (uint16_t)((1u << (mesh.PrimCount % 16)) - 1);
+                    cc.AcceptMask &= trail;
+                    cc.NonTrivialMask &= trail;
+                }
+                if (cc.NonTrivialMask) cnt[ORC_TRIS_CLIPPED] += (uint64_t)__builtin_popcount(cc.NonTrivialMask);
+                if (cc.AcceptMask == 0) continue;
+                Packet& pk = batch[nextPacketIdx];
+                uint32_t accept = 0;
+                for (uint32_t l = 0; l < 16; l++)
+                    if (tri_setup(v[0][l], v[1][l], v[2][l], halfW, halfH, mesh.CullMode, pk.lane[l])) accept |= 1u << l;
+                accept &= cc.AcceptMask;
+                if (accept == 0) continue;
+                cnt[ORC_TRIS_RASTERIZED] += (uint64_t)__builtin_popcount(accept);
+                pk.meshletId = meshIdx, pk.basePrim = primOffset, pk.fsId = mesh.FragmentShaderId;
+                // DistributeToBins: every bin a lane's render box touches
+                uint32_t bMin[16], bMax[16];
+                uint32_t x0 = UINT32_MAX, y0 = UINT32_MAX, x1 = 0, y1 = 0;
+                for (uint32_t l = 0; l < 16; l++) {
+                    if (!((accept >> l) & 1)) continue;
+                    uint32_t lo, hi;
+                    render_bbox(pk.lane[l], halfW, halfH, lo, hi);
+                    bMin[l] = ((lo & 0xFFFF) >> kBinShift) | (((lo >> 16) >> kBinShift) << 16);
+                    const uint32_t hm = hi - 0x00010001u;
+                    bMax[l] = ((hm & 0xFFFF) >> kBinShift) | (((hm >> 16) >> kBinShift) << 16);
+                    x0 = std::min(x0, bMin[l] & 0xFFFF), y0 = std::min(y0, bMin[l] >> 16);
+                    x1 = std::max(x1, bMax[l] & 0xFFFF), y1 = std::max(y1, bMax[l] >> 16);
+                }
+                bool underCap = true;
+                for (uint32_t y = y0; y <= y1; y++)
+                    for (uint32_t x = x0; x <= x1; x++) {
+                        uint32_t m = 0;
+                        for (uint32_t l = 0; l < 16; l++)
+                            if (((accept >> l) & 1) && x >= (bMin[l] & 0xFFFF) && x <= (bMax[l] & 0xFFFF) &&
+                                y >= (bMin[l] >> 16) && y <= (bMax[l] >> 16))
+                                m |= 1u << l;
+                        if (m) underCap &= insert_bin(w, x + y * binsPerRow, nextPacketIdx, m);
+                    }
+                batchFull |= !underCap;
+                batchFull |= nextPacketIdx + 1 >= maxPacketIdx;
+                nextPacketIdx++;
+            }
+            if (batchFull || isIdle) {
+                ready.wait();
+                if (doneMeshCount.load(std::memory_order_acquire) >= meshCount) break;
+                if (w == 0) {
+                    std::swap(committedBatch, batch);
+                    std::swap(committedBins, bins);
+                    std::fill(frameBitmap.begin(), frameBitmap.end(), 0ull);
+                    for (uint32_t i = 0; i < numWorkers; i++)
+                        for (uint32_t j = 0; j < bitmapWords; j++) {
+                            frameBitmap[j] |= workerBitmap[(size_t)i * bitmapWords + j];
+                            workerBitmap[(size_t)i * bitmapWords + j] = 0;
+                        }
+                }
+                ready.wait();
+                for (uint32_t i = 0; i < bitmapWords; i++) {
+                    const uint64_t m = frameBitmap[i] & (electMask << (w % 64));
+                    for (uint64_t bits = m; bits; bits &= bits - 1) rasterize_bin(i * 64 + (uint32_t)__builtin_ctzll(bits), w);
+                    cnt[ORC_BIN_FLUSHES] += (uint64_t)__builtin_popcountll(m);
+                }
+                if (nextMeshIdx >= meshCount && primOffset >= mesh.PrimCount) {
+                    doneMeshCount.fetch_add(meshJobs, std::memory_order_acq_rel);
+                    meshJobs = 0;
+                }
+                nextPacketIdx = w * kMaxWorkerBatch;
+            }
+        }
+    };
+    std::vector<std::thread> threads;
+    for (uint32_t w = 1; w < numWorkers; w++) threads.emplace_back(worker, w);
+    worker(0);
+    for (auto& t : threads) t.join();
+    if (counters)
+        for (const auto& c : perWorker)
+            for (int k = 0; k < 4; k++) counters[k] += c[k];
+}
+
 }  // namespace orc
 
 using namespace orc;
 
 extern "C" {
+
+void orc_draw_meshlets_binned(orc_framebuffer* fb, uint32_t count, const orc_shading_context* ctx, uint32_t num_threads,
+                              uint64_t counters[4]) {
+    draw_meshlets_binned(fb, count, ctx, std::max(1u, std::min(num_threads, 64u)), counters);
+}
+
 
 uint32_t orc_meshlet_size(void) { return (uint32_t)sizeof(Meshlet); }
 
