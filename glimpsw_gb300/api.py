@@ -21,6 +21,7 @@ SWR_OK, SWR_EINVAL, SWR_ECAPACITY, SWR_ETIMEOUT, SWR_ECUDA, SWR_ENOMEM = range(6
 STATUS_NAMES = {0: "SWR_OK", 1: "SWR_EINVAL", 2: "SWR_ECAPACITY", 3: "SWR_ETIMEOUT", 4: "SWR_ECUDA", 5: "SWR_ENOMEM"}
 FORMAT_RGBA8U, FORMAT_R11G11B10F, FORMAT_R32F = 0, 1, 2
 VisBufferShader = 0
+DeferredShader = SHADER_DEFERRED = 1
 OverdrawShader = 2
 # DebugLayer (Shading.h:8) for ShadingContext.resolve_debug
 (DEBUG_NONE, DEBUG_BASE_COLOR, DEBUG_NORMALS, DEBUG_METALLIC_ROUGHNESS, DEBUG_MESHLET_ID, DEBUG_TRIANGLE_ID,
@@ -93,6 +94,10 @@ _SIGS = {
     "swr_scene_upload_meshlets": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32],
     "swr_scene_set_materials": [C.c_void_p, C.c_void_p, C.c_uint32],
     "swr_scene_meshlet_count": [C.c_void_p, C.c_void_p],
+    "swr_scene_meshlets_device": [C.c_void_p, C.c_void_p],
+    "swr_draw_shaded_meshlets": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p],
+    "swr_draw_meshlets_hooked": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int],
+    "swr_fragment_source_get": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p],
     "swr_texture_create": [C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, C.c_void_p],
     "swr_texture_destroy": [C.c_void_p],
     "swr_texture_set_pixels": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32],
@@ -335,6 +340,7 @@ class ShadingContext:
     """ShadingContext (Shading.h:12-50) bound to a device Scene."""
 
     VisBufferShader = VisBufferShader
+    DeferredShader = DeferredShader
     OverdrawShader = OverdrawShader
 
     def __init__(self, scene: Scene, object_to_clip, world_to_clip=None, object_to_world=None,

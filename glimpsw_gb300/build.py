@@ -16,8 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libswr_gb300.so")
 SOURCES = ["swr_api.cu", "swr_raster.cu", "swr_texture.cu", "swr_shade.cu", "swr_batch.cu", "swr_noalloc.cu",
-           "swr_neural.cu", "swr_neural_api.cu", "swr_meshletize.cpp"]
-HEADERS = ["swr_device.cuh", "swr_internal.h", "swr_tc.cuh", "swr_neural.h", "swr_sample.cuh"]
+           "swr_neural.cu", "swr_neural_api.cu", "swr_gbuffer.cu", "swr_meshletize.cpp"]
+HEADERS = ["swr_device.cuh", "swr_internal.h", "swr_tc.cuh", "swr_neural.h", "swr_sample.cuh", "swr_surface.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -37,7 +37,8 @@ def build(force: bool = False, verbose: bool = False) -> str:
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
     deps = srcs + [os.path.join(CSRC, h) for h in HEADERS]
     inc = os.path.join(HERE, "..", "include")
-    deps += [os.path.join(inc, "swr_gb300.h"), os.path.join(inc, "swr", "hostmath.h"), os.path.join(inc, "swr", "approx14.h")]
+    deps += [os.path.join(inc, "swr_gb300.h")]
+    deps += [os.path.join(inc, "swr", h) for h in ("hostmath.h", "approx14.h", "device.cuh", "raster_math.cuh", "shader.cuh")]
     if not force and os.path.exists(LIB) and all(os.path.getmtime(LIB) >= os.path.getmtime(d) for d in deps):
         return LIB
     os.makedirs(BUILD_DIR, exist_ok=True)

@@ -407,6 +407,7 @@ swr_status swr_scene_destroy(swr_scene s) {
     if (!s) return SWR_OK;
     cudaFree(s->meshlets);
     cudaFree(s->materials);
+    cudaFree(s->fsIds);
     delete s;
     return SWR_OK;
 }
@@ -443,7 +444,8 @@ swr_status swr_scene_upload_meshlets(swr_scene s, const void* meshlets, uint32_t
 swr_status swr_scene_set_materials(swr_scene s, const swr_material* materials, uint32_t count) {
     if (!s || (!materials && count)) return fail(SWR_EINVAL, "swr_scene_set_materials: bad argument");
     std::vector<DevMaterial> h(count);
-    bool hasAlpha = false;
+    std::vector<uint8_t> fsIds(count);
+    bool hasAlpha = false, hasAlphaAll = false;
     for (uint32_t i = 0; i < count; i++) {
         DevMaterial& d = h[i];
         memset(&d, 0, sizeof(d));
@@ -454,17 +456,30 @@ swr_status swr_scene_set_materials(swr_scene s, const swr_material* materials, u
             d.tex = materials[i].texture->d;
         }
         hasAlpha = hasAlpha || material_alpha_tested(d);
+        hasAlphaAll = hasAlphaAll || material_alpha_tested_all(d);
+        fsIds[i] = material_alpha_tested(d) ? 1 : 0;
     }
     cudaFree(s->materials);
+    cudaFree(s->fsIds);
     s->materials = nullptr;
+    s->fsIds = nullptr;
     s->num_materials = 0;
     s->hasAlpha = hasAlpha;
+    s->hasAlphaAll = hasAlphaAll;
     s->version++;
     if (count) {
         SWR_CUDA(cudaMalloc(&s->materials, count * sizeof(DevMaterial)));
         SWR_CUDA(cudaMemcpy(s->materials, h.data(), count * sizeof(DevMaterial), cudaMemcpyHostToDevice));
+        SWR_CUDA(cudaMalloc(&s->fsIds, count));
+        SWR_CUDA(cudaMemcpy(s->fsIds, fsIds.data(), count, cudaMemcpyHostToDevice));
     }
     s->num_materials = count;
+    return SWR_OK;
+}
+
+swr_status swr_scene_meshlets_device(swr_scene s, const void** out) {
+    if (!s || !out) return fail(SWR_EINVAL, "swr_scene_meshlets_device: bad argument");
+    *out = s->meshlets;
     return SWR_OK;
 }
 
@@ -475,26 +490,35 @@ swr_status swr_scene_meshlet_count(swr_scene s, uint32_t* out) {
 }
 
 // ------------------------------------------------------------------ draw
-swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t count, uint32_t shader_table,
-                             const swr_shading_context* ctx) {
-    if (!r || !fb || !ctx || !ctx->scene) return fail(SWR_EINVAL, "swr_draw_meshlets: NULL argument");
-    if (shader_table != SWR_SHADER_VISBUFFER && shader_table != SWR_SHADER_OVERDRAW)
-        return fail(SWR_EINVAL, "swr_draw_meshlets: unknown shader table %u", shader_table);
-    const bool overdraw = shader_table == SWR_SHADER_OVERDRAW;
+}  // extern "C"
+
+namespace {
+
+enum class DrawKind { VisBuffer, Overdraw, Hooked };
+
+// One draw's visibility: the mesh stage (ShadeMeshlet, or the records of a user mesh shader) and the
+// chunk stage into the framebuffer's keys. Vis-buffer draws leave the layers pending
+// (layers_stale); overdraw draws finalize their counters; hooked draws start from keys with no
+// pending fragments, so that the fragment stage (swr_fragment_source_get) finds this draw's alone.
+swr_status draw_impl(swr_rasterizer r, swr_framebuffer fb, uint32_t count, const swr_shading_context* ctx, DrawKind kind,
+                     const void* shaded, bool alphaAll, const char* what) {
+    if (!r || !fb || !ctx || !ctx->scene) return fail(SWR_EINVAL, "%s: NULL argument", what);
+    const bool overdraw = kind == DrawKind::Overdraw;
     swr_scene sc = ctx->scene;
     if ((uint64_t)ctx->meshlet_offset + count > sc->count)
-        return fail(SWR_EINVAL, "swr_draw_meshlets: meshlets [%u, %llu) outside the scene's %u", ctx->meshlet_offset,
+        return fail(SWR_EINVAL, "%s: meshlets [%u, %llu) outside the scene's %u", what, ctx->meshlet_offset,
                     (unsigned long long)ctx->meshlet_offset + count, sc->count);
     if (count == 0) return SWR_OK;
+    const bool hasAlpha = !overdraw && (alphaAll ? sc->hasAlphaAll : sc->hasAlpha);
     swr_status st = ensure_scratch(r);
     if (st == SWR_OK) st = size_queue(r, count);
-    if (st == SWR_OK && sc->hasAlpha && !overdraw) st = size_alpha_list(r, count);
+    if (st == SWR_OK && hasAlpha) st = size_alpha_list(r, count);
     if (st != SWR_OK) return st;
     if (overdraw && !fb->counts) SWR_CUDA(cudaMalloc(&fb->counts, (size_t)fb->layer_stride * 8));
-    if (overdraw && (st = swr_internal_finalize(fb)) != SWR_OK) return st;  // its counters add to layer 0
-    if (!fb->keys_valid) {
+    if ((overdraw || kind == DrawKind::Hooked) && (st = swr_internal_finalize(fb)) != SWR_OK) return st;
+    if (!fb->keys_valid || kind == DrawKind::Hooked) {
         launch_init_keys(fb->layers + fb->layer_stride, fb->keys, fb->tileMin, fb->width * fb->height, t_stream);
-        SWR_CHECK_LAUNCH("swr_draw_meshlets: init keys");
+        SWR_CHECK_LAUNCH("draw: init keys");
         fb->keys_valid = true;
     }
     DrawArgs a = {};
@@ -503,7 +527,7 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
     a.numMaterials = sc->num_materials;
     a.meshletOffset = ctx->meshlet_offset;
     a.count = count;
-    a.cullBitmap = ctx->cull_bitmap;
+    a.cullBitmap = shaded ? nullptr : ctx->cull_bitmap;
     memcpy(a.m, ctx->object_to_clip, sizeof(a.m));
     a.halfW = (int)fb->width / 2, a.halfH = (int)fb->height / 2;
     a.width = fb->width, a.height = fb->height;
@@ -516,7 +540,9 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
     a.keys = fb->keys;
     a.tileMin = fb->tileMin;
     a.s = r->scratch;
-    if (!sc->hasAlpha || overdraw) a.s.alphaList = nullptr;  // no alpha pass
+    a.shaded = (const uint8_t*)shaded;
+    a.alphaAll = alphaAll ? 1u : 0u;
+    if (!hasAlpha) a.s.alphaList = nullptr;  // no alpha pass
     if (overdraw) {  // no depth test: no tile depth bounds; counters restart per draw
         a.tileMin = nullptr;
         a.counts = fb->counts;
@@ -524,7 +550,7 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
     }
     SWR_CUDA(cudaMemsetAsync(r->scratch.control, 0, 3 * sizeof(unsigned long long), t_stream));
     launch_draw(a, t_stream, num_sms());
-    SWR_CHECK_LAUNCH("swr_draw_meshlets");
+    SWR_CHECK_LAUNCH(what);
     if (!r->statusPending) {
         SWR_CUDA(cudaMemcpyAsync(r->hostStatus, r->scratch.control + 2, sizeof(unsigned long long),
                                  cudaMemcpyDeviceToHost, t_stream));
@@ -539,6 +565,59 @@ swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t coun
     } else {
         fb->layers_stale = kStaleAll;  // written by the next reader of the layers
     }
+    return SWR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t count, uint32_t shader_table,
+                             const swr_shading_context* ctx) {
+    if (shader_table == SWR_SHADER_DEFERRED) return swr_internal_draw_deferred(r, fb, count, ctx);
+    if (shader_table != SWR_SHADER_VISBUFFER && shader_table != SWR_SHADER_OVERDRAW)
+        return fail(SWR_EINVAL, "swr_draw_meshlets: unknown shader table %u", shader_table);
+    return draw_impl(r, fb, count, ctx, shader_table == SWR_SHADER_OVERDRAW ? DrawKind::Overdraw : DrawKind::VisBuffer,
+                     nullptr, false, "swr_draw_meshlets");
+}
+
+swr_status swr_draw_meshlets_hooked(swr_rasterizer r, swr_framebuffer fb, uint32_t count, const swr_shading_context* ctx,
+                                    int alpha_test_all) {
+    return draw_impl(r, fb, count, ctx, DrawKind::Hooked, nullptr, alpha_test_all != 0, "swr_draw_meshlets_hooked");
+}
+
+swr_status swr_draw_shaded_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t count, const void* shaded_device,
+                                    const swr_shading_context* ctx) {
+    if (!shaded_device && count) return fail(SWR_EINVAL, "swr_draw_shaded_meshlets: NULL records");
+    if (((uintptr_t)shaded_device & 15) != 0) return fail(SWR_EINVAL, "swr_draw_shaded_meshlets: records not 16-byte aligned");
+    return draw_impl(r, fb, count, ctx, DrawKind::Hooked, shaded_device, false, "swr_draw_shaded_meshlets");
+}
+
+swr_status swr_fragment_source_get(swr_rasterizer r, swr_framebuffer fb, uint32_t count, const void* shaded_device,
+                                   const swr_shading_context* ctx, swr_fragment_source* out) {
+    if (!r || !fb || !ctx || !ctx->scene || !out) return fail(SWR_EINVAL, "swr_fragment_source_get: NULL argument");
+    if (!fb->keys_valid) return fail(SWR_EINVAL, "swr_fragment_source_get: no hooked draw into this framebuffer");
+    swr_scene sc = ctx->scene;
+    if (fb->layers_stale != kStaleNone) {  // the draw's depth; layer 0 is the fragment stage's
+        launch_finalize(fb->keys, nullptr, fb->layers + fb->layer_stride, fb->width * fb->height, t_stream);
+        SWR_CHECK_LAUNCH("swr_fragment_source_get: depth");
+        fb->layers_stale = kStaleNone;
+    }
+    memset(out, 0, sizeof(*out));
+    out->keys = (uint64_t*)fb->keys;
+    out->layers = fb->layers;
+    out->width = fb->width, out->height = fb->height, out->layer_stride = fb->layer_stride, out->num_layers = fb->num_layers;
+    out->meshlets = sc->meshlets;
+    out->shaded = shaded_device;
+    out->material_fs_ids = sc->fsIds;
+    out->num_materials = sc->num_materials;
+    out->meshlet_offset = ctx->meshlet_offset, out->count = count;
+    memcpy(out->object_to_clip, ctx->object_to_clip, sizeof(out->object_to_clip));
+    out->guard_x = (float)SWR_MAX_RENDER_SIZE / (float)fb->width;
+    out->guard_y = (float)SWR_MAX_RENDER_SIZE / (float)fb->height;
+    if (!r->enable_binning && !r->enable_guardband) out->guard_x = out->guard_y = 1.0f;
+    out->half_w = (int32_t)fb->width / 2, out->half_h = (int32_t)fb->height / 2;
+    out->clip_mode = (!r->enable_binning && r->enable_clipping) ? 1u : 0u;
     return SWR_OK;
 }
 

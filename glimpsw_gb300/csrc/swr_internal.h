@@ -37,6 +37,11 @@ struct DevMaterial {
 inline __host__ __device__ bool material_alpha_tested(const DevMaterial& m) {
     return m.alpha_cutoff - 1u < 254u && m.has_texture;
 }
+// FS_EncodeGBuffer (Shading.cpp:357-359) alpha-tests every material with a texture (a cutoff of 0
+// passes every texel and stays opaque).
+inline __host__ __device__ bool material_alpha_tested_all(const DevMaterial& m) {
+    return m.alpha_cutoff != 0u && m.has_texture;
+}
 
 #ifdef __CUDACC__
 // Backface-cone culling of one meshlet record (no counterpart in the reference's CullMeshlets; the
@@ -158,7 +163,15 @@ struct DrawArgs {
     // the shading steps read a pixel's key before its atomicMax only for triangles of at most this
     // many tiles (0: for all); set by launch_draw
     uint32_t keyReadTiles;
+    // single view: swr_shaded_meshlet records of a user mesh shader (record i = meshlet i of the
+    // draw) in place of ShadeMeshlet's transform; nullptr for the built-in mesh shader
+    const uint8_t* shaded;
+    // FS_EncodeGBuffer's alpha test: every material with a texture is alpha-tested with its cutoff
+    uint32_t alphaAll;
 };
+
+// swr_shaded_meshlet (ShadedMeshlet, Rasterizer.h:82-99) offsets.
+constexpr uint32_t kShadedSize = 1472, kShadedIndices = 64, kShadedPositions = 448;
 
 // The mesh stage draws a view's meshlets in the order p -> (p * stride) mod count: a Weyl sequence
 // with stride near count / golden ratio (coprime to count), so neighbouring positions, fetched
@@ -218,6 +231,8 @@ struct swr_framebuffer_t {
     uint8_t layers_stale;          // the keys hold draws not yet written to the layers: kStale*
 };
 enum : uint8_t { kStaleNone = 0, kStaleDepth = 1, kStaleAll = 2 };  // kStaleDepth: depth-only views of a batch
+// swr_draw_meshlets with SWR_SHADER_DEFERRED (swr_gbuffer.cu).
+swr_status swr_internal_draw_deferred(swr_rasterizer r, swr_framebuffer fb, uint32_t count, const swr_shading_context* ctx);
 // Writes pending vis-buffer draws from the keys to layers 0 and 1 (k_finalize); every reader or
 // writer of the layers calls it first, so consecutive draws into one framebuffer finalize once.
 swr_status swr_internal_finalize(swr_framebuffer fb);
@@ -228,6 +243,8 @@ struct swr_scene_t {
     swr::DevMaterial* materials;
     uint32_t num_materials;
     bool hasAlpha;                 // some material selects FS_EncodeSurfaceId<true> (swr::material_alpha_tested)
+    bool hasAlphaAll;              // some material is alpha-tested under FS_EncodeGBuffer (material_alpha_tested_all)
+    uint8_t* fsIds;                // device: FragmentShaderId of each material under ShadeMeshlet
     uint64_t version;              // bumped when meshlets or materials move (recorded draw graphs re-capture)
 };
 

@@ -29,6 +29,7 @@
 #include <type_traits>
 
 #include "../../include/swr/approx14.h"
+#include "../../include/swr/raster_math.cuh"
 #include "swr_device.cuh"
 #include "swr_internal.h"
 #include "swr_sample.cuh"
@@ -42,125 +43,27 @@ constexpr int kPacketTiles = 128;  // in-warp tile budget of a 32-triangle step
 constexpr int kSpreadTiles = 4;    // over budget, triangles above this many tiles are queued
 constexpr int kChunkTiles = 8;  // chunk = 8x8 tiles = 32x32 pixels
 
-struct Vtx { float x, y, z, w; };
-
-// ------------------------------------------------------------------ setup (per lane)
-struct Setup {
-    uint32_t Pos0, Pos1, Pos2;
-    float Z0, Z1, Z2;
-    float W0, W1, W2;  // 1 / w of the vertices (simd::perspective_div)
-};
-
-// TrianglePacket::GetBoundingBox / GetRenderBoundingBox (Rasterizer.cpp:331-351).
-__device__ __forceinline__ void render_bbox(const Setup& t, int halfW, int halfH, uint32_t& bbMin, uint32_t& bbMax) {
-    uint32_t minPos = __vmins2(__vmins2(t.Pos0, t.Pos1), t.Pos2);
-    uint32_t maxPos = __vmaxs2(__vmaxs2(t.Pos0, t.Pos1), t.Pos2);
-    minPos = srai16_4(minPos + 0x00070007u);  // 32-bit add, as the reference
-    maxPos = srai16_4(maxPos + 0x00070007u);
-    uint32_t vp = (uint32_t)halfW | ((uint32_t)halfH << 16);
-    uint32_t x = __vmins2(__vmaxs2(__vadd2(minPos, vp), 0u), vp * 2);
-    uint32_t y = __vmins2(__vmaxs2(__vadd2(maxPos, vp), 0u), vp * 2);
-    bbMin = x & ~0x00030003u;
-    bbMax = (y + 0x00030003u) & ~0x00030003u;
-}
-
-// ShadeMeshlet's vertex transform (Shading.cpp:295-298, simd::mul with w = 1, SIMD.h:457-464): the
-// clip position of a vertex slot; slots past the 16-vertex chunks up to NumVertices are zero.
+// ShadeMeshlet's vertex transform (Shading.cpp:295-298): the clip position of a vertex slot; slots
+// past the 16-vertex chunks up to NumVertices are zero.
 __device__ __forceinline__ float4 clip_position(float x, float y, float z, bool live, const ViewParams& vp) {
-    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (live) {
-        c.x = ffma(x, vp.m[0], ffma(y, vp.m[4], ffma(z, vp.m[8], vp.m[12])));
-        c.y = ffma(x, vp.m[1], ffma(y, vp.m[5], ffma(z, vp.m[9], vp.m[13])));
-        c.z = ffma(x, vp.m[2], ffma(y, vp.m[6], ffma(z, vp.m[10], vp.m[14])));
-        c.w = ffma(x, vp.m[3], ffma(y, vp.m[7], ffma(z, vp.m[11], vp.m[15])));
-    }
-    return c;
+    return live ? clip_transform(x, y, z, vp.m) : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-// A vertex after simd::perspective_div (SIMD.h:473-476): x/w, y/w, z/w and 1/w. The correctly
-// rounded reciprocal is the same value as 1.0f / w.
-struct Ndc { float x, y, z, rw; };
-__device__ __forceinline__ Ndc project(float x, float y, float z, float w) {
-    const float rw = __frcp_rn(w);
-    return { fmul(x, rw), fmul(y, rw), fmul(z, rw), rw };
-}
-
-// The face test of TrianglePacket::Setup (Rasterizer.cpp:262-266): the float determinant of the
-// projected vertices, negated for FrontCW or made absolute for None; the triangle is kept if > 0.
-__device__ __forceinline__ bool front_facing(const Ndc& n0, const Ndc& n1, const Ndc& n2, int cullMode) {
-    const float x0 = n0.x, y0 = n0.y, x1 = n1.x, y1 = n1.y, x2 = n2.x, y2 = n2.y;
-    float det = fsub(fmul(fsub(x2, x0), fsub(y1, y0)), fmul(fsub(x0, x1), fsub(y0, y2)));
-    if (cullMode != kCullFrontCCW) {
-        bool flip = (cullMode == kCullFrontCW) ? true : (det < 0);
-        det = flip ? -det : det;
-    }
-    return det > 0;
-}
-
-// TrianglePacket::Setup (Rasterizer.cpp:257-289) from projected vertices; returns the lane's keep bit.
-__device__ __forceinline__ bool tri_setup_ndc(const Ndc& n0, const Ndc& n1, const Ndc& n2, int halfW, int halfH,
-                                              int cullMode, Setup& t, uint32_t& bbMin, uint32_t& bbMax) {
-    const float x0 = n0.x, y0 = n0.y, x1 = n1.x, y1 = n1.y, x2 = n2.x, y2 = n2.y;
-    bool keep = front_facing(n0, n1, n2, cullMode);
-    float fsx = (float)(halfW * 16), fsy = (float)(halfH * 16);
-    int32_t ix0 = round2i(fmul(x0, fsx)), iy0 = round2i(fmul(y0, fsy));
-    int32_t ix1 = round2i(fmul(x1, fsx)), iy1 = round2i(fmul(y1, fsy));
-    int32_t ix2 = round2i(fmul(x2, fsx)), iy2 = round2i(fmul(y2, fsy));
-    t.Pos0 = ((uint32_t)ix0 & 0xFFFF) | ((uint32_t)iy0 << 16);
-    t.Pos1 = ((uint32_t)ix1 & 0xFFFF) | ((uint32_t)iy1 << 16);
-    t.Pos2 = ((uint32_t)ix2 & 0xFFFF) | ((uint32_t)iy2 << 16);
-    render_bbox(t, halfW, halfH, bbMin, bbMax);
-    if (lo16(bbMin) >= lo16(bbMax) || hi16(bbMin) >= hi16(bbMax)) keep = false;
-    t.Z0 = n0.z, t.Z1 = n1.z, t.Z2 = n2.z;
-    t.W0 = n0.rw, t.W1 = n1.rw, t.W2 = n2.rw;
-    return keep;
-}
-
-// TrianglePacket::Setup from clip-space vertices (the clipper's output triangles).
-__device__ __forceinline__ bool tri_setup(Vtx v0, Vtx v1, Vtx v2, int halfW, int halfH, int cullMode, Setup& t,
-                                          uint32_t& bbMin, uint32_t& bbMax) {
-    return tri_setup_ndc(project(v0.x, v0.y, v0.z, v0.w), project(v1.x, v1.y, v1.z, v1.w),
-                         project(v2.x, v2.y, v2.z, v2.w), halfW, halfH, cullMode, t, bbMin, bbMax);
-}
-
-// ComputeEdge (Rasterizer.cpp:291-295), wrapping int32.
-__device__ __forceinline__ int32_t compute_edge(int32_t a, int32_t x, int32_t b, int32_t y) {
-    int32_t w = (int32_t)((uint32_t)a * (uint32_t)x + (uint32_t)b * (uint32_t)y);
-    w = (int32_t)((uint32_t)w + ((a > 0 || (a == 0 && b > 0)) ? 0u : 0xFFFFFFFFu));
-    return w >> 4;
-}
-
-// TriangleEdgeVars::Setup (Rasterizer.cpp:296-329), depth terms (the opaque vis-buffer shader
-// does not read the perspective-correct barycentrics; alpha_ext adds them from *rcpAreaOut).
-// Returns the fixed-point determinant (> 0, or 0 for a triangle degenerate in fixed point).
+// TriangleEdgeVars::Setup (Rasterizer.cpp:296-329) into a TriRec with its rank (the opaque
+// vis-buffer shader does not read the perspective-correct barycentrics; alpha_ext adds them from
+// *rcpAreaOut). Returns the fixed-point determinant (> 0, or 0 for a triangle degenerate in fixed
+// point).
 __device__ __forceinline__ int32_t edge_setup(const Setup& t, int halfW, int halfH, uint32_t bbMin, uint32_t bbMax,
                                               uint32_t rank, TriRec& r, float* rcpAreaOut = nullptr) {
-    int32_t x0 = lo16(t.Pos0), y0 = hi16(t.Pos0);
-    int32_t x1 = lo16(t.Pos1), y1 = hi16(t.Pos1);
-    int32_t x2 = lo16(t.Pos2), y2 = hi16(t.Pos2);
-    int32_t A01 = y1 - y0, B01 = x0 - x1;
-    int32_t A12 = y2 - y1, B12 = x1 - x2;
-    int32_t A20 = y0 - y2, B20 = x2 - x0;
-    int32_t det = (int32_t)((uint32_t)B20 * (uint32_t)A01 - (uint32_t)B01 * (uint32_t)A20);
-    if (det < 0) {
-        A01 = -A01, B01 = -B01, A12 = -A12, B12 = -B12, A20 = -A20, B20 = -B20;
-        det = -det;
-    }
-    int32_t sx = (int32_t)((uint32_t)(-halfW) << 4) + 8, sy = (int32_t)((uint32_t)(-halfH) << 4) + 8;
-    r.E0 = compute_edge(A12, sx - x1, B12, sy - y1);
-    r.E1 = compute_edge(A20, sx - x2, B20, sy - y2);
-    r.E2 = compute_edge(A01, sx - x0, B01, sy - y0);
-    r.A12 = A12, r.B12 = B12, r.A20 = A20, r.B20 = B20, r.A01 = A01, r.B01 = B01;
-    // 16.0f / det: scaling the correctly rounded reciprocal by 16 is exact (|det| >= 1 or 0)
-    float rcpArea = fmul(16.0f, __frcp_rn(__int2float_rn(det)));
-    r.Z0 = t.Z0;
-    r.Z10 = fmul(fsub(t.Z1, t.Z0), rcpArea);
-    r.Z20 = fmul(fsub(t.Z2, t.Z0), rcpArea);
+    const Edges e = edge_vars(t, halfW, halfH);
+    r.E0 = e.E0, r.E1 = e.E1, r.E2 = e.E2;
+    r.A12 = e.A12, r.B12 = e.B12, r.A20 = e.A20, r.B20 = e.B20, r.A01 = e.A01, r.B01 = e.B01;
+    r.Z0 = e.Z0, r.Z10 = e.Z10, r.Z20 = e.Z20;
     r.bbMin = bbMin, r.bbMax = bbMax;
     r.lowword = 0xFFFFFFFEu - rank;
     r.pad = 0;
-    if (rcpAreaOut) *rcpAreaOut = rcpArea;
-    return det;
+    if (rcpAreaOut) *rcpAreaOut = e.rcpArea;
+    return e.det;
 }
 
 
@@ -312,16 +215,8 @@ struct TexCoord { float u, v; };
 
 // Interpolated texcoord of the sample whose edge values are (u, v) (as floats).
 __device__ __forceinline__ TexCoord alpha_texcoord(const AlphaExt& x, float u, float v) {
-    const float pw0 = ffma(fadd(u, v), -x.W0S, x.W0);
-    const float w = ffma(u, x.W1S, ffma(v, x.W2S, pw0));
-    float rcpW = swr_rcp14(w);  // simd::approx_rcp (VRCP14PS, bit-exact)
-    rcpW = fmul(rcpW, ffma(-w, rcpW, 2.0f));  // Newton-Raphson step
-    float bu = fmul(u, fmul(x.W1S, rcpW)), bv = fmul(v, fmul(x.W2S, rcpW));
-    if (x.material & kTriAlpha) {  // clipped: barycentrics of the source triangle
-        const float cu = ffma(bu, x.ru[1], ffma(bv, x.ru[2], x.ru[0]));
-        const float cv = ffma(bu, x.rv[1], ffma(bv, x.rv[2], x.rv[0]));
-        bu = cu, bv = cv;
-    }
+    float bu, bv;  // clipped (kTriAlpha): barycentrics of the source triangle
+    perspective_bary(u, v, x.W0, x.W0S, x.W1S, x.W2S, (x.material & kTriAlpha) != 0, x.ru, x.rv, bu, bv);
     const float b0 = fsub(fsub(1.0f, bu), bv);
     TexCoord s;
     s.u = ffma(h2f(x.tc0 & 0xFFFF), b0, ffma(h2f(x.tc1 & 0xFFFF), bu, fmul(h2f(x.tc2 & 0xFFFF), bv)));
@@ -688,52 +583,17 @@ __device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t out
                                             uint32_t gMeshlet, uint32_t prim, unsigned long long& nRaster,
                                             uint32_t alphaMat, const uint8_t* mp, const uint8_t* idxBytes) {
     const bool alpha = alphaMat != ~0u;
-    const int rows = alpha ? 6 : 4;
-    float V[6][16];  // x, y, z, w and the barycentric u, v of the polygon's vertices
-    V[0][0] = v0.x, V[1][0] = v0.y, V[2][0] = v0.z, V[3][0] = v0.w;
-    V[0][1] = v1.x, V[1][1] = v1.y, V[2][1] = v1.z, V[3][1] = v1.w;
-    V[0][2] = v2.x, V[1][2] = v2.y, V[2][2] = v2.z, V[3][2] = v2.w;
-    V[4][0] = 0.0f, V[4][1] = 1.0f, V[4][2] = 0.0f;
-    V[5][0] = 0.0f, V[5][1] = 0.0f, V[5][2] = 1.0f;
-    uint8_t idx[16] = { 0, 1, 2 };
-    uint32_t vertCount = 3, nextIdx = 3;
-    const float guard[2] = { vp.bx, vp.by };
-
-    for (uint32_t planeId = 0; planeId < 6; planeId++) {
-        if (!((outcodes >> planeId) & 1)) continue;
-        uint8_t out[16];
-        uint32_t outCount = 0;
-        float planeScale = planeId < 4 ? guard[planeId / 2] : 1.0f;
-        for (uint32_t vi = 0; vi < vertCount; vi++) {
-            uint32_t ia = idx[vi], ib = idx[(vi + 1) % vertCount];
-            float aa = V[planeId / 2][ia], ab = V[planeId / 2][ib];
-            if (planeId & 1) aa = -aa, ab = -ab;
-            float da = fadd(aa, fmul(V[3][ia], planeScale));
-            float db = fadd(ab, fmul(V[3][ib], planeScale));
-            // A convex polygon gains at most one vertex per plane (at most 9 vertices, 12 new
-            // ones); a numerically non-convex one could exceed the buffers, which the reference
-            // only asserts (Rasterizer.cpp:441). Such a triangle is dropped and flagged.
-            if (outCount + 2 > 16 || nextIdx >= 16) {
-                atomicOr(&a.s.control[2], kStatusClipOverflow);
-                return;
-            }
-            if (da >= 0) out[outCount++] = (uint8_t)ia;
-            if ((da >= 0) != (db >= 0)) {
-                float t = fdiv(da, fsub(da, db));
-                for (int k = 0; k < rows; k++) V[k][nextIdx] = ffma(V[k][ib], t, ffma(-t, V[k][ia], V[k][ia]));
-                out[outCount++] = (uint8_t)nextIdx++;
-            }
-        }
-        if (vertCount < 3) break;  // stale count check, Rasterizer.cpp:443
-        vertCount = outCount;
-        for (int k = 0; k < 16; k++) idx[k] = out[k];
+    ClipPoly P;
+    if (!clip_polygon(v0, v1, v2, outcodes, vp.bx, vp.by, alpha ? 6 : 4, P)) {
+        atomicOr(&a.s.control[2], kStatusClipOverflow);
+        return;
     }
+    const uint32_t vertCount = P.count;
     if (vertCount < 2) return;
     for (uint32_t vi = 0; vi + 2 < vertCount; vi++) {
-        uint32_t i0 = idx[0], i1 = idx[vi + 1], i2 = idx[vi + 2];
-        Vtx a0 = { V[0][i0], V[1][i0], V[2][i0], V[3][i0] };
-        Vtx a1 = { V[0][i1], V[1][i1], V[2][i1], V[3][i1] };
-        Vtx a2 = { V[0][i2], V[1][i2], V[2][i2], V[3][i2] };
+        Vtx a0, a1, a2;
+        float ru[3], rv[3];
+        clip_fan(P, vi, a0, a1, a2, alpha ? ru : nullptr, rv);
         Setup t;
         uint32_t bbMin, bbMax;
         if (!tri_setup(a0, a1, a2, vp.halfW, vp.halfH, cullMode, t, bbMin, bbMax)) continue;
@@ -745,9 +605,7 @@ __device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t out
         if (alpha) {
             AlphaExt x = alpha_ext(t, rcpArea, texcoord_word(mp, idxBytes[prim]), texcoord_word(mp, idxBytes[128 + prim]),
                                    texcoord_word(mp, idxBytes[256 + prim]), alphaMat | kTriAlpha);
-            const float u0 = V[4][i0], w0 = V[5][i0];  // TriangleClipData, Rasterizer.cpp:455-458
-            x.ru[0] = u0, x.ru[1] = fsub(V[4][i1], u0), x.ru[2] = fsub(V[4][i2], u0);
-            x.rv[0] = w0, x.rv[1] = fsub(V[5][i1], w0), x.rv[2] = fsub(V[5][i2], w0);
+            for (int k = 0; k < 3; k++) x.ru[k] = ru[k], x.rv[k] = rv[k];  // TriangleClipData, Rasterizer.cpp:455-458
             r.pad = viewIndex | kTriAlpha;
             if (!enqueue_alpha(r, x, a, chunk)) raster_serial_alpha(r, x, a.materials, vp.keys, vp.width);
             continue;
@@ -767,21 +625,6 @@ struct LaneTri {
     uint32_t partial;   // OR of the vertices' out codes
     bool acc, nontriv;  // trivially accepted / accepted but needs clipping
 };
-
-// Per-vertex part of Clipper::ComputeClipCodes (Rasterizer.cpp:353-397): the six out-code bits and,
-// in bit 6, the guard-band test |x| < w bx and |y| < w by. A triangle's codes combine its vertices'.
-constexpr uint32_t kCodeInBand = 0x40u;
-__device__ __forceinline__ uint32_t vertex_code(float4 q, const ViewParams& vp) {
-    uint32_t oc = 0;
-    oc |= (q.x < -q.w) ? 1u : 0u;
-    oc |= (q.x > q.w) ? 2u : 0u;
-    oc |= (q.y < -q.w) ? 4u : 0u;
-    oc |= (q.y > q.w) ? 8u : 0u;
-    oc |= (q.z < -q.w) ? 16u : 0u;
-    oc |= (q.z > q.w) ? 32u : 0u;
-    if (fabsf(q.x) < fmul(q.w, vp.bx) && fabsf(q.y) < fmul(q.w, vp.by)) oc |= kCodeInBand;
-    return oc;
-}
 
 __device__ __forceinline__ LaneTri lane_triangle(const float4* ndc, const uint8_t* codes, const uint8_t* idxBytes,
                                                  uint32_t p, bool valid) {
@@ -841,7 +684,11 @@ __device__ __forceinline__ uint32_t draw_order(uint32_t p, uint32_t count, uint3
 }
 
 enum : int { kPassOpaque = 0, kPassAlpha = 1, kPassOverdraw = 2 };
-template <int kPass>
+// kShaded: the meshlets come shaded by a user mesh shader (a.shaded, swr_shaded_meshlet records):
+// clip positions, indices, PrimCount, CullMode and FragmentShaderId are read from the record
+// instead of ShadeMeshlet's transform of the Meshlet (whose texcoords and material the alpha test
+// still reads).
+template <int kPass, bool kShaded = false>
 __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     constexpr bool kAlpha = kPass == kPassAlpha, kOver = kPass == kPassOverdraw;
     using Smem = typename std::conditional<kAlpha, WarpSmemAlpha, WarpSmem>::type;
@@ -953,21 +800,27 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
         const uint8_t* mp = a.meshlets + (size_t)g * kMeshletSize;
         // The record's positions (all 64 slots) and index bytes are loaded together with its header,
         // not after it: one memory round trip per meshlet instead of two.
-        const float* P = (const float*)(mp + kOffPositions);
+        const uint8_t* sp = kShaded ? a.shaded + (size_t)m * kShadedSize : nullptr;
+        const float* P = (const float*)(kShaded ? sp + kShadedPositions : mp + kOffPositions);
         const float px0 = P[lane], py0 = P[64 + lane], pz0 = P[128 + lane];
         const float px1 = P[32 + lane], py1 = P[96 + lane], pz1 = P[160 + lane];
-        const uint32_t* I = (const uint32_t*)(mp + kOffIndices);
+        float pw0 = 1.0f, pw1 = 1.0f;
+        if constexpr (kShaded) pw0 = P[192 + lane], pw1 = P[224 + lane];
+        const uint32_t* I = (const uint32_t*)(kShaded ? sp + kShadedIndices : mp + kOffIndices);
         const uint32_t ix0 = I[lane], ix1 = I[32 + lane], ix2 = I[64 + lane];
-        const uint32_t hdr = *(const uint32_t*)(mp + kOffNumVertices);
+        const uint32_t hdr = *(const uint32_t*)(kShaded ? sp : mp + kOffNumVertices);
         const uint32_t matId = *(const uint32_t*)(mp + kOffMaterialId);
-        const uint32_t nv = hdr & 0xFF, nt = min((hdr >> 8) & 0xFF, 128u);  // record arrays hold 64 / 128
+        // record arrays hold 64 / 128; a shaded meshlet defines all 64 vertex slots
+        const uint32_t nv = kShaded ? 64u : hdr & 0xFF, nt = min((kShaded ? hdr : hdr >> 8) & 0xFF, 128u);
         int cullMode = kCullFrontCCW;
         bool alphaTested = false;  // FragmentShaderId 1
         if (matId != 0xFFFFFFFFu && matId < a.numMaterials) {  // Shading.cpp:302-306
             const DevMaterial& mt = a.materials[matId];
             cullMode = mt.is_double_sided ? kCullNone : kCullFrontCCW;
-            alphaTested = material_alpha_tested(mt);
+            alphaTested = a.alphaAll ? material_alpha_tested_all(mt) : material_alpha_tested(mt);
+            if constexpr (kShaded) alphaTested = alphaTested && ((hdr >> 16) & 0xFF) == 1;
         }
+        if constexpr (kShaded) cullMode = (int)((hdr >> 8) & 0xFF);
         if (kPass == kPassOpaque && alphaTested) {  // drawn by the alpha pass
             if (lane == 0) a.s.alphaList[atomicAdd(&a.s.control[9], 1ull)] = item;
             continue;
@@ -978,14 +831,14 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
         // ShadeMeshlet vertex loop (Shading.cpp:295-298): 16-vertex chunks up to NumVertices; the
         // slots past them are zero.
         const uint32_t nvr = min((nv + 15) & ~15u, 64u);
-        auto xform = [&](uint32_t v, float x, float y, float z) {
-            const float4 c = clip_position(x, y, z, v < nvr, vp);
+        auto xform = [&](uint32_t v, float x, float y, float z, float w) {
+            const float4 c = kShaded ? make_float4(x, y, z, w) : clip_position(x, y, z, v < nvr, vp);
             const Ndc n = project(c.x, c.y, c.z, c.w);
             S.ndc[v] = make_float4(n.x, n.y, n.z, n.rw);
-            S.code[v] = (uint8_t)vertex_code(c, vp);
+            S.code[v] = (uint8_t)vertex_code(c, vp.bx, vp.by);
         };
-        xform(lane, px0, py0, pz0);
-        xform(32 + lane, px1, py1, pz1);
+        xform(lane, px0, py0, pz0, pw0);
+        xform(32 + lane, px1, py1, pz1, pw1);
         S.idx[lane] = ix0, S.idx[32 + lane] = ix1, S.idx[64 + lane] = ix2;
         __syncwarp();
 
@@ -1052,9 +905,9 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                 }
             }
             if (lt.nontriv && a.clipMode) {  // rare: the clip-space vertices are transformed again
-                const float* P = (const float*)(mp + kOffPositions);
                 auto clip_vertex = [&](uint32_t v) {
-                    const float4 c = clip_position(P[v], P[64 + v], P[128 + v], v < nvr, vp);
+                    const float4 c = kShaded ? make_float4(P[v], P[64 + v], P[128 + v], P[192 + v])
+                                             : clip_position(P[v], P[64 + v], P[128 + v], v < nvr, vp);
                     return Vtx{ c.x, c.y, c.z, c.w };
                 };
                 clip_and_queue(clip_vertex(preload64_index(idxBytes[p])), clip_vertex(preload64_index(idxBytes[128 + p])),
@@ -1343,7 +1196,7 @@ uint32_t order_stride(uint32_t count) {
 // because draws may come from several host threads.
 static void raise_smem_limit(int pass, const void* kernel, size_t bytes) {
     static std::mutex mu;
-    static size_t setSize[64][3] = {};
+    static size_t setSize[64][5] = {};
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
     std::lock_guard<std::mutex> lock(mu);
@@ -1380,13 +1233,26 @@ void launch_draw(const DrawArgs& args, cudaStream_t st, int numSMs) {
                                                        a.width, a.views, chunk, a.materials, a.counts, 0u);
         return;
     }
-    {
-        LaunchScope ls("k_draw_meshlets", st);
-        k_draw_meshlets<kPassOpaque><<<grid, warps * 32, smem, st>>>(a);
-    }
-    if (a.s.alphaList) {  // the scene has alpha-tested materials
-        LaunchScope ls("k_draw_meshlets_alpha", st);
-        k_draw_meshlets<kPassAlpha><<<grid, warps * 32, smemAlpha, st>>>(a);
+    if (a.shaded) {  // meshlets shaded by a user mesh shader
+        if (smem > 48 * 1024) raise_smem_limit(3, (const void*)k_draw_meshlets<kPassOpaque, true>, smem);
+        if (a.s.alphaList && smemAlpha > 48 * 1024) raise_smem_limit(4, (const void*)k_draw_meshlets<kPassAlpha, true>, smemAlpha);
+        {
+            LaunchScope ls("k_draw_meshlets_shaded", st);
+            k_draw_meshlets<kPassOpaque, true><<<grid, warps * 32, smem, st>>>(a);
+        }
+        if (a.s.alphaList) {
+            LaunchScope ls("k_draw_meshlets_shaded_alpha", st);
+            k_draw_meshlets<kPassAlpha, true><<<grid, warps * 32, smemAlpha, st>>>(a);
+        }
+    } else {
+        {
+            LaunchScope ls("k_draw_meshlets", st);
+            k_draw_meshlets<kPassOpaque><<<grid, warps * 32, smem, st>>>(a);
+        }
+        if (a.s.alphaList) {  // the scene has alpha-tested materials
+            LaunchScope ls("k_draw_meshlets_alpha", st);
+            k_draw_meshlets<kPassAlpha><<<grid, warps * 32, smemAlpha, st>>>(a);
+        }
     }
     {
         LaunchScope ls("k_raster_big", st);

@@ -25,31 +25,11 @@
 #include "swr_internal.h"
 #include "swr_neural.h"
 #include "swr_sample.cuh"
+#include "swr_surface.cuh"
 
 namespace swr {
 namespace {
 
-struct F3 { float x, y, z; };
-
-__device__ __forceinline__ float approx_rcp(float x) { return swr_rcp14(x); }
-__device__ __forceinline__ float approx_rsqrt(float x) { return swr_rsqrt14(x); }
-__device__ __forceinline__ float approx_sqrt(float x) { return swr_sqrt14(x); }
-__device__ __forceinline__ float mulsign(float x, float y) {
-    return __uint_as_float(__float_as_uint(x) ^ (__float_as_uint(y) & 0x80000000u));
-}
-__device__ __forceinline__ float dot3(F3 a, F3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
-__device__ __forceinline__ F3 normalize3(F3 a) {
-    float r = approx_rsqrt(dot3(a, a));
-    return { a.x * r, a.y * r, a.z * r };
-}
-__device__ __forceinline__ float lerpf(float a, float b, float t) { return fmaf(t, b, fmaf(-t, a, a)); }
-__device__ __forceinline__ F3 xform4(const float* m, F3 p, float& w) {  // simd::mul(mat4, (p, 1))
-    F3 r = { fmaf(p.x, m[0], fmaf(p.y, m[4], fmaf(p.z, m[8], 1.0f * m[12]))),
-             fmaf(p.x, m[1], fmaf(p.y, m[5], fmaf(p.z, m[9], 1.0f * m[13]))),
-             fmaf(p.x, m[2], fmaf(p.y, m[6], fmaf(p.z, m[10], 1.0f * m[14]))) };
-    w = fmaf(p.x, m[3], fmaf(p.y, m[7], fmaf(p.z, m[11], 1.0f * m[15])));
-    return r;
-}
 
 // =========================================================================== culling
 struct CullArgs {
@@ -260,14 +240,6 @@ __device__ __forceinline__ uint32_t sat_u8(int32_t v) { return (uint32_t)min(max
 __device__ __forceinline__ float unpack_f11(uint32_t x) { x <<= 17; return __uint_as_float((x & 0x0FFE0000u) + 0x38000000u); }
 __device__ __forceinline__ float unpack_f10(uint32_t x) { x <<= 18; return __uint_as_float((x & 0x0FFC0000u) + 0x38000000u); }
 __device__ __forceinline__ F3 unpack_r11(uint32_t p) { return { unpack_f11(p >> 21), unpack_f11(p >> 10), unpack_f10(p) }; }
-__device__ __forceinline__ F3 unmap_oct(float u, float v) {
-    u = u * 2.0f - 1.0f, v = v * 2.0f - 1.0f;
-    F3 n = { u, v, 1.0f - fabsf(u) - fabsf(v) };
-    float t = vmax(-n.z, 0.0f);
-    n.x -= mulsign(t, n.x);
-    n.y -= mulsign(t, n.y);
-    return normalize3(n);
-}
 
 // SampleOctLevel<EnvSampler>(dir, 1) on an R11G11B10 map (Texture.h:467-480; level 1 has no fraction).
 __device__ F3 sample_env(const DevTexture& t, F3 dir) {

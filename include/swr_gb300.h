@@ -45,6 +45,18 @@ typedef struct swr_texture_t* swr_texture;
 /* ShadingContext::VisBufferShader (Shading.cpp:649-654): mesh shader ShadeMeshlet with fragment
  * entry points FS_EncodeSurfaceId<false> (0) and FS_EncodeSurfaceId<true> (1). */
 #define SWR_SHADER_VISBUFFER 0u
+/* ShadingContext::DeferredShader (Shading.cpp:655): ShadeMeshlet with FS_EncodeGBuffer (344-414) for
+ * every fragment entry point. A fragment survives the depth test and, when its material has a
+ * texture, the alpha test texel alpha >= AlphaCutoff (for every material, cutoff 255 included); the
+ * front-most survivor writes depth (layer 1), its base colour (layer 0) and, for two-layer
+ * textures, the packed octahedral normal and metal/roughness (layer 2; 0 otherwise). Needs a
+ * framebuffer of 3 layers. Shading runs after visibility (the fragment stage of the shader hooks,
+ * swr/shader.cuh), so only the visible fragment of each pixel is shaded. Defined deviations: a
+ * material without a texture (the reference dereferences it) passes the alpha test with base colour
+ * 0xFFFFFFFF and layer 2 = 0; a visible surface without a material stores its depth and leaves
+ * layers 0 and 2 as they were (where the reference keeps the colour of the last material fragment
+ * drawn there, which may lie behind it). */
+#define SWR_SHADER_DEFERRED 1u
 /* ShadingContext::OverdrawShader (Shading.cpp:656): FS_Overdraw (333-342) for every fragment entry
  * point. No depth test: each 4x4 tile a triangle covers adds 1 to the high 16 bits of its covered
  * pixels' layer-0 words and 1 to the low 16 bits of the others (saturating), and layer 1 keeps the
@@ -145,6 +157,61 @@ swr_status swr_rasterizer_reset_counters(swr_rasterizer r);
  * first-submitted triangle of a single-threaded draw. */
 swr_status swr_draw_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t count, uint32_t shader_table,
                              const swr_shading_context* ctx);
+
+/* ---- Shader hooks (Rasterizer.h:82-138, 178-196) ----
+ * The reference binds a mesh shader MeshFn(ctx, idx, ShadedMeshlet&) and up to four fragment
+ * shaders FragFn(ctx, Framebuffer&, FragmentVars&) as CPU function pointers. On the GPU they are
+ * __device__ functors instantiated into the kernels of the header-only swr/shader.cuh
+ * (swr::DrawMeshlets<MeshFn, FragFn...>), which drives the entry points below. */
+
+/* ShadedMeshlet (Rasterizer.h:82-99), the reference's layout: 1472 bytes, 64-byte aligned. */
+typedef struct {
+    uint8_t prim_count;          /* PrimCount (0: nothing is drawn) */
+    uint8_t cull_mode;           /* FaceCullMode: 0 None, 1 FrontCCW, 2 FrontCW */
+    uint8_t fragment_shader_id;  /* FragmentShaderId: entry point 0-3 of the fragment stage */
+    uint8_t pad[61];
+    uint8_t indices[3][128];     /* Indices: vertex slots of each primitive */
+    float position[4][64];       /* Position: clip-space x, y, z, w of each vertex slot */
+} swr_shaded_meshlet;
+
+/* Rasterizer::DrawMeshlets for meshlets a mesh shader has already shaded: shaded_device holds count
+ * swr_shaded_meshlet records (device memory), record i standing for meshlet ctx->meshlet_offset + i of
+ * the scene (whose texcoords and material the alpha test of FragmentShaderId 1 reads). Visibility
+ * only: the depth test, alpha test and tie rules of swr_draw_meshlets; the keys stay pending for
+ * swr_fragment_source_get. ctx->cull_bitmap and ctx->object_to_clip are not used (the mesh shader
+ * culls by PrimCount 0 and transforms). Single view. */
+swr_status swr_draw_shaded_meshlets(swr_rasterizer r, swr_framebuffer fb, uint32_t count, const void* shaded_device,
+                                    const swr_shading_context* ctx);
+
+/* Everything the fragment stage of swr/shader.cuh needs to rebuild the visible fragments of one
+ * draw, in device memory. */
+typedef struct {
+    uint64_t* keys;                  /* per-pixel vis-buffer keys (4x4-tiled like the layers) */
+    uint32_t* layers;                /* layer k at layers + k * layer_stride */
+    uint32_t width, height, layer_stride, num_layers;
+    const void* meshlets;            /* the scene's Meshlet records */
+    const void* shaded;              /* the draw's swr_shaded_meshlet records, or NULL (built-in ShadeMeshlet) */
+    const uint8_t* material_fs_ids;  /* FragmentShaderId of each material under ShadeMeshlet (0 or 1) */
+    uint32_t num_materials;
+    uint32_t meshlet_offset, count;  /* the draw's meshlets: [meshlet_offset, meshlet_offset + count) */
+    float object_to_clip[16];        /* ShadeMeshlet's transform (built-in mesh shader) */
+    float guard_x, guard_y;          /* guard-band factors of the clipper */
+    int32_t half_w, half_h;
+    uint32_t clip_mode;              /* non-trivial triangles were clipped (1) or dropped (0) */
+} swr_fragment_source;
+
+/* Writes the depth of the draw's visible fragments to layer 1 and fills *out for the fragment stage
+ * of the draw just made with swr_draw_meshlets_hooked or swr_draw_shaded_meshlets (count meshlets
+ * from ctx->meshlet_offset; shaded_device as given to the draw, or NULL). The fragment stage then
+ * shades every pixel whose visible fragment belongs to the draw and marks the pixel done. */
+swr_status swr_fragment_source_get(swr_rasterizer r, swr_framebuffer fb, uint32_t count, const void* shaded_device,
+                                   const swr_shading_context* ctx, swr_fragment_source* out);
+
+/* The visibility part of swr_draw_meshlets for a draw whose fragment stage is user code
+ * (swr/shader.cuh): mesh shader ShadeMeshlet, depth and alpha tests as SWR_SHADER_VISBUFFER (with
+ * alpha_test_all, as SWR_SHADER_DEFERRED: every textured material's texel alpha >= its cutoff). */
+swr_status swr_draw_meshlets_hooked(swr_rasterizer r, swr_framebuffer fb, uint32_t count,
+                                    const swr_shading_context* ctx, int alpha_test_all);
 
 /* No counterpart in the reference. The vis-buffer draw of swr_draw_meshlets for callers that
  * cannot allocate device memory (their memory belongs to another allocator, or they run where
@@ -247,6 +314,9 @@ swr_status swr_scene_destroy(swr_scene s);
 swr_status swr_scene_upload_meshlets(swr_scene s, const void* meshlets, uint32_t first, uint32_t count);
 swr_status swr_scene_set_materials(swr_scene s, const swr_material* materials, uint32_t count);
 swr_status swr_scene_meshlet_count(swr_scene s, uint32_t* out);
+/* The device copy of the records (ShadingContext::Meshlets, Shading.h:13), for user shaders
+ * (swr/shader.cuh) that read the meshlets' attributes; valid until the next upload grows the pool. */
+swr_status swr_scene_meshlets_device(swr_scene s, const void** out);
 
 /* ---- Textures (Texture.h:314-636) ---- */
 /* CreateTexture2D<format>(width, height, maxLevels, numLayers): power-of-two sizes. */

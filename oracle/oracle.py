@@ -57,7 +57,7 @@ class OrcRasterFlags(C.Structure):
                 ("shader", C.c_int)]
 
 
-SHADER_VISBUFFER, SHADER_OVERDRAW = 0, 2
+SHADER_VISBUFFER, SHADER_DEFERRED, SHADER_OVERDRAW, SHADER_TEXCOORD = 0, 1, 2, 3
 
 
 def lib():

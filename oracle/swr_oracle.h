@@ -75,12 +75,14 @@ typedef struct {
 } orc_shading_context;
 
 // Rasterizer flags (Rasterizer.h:205-208) and the shader table of the draw: 0 VisBufferShader,
-// 2 OverdrawShader (Shading.cpp:649-656).
+// 1 DeferredShader, 2 OverdrawShader (Shading.cpp:649-656), and 3, the texcoord shader of the
+// shader-hook tests (depth test; depth, surface id, and the bits of the interpolated texcoords in
+// layers 2 and 3).
 typedef struct {
     int enable_binning, enable_clipping, enable_guardband;
     int shader;
 } orc_raster_flags;
-enum { ORC_SHADER_VISBUFFER = 0, ORC_SHADER_OVERDRAW = 2 };
+enum { ORC_SHADER_VISBUFFER = 0, ORC_SHADER_DEFERRED = 1, ORC_SHADER_OVERDRAW = 2, ORC_SHADER_TEXCOORD = 3 };
 
 // PerfCounter (Rasterizer.h:366-370): processed, rasterized, clipped, bin flushes.
 enum { ORC_TRIS_PROCESSED = 0, ORC_TRIS_RASTERIZED = 1, ORC_TRIS_CLIPPED = 2, ORC_BIN_FLUSHES = 3 };

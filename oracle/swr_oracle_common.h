@@ -107,5 +107,8 @@ static inline float half_to_float(uint32_t h) {
 // Texture2D::SampleLevel<SurfaceSampler> on an RGBA8 texture for the 16 lanes of a 4x4 tile
 // (u, v, mip levels per lane; the filter is chosen over all 16), swr_oracle_resolve.cpp.
 void sample_rgba8(const orc_texture& t, const float* u, const float* v, int layer, const int32_t* mipIn, uint32_t* out);
+// FS_EncodeGBuffer's shading after its depth test for the 16 lanes of a tile, swr_oracle_resolve.cpp.
+uint32_t gbuffer_tile(const orc_shading_context* sc, const void* meshletRecord, const uint32_t vid[3], const float* bu,
+                      const float* bv, uint32_t mask, uint32_t* baseColor, uint32_t* ch2);
 
 }  // namespace orc

@@ -317,6 +317,93 @@ static void draw_triangle_alpha(DrawCtx& dc, const EdgeVars& e, uint32_t bbMin, 
     }
 }
 
+// DrawTriangle<FragFn> (Rasterizer.h:250-328) for the fragment shaders that need the full
+// FragmentVars: FS_EncodeGBuffer (kind ORC_SHADER_DEFERRED, Shading.cpp:344-414) and the texcoord
+// shader of the shader-hook tests (ORC_SHADER_TEXCOORD: depth test, depth, surface id in layer 0 and
+// the bits of the interpolated texcoords, FragmentVars::Interpolate of Mesh::TexCoords[VertexId],
+// in layers 2 and 3). Per 4x4 tile with a covered sample: depth test, then the perspective-correct
+// barycentrics of all 16 lanes (rcp14 + Newton step, clip remap, Rasterizer.h:300-317).
+static void draw_triangle_frag(DrawCtx& dc, const EdgeVars& e, uint32_t bbMin, uint32_t bbMax, uint32_t meshletId,
+                               uint32_t primId, const uint8_t vid8[3], const float* ru, const float* rv, int kind) {
+    orc_framebuffer* fb = dc.fb;
+    const uint32_t minX = bbMin & 0xFFFF, minY = bbMin >> 16, maxX = bbMax & 0xFFFF, maxY = bbMax >> 16;
+    float* depthBuf = (float*)&fb->data[1 * fb->layer_stride];
+    uint32_t* colorBuf = &fb->data[0];
+    const uint32_t g = dc.sc->meshlet_offset + meshletId;
+    const Meshlet& mesh = ((const Meshlet*)dc.sc->meshlets)[g];
+    const uint32_t vid[3] = { vid8[0], vid8[1], vid8[2] };
+    for (uint32_t ty = std::max(minY, dc.rowBegin & ~3u); ty < maxY && ty < dc.rowEnd; ty += 4) {
+        for (uint32_t tx = minX; tx < maxX; tx += 4) {
+            float u[16], v[16], depth[16];
+            uint32_t mask = 0;
+            for (uint32_t l = 0; l < 16; l++) {
+                const uint32_t x = tx + (l & 3), y = ty + (l >> 2);
+                const int32_t e0 = (int32_t)((uint32_t)e.Edge0 + (uint32_t)e.A12 * x + (uint32_t)e.B12 * y);
+                const int32_t e1 = (int32_t)((uint32_t)e.Edge1 + (uint32_t)e.A20 * x + (uint32_t)e.B20 * y);
+                const int32_t e2 = (int32_t)((uint32_t)e.Edge2 + (uint32_t)e.A01 * x + (uint32_t)e.B01 * y);
+                if ((e0 | e1 | e2) >= 0) mask |= 1u << l;
+                u[l] = (float)e1, v[l] = (float)e2;
+                depth[l] = std::fma(u[l], e.Z10, std::fma(v[l], e.Z20, e.Z0));
+            }
+            if (mask == 0) continue;
+            for (uint32_t l = 0; l < 16; l++) {  // depth test; rows this call does not own are never written
+                const uint32_t y = ty + (l >> 2);
+                if (!((mask >> l) & 1)) continue;
+                if (y < dc.rowBegin || y >= dc.rowEnd || !(depth[l] > depthBuf[pixel_offset(fb, tx + (l & 3), y)]))
+                    mask &= ~(1u << l);
+            }
+            if (mask == 0) continue;
+            float bu[16], bv[16];
+            for (uint32_t l = 0; l < 16; l++) {
+                const float pw0 = std::fma(u[l] + v[l], -e.W0S, e.W0);
+                const float w = std::fma(u[l], e.W1S, std::fma(v[l], e.W2S, pw0));
+                float rcpW = approx_rcp(w);
+                rcpW *= std::fma(-w, rcpW, 2.0f);
+                bu[l] = u[l] * (e.W1S * rcpW);
+                bv[l] = v[l] * (e.W2S * rcpW);
+                if (ru) {
+                    const float cu = std::fma(bu[l], ru[1], std::fma(bv[l], ru[2], ru[0]));
+                    const float cv = std::fma(bu[l], rv[1], std::fma(bv[l], rv[2], rv[0]));
+                    bu[l] = cu, bv[l] = cv;
+                }
+            }
+            uint32_t out0[16], out2[16], out3[16];
+            bool writeColor = true;
+            if (kind == ORC_SHADER_DEFERRED) {
+                if (mesh.MaterialId == UINT32_MAX) {
+                    writeColor = false;  // Shading.cpp:350-353: depth only
+                } else {
+                    mask = gbuffer_tile(dc.sc, &mesh, vid, bu, bv, mask, out0, out2);
+                }
+            } else {
+                float tc[3][2];
+                for (int k = 0; k < 3; k++) {
+                    uint32_t w = 0;
+                    if (832u + 4u * vid[k] < sizeof(Meshlet)) memcpy(&w, (const uint8_t*)&mesh + 832 + 4 * vid[k], 4);
+                    tc[k][0] = half_to_float(w & 0xFFFF), tc[k][1] = half_to_float(w >> 16);
+                }
+                for (uint32_t l = 0; l < 16; l++) {
+                    const float b0 = 1 - bu[l] - bv[l];
+                    const float su = std::fma(tc[0][0], b0, std::fma(tc[1][0], bu[l], tc[2][0] * bv[l]));
+                    const float sv = std::fma(tc[0][1], b0, std::fma(tc[1][1], bu[l], tc[2][1] * bv[l]));
+                    out0[l] = g * 128u + primId;
+                    memcpy(&out2[l], &su, 4);
+                    memcpy(&out3[l], &sv, 4);
+                }
+            }
+            for (uint32_t l = 0; l < 16; l++) {
+                if (!((mask >> l) & 1)) continue;
+                const uint32_t off = pixel_offset(fb, tx + (l & 3), ty + (l >> 2));
+                depthBuf[off] = depth[l];
+                if (!writeColor) continue;
+                colorBuf[off] = out0[l];
+                if (fb->num_layers > 2) fb->data[2 * fb->layer_stride + off] = out2[l];
+                if (kind == ORC_SHADER_TEXCOORD && fb->num_layers > 3) fb->data[3 * fb->layer_stride + off] = out3[l];
+            }
+        }
+    }
+}
+
 // DrawTriangle<FS_Overdraw> (Rasterizer.h:250-328, Shading.cpp:333-342): no depth test; every tile
 // of the box with a covered sample adds 1 to the high 16 bits of its covered pixels' colour words
 // and 1 to the low 16 bits of the others (saturating, _mm512_adds_epu16), and stores
@@ -486,7 +573,8 @@ static void draw_meshlets(DrawCtx& dc, uint32_t count, const orc_raster_flags* f
         const orc_texture* alphaTex = nullptr;
         uint32_t cutoff = 0;
         const bool overdraw = flags->shader == ORC_SHADER_OVERDRAW;  // one entry point for every FS id (Rasterizer.h:356-360)
-        if (mesh.FragmentShaderId != 0 && !overdraw) {
+        const int fragKind = (flags->shader == ORC_SHADER_DEFERRED || flags->shader == ORC_SHADER_TEXCOORD) ? flags->shader : 0;
+        if (mesh.FragmentShaderId != 0 && !overdraw && !fragKind) {
             const orc_material& mat = sc->materials[mesh.MaterialId];
             if (mat.texture != UINT32_MAX && sc->textures && sc->textures[mat.texture].data) alphaTex = &sc->textures[mat.texture];
             cutoff = (uint32_t)mat.alpha_cutoff << 24;
@@ -528,9 +616,13 @@ static void draw_meshlets(DrawCtx& dc, uint32_t count, const orc_raster_flags* f
                     render_bbox(t, halfW, halfH, bbMin, bbMax);
                     EdgeVars e;
                     edge_setup(t, halfW, halfH, e);
+                    const uint32_t p = primOffset + l;
                     if (overdraw) draw_triangle_overdraw(dc, e, bbMin, bbMax);
-                    else if (alphaTex) draw_triangle_alpha(dc, e, bbMin, bbMax, meshIdx, primOffset + l, alpha_tri(primOffset + l, nullptr));
-                    else draw_triangle(dc, e, bbMin, bbMax, meshIdx, primOffset + l);
+                    else if (fragKind) {
+                        const uint8_t vid[3] = { mesh.Indices[0][p], mesh.Indices[1][p], mesh.Indices[2][p] };
+                        draw_triangle_frag(dc, e, bbMin, bbMax, meshIdx, p, vid, nullptr, nullptr, fragKind);
+                    } else if (alphaTex) draw_triangle_alpha(dc, e, bbMin, bbMax, meshIdx, p, alpha_tri(p, nullptr));
+                    else draw_triangle(dc, e, bbMin, bbMax, meshIdx, p);
                     if (dc.counters) dc.counters[ORC_TRIS_RASTERIZED]++;
                 }
             }
@@ -545,7 +637,10 @@ static void draw_meshlets(DrawCtx& dc, uint32_t count, const orc_raster_flags* f
                     edge_setup(co.t, halfW, halfH, e);
                     uint32_t prim = primOffset + co.primId;
                     if (overdraw) draw_triangle_overdraw(dc, e, bbMin, bbMax);
-                    else if (alphaTex) draw_triangle_alpha(dc, e, bbMin, bbMax, meshIdx, prim, alpha_tri(prim, &co));
+                    else if (fragKind) {
+                        const uint8_t vid[3] = { mesh.Indices[0][prim], mesh.Indices[1][prim], mesh.Indices[2][prim] };
+                        draw_triangle_frag(dc, e, bbMin, bbMax, meshIdx, prim, vid, co.ru, co.rv, fragKind);
+                    } else if (alphaTex) draw_triangle_alpha(dc, e, bbMin, bbMax, meshIdx, prim, alpha_tri(prim, &co));
                     else draw_triangle(dc, e, bbMin, bbMax, meshIdx, prim);
                     if (dc.counters) dc.counters[ORC_TRIS_RASTERIZED]++;
                 }

@@ -185,6 +185,84 @@ inline F3 bary_lerp(const float* b, F3 a0, F3 a1, F3 a2) {  // BaryLerp, Rasteri
              std::fma(a0.z, b[0], std::fma(a1.z, b[1], a2.z * b[2])) };
 }
 
+}  // namespace
+
+// FS_EncodeGBuffer (Shading.cpp:344-414) after its depth test, for the 16 lanes of a tile: the
+// caller gives the perspective-correct barycentrics of every lane (bu, bv) and the lanes that passed
+// the depth test (mask); returns the lanes that also pass the alpha test, with their base colour
+// and packed layer-2 word. A material without a texture (the reference dereferences it) passes
+// every lane with base colour 0xFFFFFFFF and layer 2 = 0.
+uint32_t gbuffer_tile(const orc_shading_context* sc, const void* meshletRecord, const uint32_t vid[3], const float* bu,
+                      const float* bv, uint32_t mask, uint32_t* baseColor, uint32_t* ch2) {
+    const Meshlet& mesh = *(const Meshlet*)meshletRecord;
+    const orc_material& mat = sc->materials[mesh.MaterialId];
+    const orc_texture* tex = (mat.texture != UINT32_MAX && sc->textures && sc->textures[mat.texture].data)
+                                 ? &sc->textures[mat.texture] : nullptr;
+    for (int l = 0; l < L; l++) baseColor[l] = 0xFFFFFFFFu, ch2[l] = 0;
+    if (!tex) return mask;
+    // Mesh::TexCoords / NormalTangents [VertexId]: index bytes past the arrays read the record's
+    // following words (0 past the record)
+    const uint8_t* rec = (const uint8_t*)meshletRecord;
+    auto word = [&](uint32_t offset, uint32_t idx) -> uint32_t {
+        uint32_t w = 0;
+        if (offset + 4 * idx < sizeof(Meshlet)) memcpy(&w, rec + offset + 4 * idx, 4);
+        return w;
+    };
+    const uint32_t offTC = (uint32_t)offsetof(Meshlet, TexCoords), offNT = (uint32_t)offsetof(Meshlet, NormalTangents);
+    float b[L][3], u[L], v[L], su[L], sv[L];
+    float tc[3][2];
+    for (int k = 0; k < 3; k++) {  // UnpackHalf2x16 (Shading.cpp:228-231)
+        const uint32_t w = word(offTC, vid[k]);
+        tc[k][0] = half_to_float(w & 0xFFFF), tc[k][1] = half_to_float(w >> 16);
+    }
+    for (int l = 0; l < L; l++) {
+        b[l][0] = 1 - bu[l] - bv[l], b[l][1] = bu[l], b[l][2] = bv[l];
+        u[l] = std::fma(tc[0][0], b[l][0], std::fma(tc[1][0], b[l][1], tc[2][0] * b[l][2]));
+        v[l] = std::fma(tc[0][1], b[l][0], std::fma(tc[1][1], b[l][1], tc[2][1] * b[l][2]));
+        su[l] = u[l] * tex->scale_lerp_u, sv[l] = v[l] * tex->scale_lerp_v;
+    }
+    // SampleImplicitLod (Texture.h:403-410): CalcMipLevel(grad) - LerpFracBits
+    int32_t mip[L];
+    for (int l = 0; l < L; l++) {
+        float gx = su[l | 1] - su[l & ~1], gy = sv[l | 1] - sv[l & ~1];
+        float gz = su[l | 4] - su[l & ~4], gw = sv[l | 4] - sv[l & ~4];
+        mip[l] = (ilog2_x86(vmax(std::fma(gx, gx, gy * gy), std::fma(gz, gz, gw * gw))) >> 1) - 8;
+    }
+    sample_rgba8(*tex, u, v, 0, mip, baseColor);
+    for (int l = 0; l < L; l++)
+        if (baseColor[l] < ((uint32_t)mat.alpha_cutoff << 24)) mask &= ~(1u << l);  // Shading.cpp:357-358
+    if (!mask || tex->num_layers < 2) return mask;
+    uint32_t nmr[L];
+    sample_rgba8(*tex, u, v, 1, mip, nmr);
+    F3 n[3], t[3];
+    for (int k = 0; k < 3; k++) {  // UnpackNormalTangent (Shading.cpp:232-236)
+        const F4 o = unpack_rgba8(word(offNT, vid[k]));
+        n[k] = unmap_oct(o.x, o.y);
+        t[k] = unmap_oct(o.z, o.w);
+    }
+    const uint32_t hand = (uint32_t)((mesh.TangentHandedness >> (vid[0] & 63)) & 1) << 31;
+    for (int l = 0; l < L; l++) {
+        const float tx = (float)(nmr[l] & 255) * (1.0f / 127.5f) - 1.0f;
+        const float ty = (float)((nmr[l] >> 8) & 255) * (1.0f / 127.5f) - 1.0f;
+        const float tz = approx_sqrt(1.0f - (tx * tx + ty * ty));
+        const F3 N = normalize3(mul3(sc->object_to_world, bary_lerp(b[l], n[0], n[1], n[2])));
+        const F3 T = normalize3(mul3(sc->object_to_world, bary_lerp(b[l], t[0], t[1], t[2])));
+        F3 B = { std::fma(N.y, T.z, -N.z * T.y), std::fma(N.z, T.x, -N.x * T.z), std::fma(N.x, T.y, -N.y * T.x) };
+        B = { u2f(f2u(B.x) ^ hand), u2f(f2u(B.y) ^ hand), u2f(f2u(B.z) ^ hand) };
+        const F3 R = normalize3({ tx * T.x + ty * B.x + tz * N.x, tx * T.y + ty * B.y + tz * N.y, tx * T.z + ty * B.z + tz * N.z });
+        float ou, ov;
+        map_oct(R, ou, ov);
+        uint32_t c = (uint32_t)(ou * 1023.0f + 0.5f);  // conv<uint32_t>: truncation
+        c |= (uint32_t)(ov * 1023.0f + 0.5f) << 10;
+        c |= ((nmr[l] >> 18) & 0x3F) << 20;
+        c |= ((nmr[l] >> 26) & 0x3F) << 26;
+        ch2[l] = c;
+    }
+    return mask;
+}
+
+namespace {
+
 // ResolveSurface (Shading.cpp:471-579) + IntersectTriangle (417-464), 16 lanes.
 void resolve_surface(const orc_shading_context* sc, const uint32_t* ids, uint16_t active, const float* su, const float* sv,
                      float W, float H, Surface* out) {
