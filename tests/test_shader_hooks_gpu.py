@@ -104,8 +104,8 @@ def test_user_mesh_shader_bit_exact(hooks):
     """CustomMesh: its own transform (here the view's), PrimCount 0 for meshlets 4 mod 5, double-sided
     for 0 mod 3, FragmentShaderId idx & 1 (entry point 1 sets bit 30 of the surface id)."""
     from glimpsw_gb300 import api
-    sc = scenes.volume_scene(n=3000, width=480, height=272, n_materials=4, extent=12.0, texture_size=8, env_size=8)
-    view = scenes.make_view(480, 272, eye=(0.0, 0.0, -20.0), target=(0.5, 0.3, 0.0))
+    sc = scenes.grid_scene(n_side=32, width=640, height=360)
+    view = sc.views[0]
     w, h, n = view.width, view.height, len(sc.meshlets)
     scene = api.Scene()
     scene.upload_meshlets(sc.meshlets)
@@ -128,7 +128,7 @@ def test_user_mesh_shader_bit_exact(hooks):
     meshlet = np.where(shown, ids // 128, 0)
     exp[0] = np.where(shown & (meshlet % 2 == 1), ids | 0x40000000, ids)
     _assert_layers_equal(_layers(fb, 4), exp, ["surface id", "depth", "u bits", "v bits"])
-    assert shown.sum() > 5000
+    assert shown.sum() > 5000 and len(np.unique(meshlet[shown])) > 300
     assert np.any(shown & (meshlet % 3 == 0)) and not np.any(shown & (meshlet % 5 == 4))
 
 
