@@ -132,6 +132,8 @@ _SIGS = {
     "swr_neural_decode": [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p],
     "swr_resolve_neural": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p],
     "swr_neural_set_wait_limit": [C.c_void_p, C.c_uint64],
+    "swr_neural_save": [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p],
+    "swr_neural_load": [C.c_void_p, C.c_void_p, C.c_size_t],
     "swr_selftest_bounded_wait": [C.c_uint64],
     "swr_meshlet_bound": [C.c_uint32],
     "swr_build_meshlets": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p],
@@ -572,6 +574,19 @@ class NeuralMaterials:
         i = self.info
         return {"latent_bytes": i.latent_bytes, "weight_bytes": i.weight_bytes, "fallback_bytes": i.fallback_bytes,
                 "plain_bytes": i.plain_bytes}
+
+    def save(self) -> bytes:
+        """The training checkpoint (swr_neural_save)."""
+        size = C.c_size_t()
+        _check(_lib.swr_neural_save(self.h, None, 0, C.byref(size)))
+        buf = (C.c_uint8 * size.value)()
+        _check(_lib.swr_neural_save(self.h, buf, size.value, C.byref(size)))
+        return bytes(buf)
+
+    def load(self, blob: bytes) -> None:
+        """Restores a training checkpoint of a model of the same shape (swr_neural_load)."""
+        buf = (C.c_uint8 * len(blob)).from_buffer_copy(blob)
+        _check(_lib.swr_neural_load(self.h, buf, len(blob)))
 
     def set_wait_limit(self, limit_ns: int) -> None:
         """Time limit of each bounded device-side wait of the model's kernels (default 1 s)."""

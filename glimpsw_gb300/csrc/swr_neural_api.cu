@@ -384,6 +384,87 @@ swr_status swr_neural_gradients(swr_neural n, uint32_t material, const uint32_t*
     return check_status(n, st, "swr_neural_gradients");
 }
 
+// Training checkpoint: a versioned little-endian blob of everything the training trajectory depends
+// on (header, per-material Adam step counts, parameters, latents and their Adam moments).
+namespace {
+constexpr uint32_t kCheckpointMagic = 0x4E525753u;  // "SWRN"
+constexpr uint32_t kCheckpointVersion = 1;
+struct CheckpointHeader {
+    uint32_t magic, version, numMaterials, levels, texelsPerMaterial, paramsPerMaterial;
+    uint64_t seed;
+    uint64_t trainCalls;
+};
+static_assert(sizeof(CheckpointHeader) == 40, "checkpoint header");
+
+size_t checkpoint_size(const swr_neural_t* n) {
+    const size_t M = n->d.numMaterials, P = (size_t)M * kNeuralParams, T = (size_t)M * n->d.texelsPerMaterial * 8;
+    return sizeof(CheckpointHeader) + M * sizeof(uint32_t) + 3 * P * sizeof(float) + 3 * T * sizeof(float);
+}
+}  // namespace
+
+swr_status swr_neural_save(swr_neural n, void* dst, size_t capacity, size_t* size) {
+    if (!n || !size) return swr_internal_fail(SWR_EINVAL, "swr_neural_save: NULL argument");
+    const size_t need = checkpoint_size(n);
+    *size = need;
+    if (!dst) return SWR_OK;
+    if (capacity < need) return swr_internal_fail(SWR_ECAPACITY, "swr_neural_save: the buffer is smaller than the checkpoint");
+    const size_t M = n->d.numMaterials, P = M * kNeuralParams, T = M * (size_t)n->d.texelsPerMaterial * 8;
+    CheckpointHeader h = { kCheckpointMagic, kCheckpointVersion, n->d.numMaterials, n->d.levels, n->d.texelsPerMaterial,
+                           kNeuralParams, n->seed, n->trainCalls };
+    uint8_t* p = (uint8_t*)dst;
+    memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    memcpy(p, n->steps.data(), M * sizeof(uint32_t));
+    p += M * sizeof(uint32_t);
+    cudaStream_t st = swr_internal_stream();
+    cudaError_t e = cudaSuccess;
+    const float* src[6] = { n->params, n->paramM, n->paramV, n->latent, n->latentM, n->latentV };
+    const size_t cnt[6] = { P, P, P, T, T, T };
+    for (int i = 0; i < 6 && e == cudaSuccess; i++) {
+        e = cudaMemcpyAsync(p, src[i], cnt[i] * sizeof(float), cudaMemcpyDeviceToHost, st);
+        p += cnt[i] * sizeof(float);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return e == cudaSuccess ? SWR_OK : swr_internal_cuda_fail(e, "swr_neural_save");
+}
+
+swr_status swr_neural_load(swr_neural n, const void* src, size_t size) {
+    if (!n || !src) return swr_internal_fail(SWR_EINVAL, "swr_neural_load: NULL argument");
+    CheckpointHeader h;
+    if (size < sizeof(h)) return swr_internal_fail(SWR_EINVAL, "swr_neural_load: blob too short");
+    memcpy(&h, src, sizeof(h));
+    if (h.magic != kCheckpointMagic || h.version != kCheckpointVersion)
+        return swr_internal_fail(SWR_EINVAL, "swr_neural_load: not a decoder checkpoint of this version");
+    if (h.numMaterials != n->d.numMaterials || h.levels != n->d.levels || h.texelsPerMaterial != n->d.texelsPerMaterial ||
+        h.paramsPerMaterial != kNeuralParams)
+        return swr_internal_fail(SWR_EINVAL, "swr_neural_load: the checkpoint was saved from a model of another shape");
+    if (size != checkpoint_size(n)) return swr_internal_fail(SWR_EINVAL, "swr_neural_load: blob size does not match");
+    const size_t M = n->d.numMaterials, P = M * kNeuralParams, T = M * (size_t)n->d.texelsPerMaterial * 8;
+    const uint8_t* p = (const uint8_t*)src + sizeof(h);
+    cudaStream_t st = swr_internal_stream();
+    // the blob stays host memory the caller may free on return: copy synchronously
+    cudaError_t e = cudaStreamSynchronize(st);
+    float* dst[6] = { n->params, n->paramM, n->paramV, n->latent, n->latentM, n->latentV };
+    const size_t cnt[6] = { P, P, P, T, T, T };
+    const uint8_t* q = p + M * sizeof(uint32_t);
+    for (int i = 0; i < 6 && e == cudaSuccess; i++) {
+        e = cudaMemcpyAsync(dst[i], q, cnt[i] * sizeof(float), cudaMemcpyHostToDevice, st);
+        q += cnt[i] * sizeof(float);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_neural_load");
+    memcpy(n->steps.data(), p, M * sizeof(uint32_t));
+    n->seed = h.seed;
+    n->trainCalls = (uint32_t)h.trainCalls;
+    {
+        LaunchScope ls("k_neural_image", st);
+        launch_neural_image(n->params, n->image, n->d.numMaterials, st);  // the BF16 operand image of the parameters
+    }
+    n->halfStale = true;
+    e = cudaGetLastError();
+    return e == cudaSuccess ? SWR_OK : swr_internal_cuda_fail(e, "swr_neural_load");
+}
+
 swr_status swr_neural_get_params(swr_neural n, uint32_t material, float* params) {
     if (!n || !params || material >= n->d.numMaterials) return swr_internal_fail(SWR_EINVAL, "swr_neural_get_params: bad argument");
     cudaError_t e = cudaMemcpyAsync(params, n->params + (size_t)material * kNeuralParams, kNeuralParams * sizeof(float),

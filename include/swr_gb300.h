@@ -417,6 +417,13 @@ swr_status swr_neural_get_params(swr_neural n, uint32_t material, float* params)
 swr_status swr_neural_set_params(swr_neural n, uint32_t material, const float* params);
 swr_status swr_neural_get_latents(swr_neural n, uint32_t material, float* latents);
 swr_status swr_neural_set_latents(swr_neural n, uint32_t material, const float* latents);
+/* Training checkpoint: the model's whole training state (per-material Adam step counts, the
+ * sampler's seed and step counter, FP32 parameters and latents with their Adam moments) as one
+ * versioned blob, so training can stop and resume on the same trajectory. swr_neural_save with
+ * dst NULL returns the size only; swr_neural_load takes a blob of a model of the same shape
+ * (materials, latent levels, texture sizes) and rebuilds the inference weights and latents. */
+swr_status swr_neural_save(swr_neural n, void* dst, size_t capacity, size_t* size);
+swr_status swr_neural_load(swr_neural n, const void* src, size_t size);
 /* Decodes count texels (packed as for swr_neural_gradients) of one material into out_device
  * (2 words per texel: layer-0 RGBA8 with AO in alpha, layer-1 RGBA8). */
 swr_status swr_neural_decode(swr_neural n, uint32_t material, const uint32_t* texels_device, uint32_t count,

@@ -295,3 +295,38 @@ def test_resolve_neural_close_to_plain():
           f"max abs {np.abs(pa - pb).max() * 255:.0f}/255")
     assert requests > 1000
     assert p > 38.0
+
+
+def test_checkpoint_save_load_resumes_training():
+    """swr_neural_save / swr_neural_load: the restored model's checkpoint is byte-identical to the
+    saved one, and training resumed from it follows the original model's trajectory. The latent
+    gradient accumulates with float atomics, whose order varies from run to run, so the two
+    continuations agree to a tolerance (rel. L2 1e-3 of parameters and latents) rather than bit for
+    bit; a model trained the same number of steps from scratch lands far away."""
+    api = _setup_stream()
+    texs = [_device_texture([scenes.value_noise_rgba(SIZE, 41 + i, cells=8, layer=l, detail=True) for l in range(2)])
+            for i in range(4)]
+    a = api.NeuralMaterials(texs, latent_levels=LEVELS, seed=3)
+    a.train(300, batch=8192, materials_per_step=4)
+    blob = a.save()
+    b = api.NeuralMaterials(texs, latent_levels=LEVELS, seed=99)
+    b.load(blob)
+    assert b.save() == blob
+    fresh = api.NeuralMaterials(texs, latent_levels=LEVELS, seed=3)
+    la = a.train(200, batch=8192, materials_per_step=4, want_loss=True)
+    lb = b.train(200, batch=8192, materials_per_step=4, want_loss=True)
+    lf = fresh.train(200, batch=8192, materials_per_step=4, want_loss=True)
+    for mat in range(4):
+        pa, pb, pf = a.get_params(mat), b.get_params(mat), fresh.get_params(mat)
+        xa, xb = a.get_latents(mat), b.get_latents(mat)
+        rel_p = np.linalg.norm(pa - pb) / np.linalg.norm(pa)
+        rel_x = np.linalg.norm(xa - xb) / np.linalg.norm(xa)
+        print(f"material {mat}: resumed vs continued rel L2 params {rel_p:.2e}, latents {rel_x:.2e}; "
+              f"fresh {np.linalg.norm(pa - pf) / np.linalg.norm(pa):.2e}")
+        assert rel_p < 1e-3 and rel_x < 1e-3
+        assert np.linalg.norm(pa - pf) / np.linalg.norm(pa) > 1e-2
+    assert abs(la - lb) <= 0.05 * la and lf > la
+    # a checkpoint of a model of another shape is refused
+    other = api.NeuralMaterials(texs[:2], latent_levels=LEVELS, seed=3)
+    with pytest.raises(Exception):
+        other.load(blob)
