@@ -19,7 +19,7 @@ LIB_PATH = os.path.join(HERE, "libswr_gb300.so")
 
 SWR_OK, SWR_EINVAL, SWR_ECAPACITY, SWR_ETIMEOUT, SWR_ECUDA, SWR_ENOMEM = range(6)
 STATUS_NAMES = {0: "SWR_OK", 1: "SWR_EINVAL", 2: "SWR_ECAPACITY", 3: "SWR_ETIMEOUT", 4: "SWR_ECUDA", 5: "SWR_ENOMEM"}
-FORMAT_RGBA8U, FORMAT_R11G11B10F, FORMAT_R32F = 0, 1, 2
+FORMAT_RGBA8U, FORMAT_R11G11B10F, FORMAT_R32F, FORMAT_RG16F = 0, 1, 2, 3
 VisBufferShader = 0
 DeferredShader = SHADER_DEFERRED = 1
 OverdrawShader = 2
@@ -111,6 +111,9 @@ _SIGS = {
     "swr_cull_meshlets_ex": [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                              C.c_void_p, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_uint32],
     "swr_downsample_depth": [C.c_void_p, C.c_void_p],
+    "swr_ibl_irradiance_map": [C.c_void_p, C.c_void_p],
+    "swr_ibl_radiance_map": [C.c_void_p, C.c_void_p],
+    "swr_ibl_env_brdf_lut": [C.c_void_p],
     "swr_resolve": [C.c_void_p, C.c_void_p, C.c_void_p],
     "swr_resolve_debug": [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32],
     "swr_batch_create": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p],

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libswr_gb300.so")
 SOURCES = ["swr_api.cu", "swr_raster.cu", "swr_texture.cu", "swr_shade.cu", "swr_batch.cu", "swr_noalloc.cu",
-           "swr_neural.cu", "swr_neural_api.cu", "swr_gbuffer.cu", "swr_meshletize.cpp"]
+           "swr_neural.cu", "swr_neural_api.cu", "swr_gbuffer.cu", "swr_ibl.cu", "swr_meshletize.cpp"]
 HEADERS = ["swr_device.cuh", "swr_internal.h", "swr_tc.cuh", "swr_neural.h", "swr_sample.cuh", "swr_surface.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -1,4 +1,5 @@
 // Textures (Texture.h:314-636): TiledY8 storage, SetPixels and GenerateMips on the device.
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -74,6 +75,12 @@ __global__ void k_generate_mip(const uint32_t* __restrict__ src, uint32_t* __res
             float g = fmul(fadd(fadd(fadd(unpack_f11(p00 >> 10), unpack_f11(p10 >> 10)), unpack_f11(p01 >> 10)), unpack_f11(p11 >> 10)), 0.25f);
             float b = fmul(fadd(fadd(fadd(unpack_f10(p00), unpack_f10(p10)), unpack_f10(p01)), unpack_f10(p11)), 0.25f);
             out = pack_f11(r) << 21 | pack_f11(g) << 10 | pack_f10(b);
+        } else if (format == SWR_FORMAT_RG16F) {
+            auto lo = [](uint32_t p) { return __half2float(__ushort_as_half((unsigned short)(p & 0xFFFF))); };
+            auto hi = [](uint32_t p) { return __half2float(__ushort_as_half((unsigned short)(p >> 16))); };
+            const float r = fmul(fadd(fadd(fadd(lo(p00), lo(p10)), lo(p01)), lo(p11)), 0.25f);
+            const float g = fmul(fadd(fadd(fadd(hi(p00), hi(p10)), hi(p01)), hi(p11)), 0.25f);
+            out = (uint32_t)__half_as_ushort(__float2half_rn(r)) | ((uint32_t)__half_as_ushort(__float2half_rn(g)) << 16);
         } else {
             out = __float_as_uint(fmul(fadd(fadd(fadd(__uint_as_float(p00), __uint_as_float(p10)), __uint_as_float(p01)),
                                             __uint_as_float(p11)), 0.25f));
@@ -94,7 +101,7 @@ extern "C" {
 swr_status swr_texture_create(uint32_t format, uint32_t width, uint32_t height, uint32_t max_levels,
                               uint32_t num_layers, swr_texture* out) {
     if (!out) return swr_internal_fail(SWR_EINVAL, "swr_texture_create: out is NULL");
-    if (format > SWR_FORMAT_R32F) return swr_internal_fail(SWR_EINVAL, "swr_texture_create: unknown format");
+    if (format > SWR_FORMAT_RG16F) return swr_internal_fail(SWR_EINVAL, "swr_texture_create: unknown format");
     if (width < 8 || height < 4 || (width & (width - 1)) || (height & (height - 1)) || width > 16384 || height > 16384)
         return swr_internal_fail(SWR_EINVAL, "swr_texture_create: sizes must be powers of two, width >= 8, height >= 4");
     if (max_levels == 0 || max_levels > 16 || num_layers == 0 || num_layers > 64)

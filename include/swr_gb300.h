@@ -77,6 +77,7 @@ typedef struct swr_texture_t* swr_texture;
 #define SWR_FORMAT_RGBA8U 0u
 #define SWR_FORMAT_R11G11B10F 1u
 #define SWR_FORMAT_R32F 2u
+#define SWR_FORMAT_RG16F 3u  /* pixfmt::RG16f (Texture.h:105-133): two IEEE halves, R in the low 16 bits */
 
 /* Perf counters (PerfCounter, Rasterizer.h:366-370). */
 #define SWR_COUNTER_TRIANGLES_PROCESSED 0
@@ -364,6 +365,19 @@ swr_status swr_resolve(swr_rasterizer r, swr_framebuffer fb, const swr_shading_c
  * (from the vis-buffer), hashed meshlet or triangle ids, or the OverdrawShader's counters through
  * the Turbo colormap; sky pixels (depth <= 0) get a grey/white checkerboard of 4x4 tiles. */
 swr_status swr_resolve_debug(swr_rasterizer r, swr_framebuffer fb, const swr_shading_context* ctx, uint32_t layer);
+
+/* ---- Image-based lighting precompute (Shading.cpp:35-219; the reference's frame driver never
+ * calls it) ----
+ * GenerateIrradianceMap: the cosine-weighted diffuse irradiance of an R11G11B10 octahedral
+ * environment map (with at least 3 mips; the integral reads level 2) over 360 x 90 angle steps, into
+ * level 0 of out (R11G11B10; the reference's is 64x64). */
+swr_status swr_ibl_irradiance_map(swr_texture env, swr_texture out);
+/* GenerateRadianceMap: every mip level L of out (R11G11B10 with mips; the reference's is 256x256,
+ * 8 levels) prefiltered with 128 GGX importance samples at roughness L / (levels - 1) (Karis 2014). */
+swr_status swr_ibl_radiance_map(swr_texture env, swr_texture out);
+/* GenerateEnvBRDFLut: the split-sum scale and bias of the environment BRDF at NoV = u, roughness = v
+ * (1024 importance samples) into level 0 of out (RG16f; the reference's is 128x128). */
+swr_status swr_ibl_env_brdf_lut(swr_texture out);
 
 /* ---- Learned texture decoder (no counterpart in the reference) ----
  * One model holds, per material, an FP16 latent pyramid of 8 channels (latent level k has the size

@@ -10,7 +10,7 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-SOURCES = ["swr_oracle_raster.cpp", "swr_oracle_texture.cpp", "swr_oracle_resolve.cpp"]
+SOURCES = ["swr_oracle_raster.cpp", "swr_oracle_texture.cpp", "swr_oracle_resolve.cpp", "swr_oracle_ibl.cpp"]
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liborc.so")
 

@@ -74,6 +74,8 @@ def lib():
         L.orc_approx14_mismatches.restype = C.c_int64
         L.orc_approx14_mismatches.argtypes = [C.c_int, C.c_uint64, C.c_uint64]
         L.orc_fb_clear.argtypes = [C.c_void_p, C.c_uint32, C.c_float]
+        for name in ("orc_ibl_irradiance_texel", "orc_ibl_radiance_texel", "orc_ibl_env_brdf_texel"):
+            getattr(L, name).restype = C.c_uint32
         L.orc_cull_meshlets.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_void_p]
     return _lib
@@ -187,6 +189,21 @@ def draw_meshlets_binned(fb: Framebuffer, ctx: Context, count: int, threads: int
     lib().orc_draw_meshlets_binned(C.byref(fb.s), C.c_uint32(count), C.byref(ctx.s), C.c_uint32(threads),
                                    _fptr(counters))
     return counters
+
+
+def ibl_irradiance_texel(env: Texture, x: int, y: int, w: int, h: int) -> int:
+    """PrefilterDiffuseIrradiance (Shading.cpp:72-102) of texel (x, y) of a w x h map, packed R11G11B10."""
+    return int(lib().orc_ibl_irradiance_texel(C.byref(env.s), x, y, w, h))
+
+
+def ibl_radiance_texel(env: Texture, level: int, levels: int, x: int, y: int, w0: int, h0: int) -> int:
+    """PrefilterEnvMap (Shading.cpp:105-147) of texel (x, y) of mip `level` of a radiance map."""
+    return int(lib().orc_ibl_radiance_texel(C.byref(env.s), level, levels, x, y, w0, h0))
+
+
+def ibl_env_brdf_texel(x: int, y: int, w: int, h: int) -> int:
+    """IntegrateBRDF (Shading.cpp:149-175) of texel (x, y) of a w x h table, packed RG16f."""
+    return int(lib().orc_ibl_env_brdf_texel(x, y, w, h))
 
 
 def cull_meshlets(meshlets: np.ndarray, count: int, proj, view, model, prev_view, frame_w, frame_h,

@@ -149,6 +149,15 @@ void orc_resolve_debug_rows(orc_framebuffer* fb, const orc_shading_context* ctx,
                             uint32_t row_begin, uint32_t row_end);
 void orc_resolve_debug_mt(orc_framebuffer* fb, const orc_shading_context* ctx, uint32_t layer, uint32_t num_threads);
 
+// Image-based lighting precompute (Shading.cpp:35-219), one output texel each:
+// PrefilterDiffuseIrradiance of texel (x, y) of a w x h map (packed R11G11B10), PrefilterEnvMap of
+// texel (x, y) of mip `level` of a `levels`-mip map with level 0 of w0 x h0 (R11G11B10), and
+// IntegrateBRDF of texel (x, y) of a w x h table (packed RG16f). env: an R11G11B10 octahedral map.
+uint32_t orc_ibl_irradiance_texel(const orc_texture* env, uint32_t x, uint32_t y, uint32_t w, uint32_t h);
+uint32_t orc_ibl_radiance_texel(const orc_texture* env, uint32_t level, uint32_t levels, uint32_t x, uint32_t y,
+                                uint32_t w0, uint32_t h0);
+uint32_t orc_ibl_env_brdf_texel(uint32_t x, uint32_t y, uint32_t w, uint32_t h);
+
 #ifdef __cplusplus
 }
 #endif
