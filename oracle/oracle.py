@@ -74,8 +74,10 @@ def lib():
         L.orc_approx14_mismatches.restype = C.c_int64
         L.orc_approx14_mismatches.argtypes = [C.c_int, C.c_uint64, C.c_uint64]
         L.orc_fb_clear.argtypes = [C.c_void_p, C.c_uint32, C.c_float]
-        for name in ("orc_ibl_irradiance_texel", "orc_ibl_radiance_texel", "orc_ibl_env_brdf_texel"):
+        for name in ("orc_ibl_irradiance_texel", "orc_ibl_radiance_texel", "orc_ibl_env_brdf_texel", "orc_debug_lerp16"):
             getattr(L, name).restype = C.c_uint32
+        L.orc_debug_calc_mip_level.restype = C.c_int32
+        L.orc_debug_calc_mip_level.argtypes = [C.c_float] * 6
         L.orc_cull_meshlets.argtypes = [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
                                         C.c_void_p, C.c_void_p, C.c_float, C.c_float, C.c_void_p]
     return _lib

@@ -74,6 +74,13 @@ inline uint32_t texel_offset(int32_t x, int32_t y, int32_t stride) {
     return (uint32_t)((y & 7) | (x << 3) | ((y & ~7) << stride));
 }
 
+// texutil::CalcMipLevel(grad, scale) (Texture.h:276-280) with the squared scales.
+inline int32_t calc_mip_level(float gx, float gy, float gz, float gw, float ssu, float ssv) {
+    const float dx = std::fma(gx, gx, gy * gy) * ssu;
+    const float dy = std::fma(gz, gz, gw * gw) * ssv;
+    return ilog2_x86(vmax(dx, dy)) >> 1;
+}
+
 // texutil::MapOctahedron / UnmapOctahedron (Texture.h:282-296)
 inline void map_oct(F3 n, float& u, float& v) {
     float w = approx_rcp(std::fabs(n.x) + std::fabs(n.y) + std::fabs(n.z));
@@ -341,11 +348,7 @@ void resolve_surface(const orc_shading_context* sc, const uint32_t* ids, uint16_
         const orc_texture& tex = sc->textures[mat.texture];
         int32_t mip[L];
         float ssu = tex.scale_u * tex.scale_u, ssv = tex.scale_v * tex.scale_v;
-        for (int l = 0; l < L; l++) {  // texutil::CalcMipLevel(grad, scale), Texture.h:276-280
-            float dx = std::fma(grad[0][l], grad[0][l], grad[1][l] * grad[1][l]) * ssu;
-            float dy = std::fma(grad[2][l], grad[2][l], grad[3][l] * grad[3][l]) * ssv;
-            mip[l] = ilog2_x86(vmax(dx, dy)) >> 1;
-        }
+        for (int l = 0; l < L; l++) mip[l] = calc_mip_level(grad[0][l], grad[1][l], grad[2][l], grad[3][l], ssu, ssv);
         uint32_t s[L];
         sample_rgba8(tex, texU, texV, 0, mip, s);
         for (int l = 0; l < L; l++) if ((iter >> l) & 1) albedo[l] = s[l];
@@ -620,4 +623,29 @@ extern "C" void orc_resolve_debug_mt(orc_framebuffer* fb, const orc_shading_cont
         threads.emplace_back([=]() { orc_resolve_debug_rows(fb, sc, layer, r0, r1); });
     }
     for (auto& th : threads) th.join();
+}
+
+// The pieces of the resolve and its sampler on their own, for the known-answer tests of tests/.
+extern "C" {
+uint32_t orc_debug_lerp16(uint32_t a, uint32_t b, uint32_t t) { return lerp16(a, b, t); }
+void orc_debug_unpack_srgb(uint32_t p, float* out) {
+    const F4 v = unpack_srgb(p);
+    out[0] = v.x, out[1] = v.y, out[2] = v.z, out[3] = v.w;
+}
+void orc_debug_unpack_r11g11b10(uint32_t p, float* out) {
+    const F3 v = unpack_r11g11b10(p);
+    out[0] = v.x, out[1] = v.y, out[2] = v.z;
+}
+int32_t orc_debug_calc_mip_level(float gx, float gy, float gz, float gw, float scaleU, float scaleV) {
+    return calc_mip_level(gx, gy, gz, gw, scaleU * scaleU, scaleV * scaleV);
+}
+void orc_debug_map_oct(const float* n, float* uv) { map_oct({ n[0], n[1], n[2] }, uv[0], uv[1]); }
+void orc_debug_unmap_oct(const float* uv, float* n) {
+    const F3 r = unmap_oct(uv[0], uv[1]);
+    n[0] = r.x, n[1] = r.y, n[2] = r.z;
+}
+void orc_debug_sample_rgba8(const orc_texture* t, const float* u, const float* v, int layer, const int32_t* mip,
+                            uint32_t* out) {
+    sample_rgba8(*t, u, v, layer, mip, out);
+}
 }
