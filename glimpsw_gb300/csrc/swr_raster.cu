@@ -349,6 +349,17 @@ __device__ __forceinline__ bool tile_empty(const TriRec& r, uint32_t px, uint32_
            tile_max_edge(e2, r.A01, r.B01) < 0;
 }
 
+// Upper bound of any fragment depth of a triangle from its vertex depths: a fragment's depth is its
+// edge functions' interpolation of Z0, Z1, Z2 inside the triangle, so at most their maximum, plus the
+// roundings of the plane terms and of the evaluation, within 16 ulp of the largest |Z| (2^-20);
+// 2^-16 of it is kept. For a small triangle this is much tighter than the plane's value at the tile
+// corners, which lie outside it. NaN vertex depths give a NaN, which never beats a fragment's.
+__device__ __forceinline__ float triangle_depth_bound(const Setup& t) {
+    const float m = fmaxf(fmaxf(fabsf(t.Z0), fabsf(t.Z1)), fabsf(t.Z2));
+    const bool nan = t.Z0 != t.Z0 || t.Z1 != t.Z1 || t.Z2 != t.Z2;
+    return nan ? __int_as_float(0x7F800000) : fadd(fmaxf(fmaxf(t.Z0, t.Z1), t.Z2), fmul(m, 0x1p-16f));
+}
+
 // True if the tile at (px, py) (4-aligned) can be shaded for r: some sample may pass the edges
 // and, when a depth bound is kept, r may beat the tile's depth bound somewhere. *known receives
 // the bound read (for the later update).
@@ -358,6 +369,14 @@ __device__ __forceinline__ bool tile_live(const TriRec& r, uint32_t px, uint32_t
     if (!tileMin) return true;
     *known = tileMin[(py >> 2) * tilesPerRow + (px >> 2)];
     return float_order(tile_depth_bound(r, px, py)) >= *known;
+}
+// tile_live with the triangle's own depth bound zmax (triangle_depth_bound) as a second bound.
+__device__ __forceinline__ bool tile_live(const TriRec& r, uint32_t px, uint32_t py, const uint32_t* tileMin,
+                                          uint32_t tilesPerRow, uint32_t* known, float zmax) {
+    if (tile_empty(r, px, py)) return false;
+    if (!tileMin) return true;
+    *known = tileMin[(py >> 2) * tilesPerRow + (px >> 2)];
+    return float_order(fminf(tile_depth_bound(r, px, py), zmax)) >= *known;
 }
 
 // Shades the live tiles of the warp-wide candidate set (the lanes in `mask` hold a tile origin
@@ -656,6 +675,7 @@ struct WarpSmem {
     uint8_t owner[32 * kSmallTiles];
     uint8_t code[64];    // vertex_code
     uint8_t live[128];   // the meshlet's triangles that survive the face test or need clipping
+    float zmax[32];      // each small triangle's depth bound (triangle_depth_bound)
 };
 struct WarpSmemAlpha : WarpSmem {
     AlphaExt exts[32];
@@ -887,6 +907,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                         tris[lane] = r;
                         if constexpr (kAlpha) S.exts[lane] = x;
                         myTiles = tilesX * tilesY;
+                        S.zmax[lane] = triangle_depth_bound(t);
                     } else {
                         bool queued;
                         if constexpr (kAlpha) {
@@ -969,7 +990,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                     const int tilesX = r.pad & 0xFF, magic = r.pad >> 8;
                     const int ty = (tile * magic) >> 8, tx = tile - ty * tilesX;
                     tpx = (r.bbMin & 0xFFFF) + tx * 4, tpy = (r.bbMin >> 16) + ty * 4;
-                    live = tile_live(r, tpx, tpy, vp.tileMin, tw, &tmin);
+                    live = tile_live(r, tpx, tpy, vp.tileMin, tw, &tmin, S.zmax[own]);
                 }
                 const unsigned liveMask = __ballot_sync(0xFFFFFFFFu, live);
                 if constexpr (kAlpha) {
