@@ -91,6 +91,14 @@ __device__ __forceinline__ float gelu(float x) {
     const float h = 0.5f * x;
     return fmaf(h, t, h);
 }
+// 2 gelu(x) = x + x tanh(sqrt(2/pi) x (1 + 0.044715 x^2)): four instructions and the tanh. The
+// inference kernel keeps its activations doubled and its next layer's weights halved (exact for
+// BF16 weights of normal magnitude), so the products, hence z2 and y, are those of gelu.
+constexpr float kGeluAB = kGeluA * kGeluB;
+__device__ __forceinline__ float gelu_x2(float x) {
+    const float t = tanh_hw(x * fmaf(kGeluAB, x * x, kGeluA));
+    return fmaf(x, t, x);
+}
 __device__ __forceinline__ float gelu_grad(float x) {
     const float x2 = x * x;
     const float t = tanh_hw(kGeluA * x * fmaf(kGeluB, x2, 1.0f));
@@ -626,6 +634,10 @@ __global__ void __launch_bounds__(128) k_neural_decode(const __grid_constant__ N
             ok = mbar_wait_drained(barLoad, loadPhase, a.n.waitNs) && ok;
             loadPhase ^= 1;
             loaded = mat;
+            // W2 and W3 halved in place: the activations they weigh are 2 gelu (gelu_x2)
+            __nv_bfloat162* w = (__nv_bfloat162*)(sm + kIW2);
+            const __nv_bfloat162 half2 = __floats2bfloat162_rn(0.5f, 0.5f);
+            for (uint32_t i = t; i < (kIB2 - kIW2) / 4; i += blockDim.x) w[i] = __hmul2(w[i], half2);
         }
         const uint32_t first = a.reqOffset[mat] + (tile - a.tileOffset[mat]) * 128;
         const bool valid = first + t < a.reqOffset[mat + 1];
@@ -652,7 +664,7 @@ __global__ void __launch_bounds__(128) k_neural_decode(const __grid_constant__ N
             float v[16];
             tmem_ld16(tRow + 16 * c, v);
 #pragma unroll
-            for (int j = 0; j < 16; j++) v[j] = gelu(v[j]);
+            for (int j = 0; j < 16; j++) v[j] = gelu_x2(v[j]);
             store_row8(sm + kDH1, 128, 2 * c, t, v);
             store_row8(sm + kDH1, 128, 2 * c + 1, t, v + 8);
         }
@@ -666,7 +678,7 @@ __global__ void __launch_bounds__(128) k_neural_decode(const __grid_constant__ N
             float v[16];
             tmem_ld16(tRow + 16 * c, v);
 #pragma unroll
-            for (int j = 0; j < 16; j++) v[j] = gelu(v[j] + b2[16 * c + j]);
+            for (int j = 0; j < 16; j++) v[j] = gelu_x2(v[j] + b2[16 * c + j]);
             store_row8(sm + kDH2, 128, 2 * c, t, v);
             store_row8(sm + kDH2, 128, 2 * c + 1, t, v + 8);
         }
