@@ -748,6 +748,7 @@ __global__ void __launch_bounds__(kScatterThreads) k_neural_scatter(const unsign
     for (uint32_t k = 0; k < kScatterPerThread; k++) {  // slot first + k * 256: coalesced loads
         const uint32_t i = first + k * kScatterThreads;
         r[k] = i < slots ? pixelReq[i] : ~0ull;
+        if (r[k] >> 63) r[k] = ~0ull;  // none, or a redirect to another slot's request
         if (r[k] != ~0ull) {
             rank[k] = atomicAdd(&sCount[(uint32_t)(r[k] >> 32)], 1u);
             atomicAdd(&sLevel[((uint32_t)r[k] >> 28) & 15u], 1u);

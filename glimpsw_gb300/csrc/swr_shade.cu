@@ -226,8 +226,12 @@ struct ResolveArgs {
 
 // Neural resolve: the emit pass records, per pixel, the texels of the levels the model decodes
 // (4 slots: the nearest texel, or the bilinear quad's 00 10 01 11 texels; ~0 = none) and counts
-// them per material; the shade pass reads the decoded texels from the same slots.
+// them per material; the shade pass reads the decoded texels from the same slots. Within a 4x4
+// tile, a slot whose texel a lower lane's slot of the same quad position already requests holds
+// kReqRedirect | that slot instead and is not decoded: a magnified texture gives most of a tile's
+// pixels the same quad.
 enum { kResolvePlain = 0, kResolveEmit = 1, kResolveNeural = 2, kResolveDebug = 3 };
+constexpr unsigned long long kReqRedirect = 1ull << 63;  // | slot; ~0 (none) has the bit too
 struct NeuralResolve {
     const DevTexture* tex;             // model textures (data == nullptr: not decoded)
     uint32_t numMaterials, decodedLevels;  // texture levels below decodedLevels are decoded
@@ -444,15 +448,31 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a, NeuralResolve nr
                             }
                         }
                         const unsigned grp = iter << (16 * half);
+                        nq = 0;
+#pragma unroll
+                        for (int k = 0; k < 4; k++) {  // requests equal to a lower lane's at the same position
+                            const unsigned peers = __match_any_sync(grp, req[k]);
+                            const int lead = __ffs(peers) - 1;
+                            const uint32_t leadOff = __shfl_sync(grp, off, lead);
+                            if (req[k] == ~0ull) continue;
+                            if (lead != (int)lane) req[k] = kReqRedirect | ((unsigned long long)leadOff * 4 + k);
+                            else nq++;
+                        }
                         const uint32_t total = __reduce_add_sync(grp, nq);
                         if (total && (int)lane == __ffs(grp) - 1) atomicAdd(&nr.counts[mid], total);
                     } else if (dec) {
-                        const uint2* d = nr.decoded + (size_t)off * 4;
-                        const uint2 d00 = d[0];
+                        // a slot's decoded texel, or the one of the slot it redirects to
+                        const ulonglong2* rq = (const ulonglong2*)(nr.pixelReq + (size_t)off * 4);
+                        const ulonglong2 r01 = rq[0], r23 = rq[1];
+                        auto at = [&](unsigned long long r, uint32_t k) {
+                            const size_t slot = (r != ~0ull && (r & kReqRedirect)) ? (size_t)(uint32_t)r : (size_t)off * 4 + k;
+                            return nr.decoded[slot];
+                        };
+                        const uint2 d00 = at(r01.x, 0);
                         uint2 r0 = d00;
                         if (!nearest) {
-                            const uint2 d10 = q.inX ? d[1] : d00, d01 = q.inY ? d[2] : d00;
-                            const uint2 d11 = q.inY ? (q.inX ? d[3] : d01) : d10;
+                            const uint2 d10 = q.inX ? at(r01.y, 1) : d00, d01 = q.inY ? at(r23.x, 2) : d00;
+                            const uint2 d11 = q.inY ? (q.inX ? at(r23.y, 3) : d01) : d10;
                             r0.x = filter_rgba8(d00.x, d10.x, d01.x, d11.x, q.fx, q.fy);
                             r0.y = filter_rgba8(d00.y, d10.y, d01.y, d11.y, q.fx, q.fy);
                         }
