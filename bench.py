@@ -340,7 +340,7 @@ NCU_WORKLOAD = (100_000, 1920, 1080)
 # ----------------------------------------------------------------------------- multi-view
 def multiview_section(args, api, stream):
     """64 views (6 depth-only cube faces at 1024^2 + 58 cameras of log-uniform resolution) of a
-    200k-meshlet grid: one batched graph launch (autotuned chunk size / warps per block) against
+    200k-meshlet grid: one batched graph launch (autotuned chunk size and shape / warps per block) against
     64 per-view sequences of clear + frustum cull + draw through the regular entry points."""
     import torch
 
@@ -399,8 +399,8 @@ def multiview_section(args, api, stream):
             "visible_meshlets_per_view": {"min": int(min(visible)), "max": int(max(visible)),
                                           "total": int(sum(visible))},
             "batched_ms": batched_ms, "per_view_ms": per_view_ms, "speedup": per_view_ms / batched_ms,
-            "autotuned": {"chunk_px": best[0] * 4, "warps_per_block": best[1],
-                          "candidates_ms": {f"{cc * 4}px/{w}w": round(t, 4) for (cc, w), t in timings.items()}},
+            "autotuned": {"chunk_px": [best[0] * 4, best[2] * 4], "warps_per_block": best[1],
+                          "candidates_ms": {f"{cw * 4}x{ch * 4}px/{w}w": round(t, 4) for (cw, w, ch), t in timings.items()}},
             "triangles_processed": int(c[0]), "gtri_per_s": float(c[0]) / (batched_ms / 1e3) / 1e9}
 
 
@@ -408,7 +408,7 @@ def multiview_section(args, api, stream):
 def combined_section(args, api, stream):
     """Combined stress workload: 1M meshlets (10 translated copies of the volume construction,
     124M triangles, 1.73 GB of meshlet records), 256 materials of two 2048^2 RGBA8 layers, 16 views
-    of 1280x720..2880x1620. One batched graph launch (autotuned chunk size and warps per block)
+    of 1280x720..2880x1620. One batched graph launch (autotuned chunk size and shape, warps per block)
     draws every view; each view is then resolved with the learned decoder (trained on the 256
     materials). Reports the batched raster time, the neural resolve time of all views, Gtri/s,
     HBM GB/s of the raster (algorithmic bytes: 1168 B per drawn meshlet + 16 B per pixel) and
@@ -488,7 +488,7 @@ def combined_section(args, api, stream):
     peak, peak_kind = peaks()
     return {"meshlets": n, "triangles": n * 124, "meshlet_bytes": int(sc.meshlets.nbytes), "materials": len(sc.materials),
             "views": len(sc.views), "sizes": [[v.width, v.height] for v in sc.views], "pixels": pixels,
-            "scene_build_s": scene_s, "autotuned": {"chunk_px": best[0] * 4, "warps_per_block": best[1]},
+            "scene_build_s": scene_s, "autotuned": {"chunk_px": [best[0] * 4, best[2] * 4], "warps_per_block": best[1]},
             "batched_raster_ms": raster_ms, "frame_ms_raster_plus_neural_resolve": frame_ms,
             "triangles_processed": int(c[0]), "gtri_per_s": float(c[0]) / (raster_ms / 1e3) / 1e9,
             "raster_hbm_gbs": raster_bytes / (raster_ms / 1e3) / 1e9, "hbm_peak_gbs": peak, "peak_kind": peak_kind,

@@ -119,6 +119,7 @@ _SIGS = {
     "swr_batch_create": [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint32, C.c_int, C.c_void_p],
     "swr_batch_set_views": [C.c_void_p, C.c_void_p, C.c_uint32],
     "swr_batch_set_tuning": [C.c_void_p, C.c_uint32, C.c_uint32],
+    "swr_batch_set_chunk_shape": [C.c_void_p, C.c_uint32, C.c_uint32],
     "swr_batch_render": [C.c_void_p],
     "swr_batch_get_counters": [C.c_void_p, C.c_void_p],
     "swr_batch_reset_counters": [C.c_void_p],
@@ -454,6 +455,10 @@ class Batch:
 
     def set_tuning(self, chunk_tiles: int = 0, warps_per_block: int = 0) -> None:
         _check(_lib.swr_batch_set_tuning(self.h, chunk_tiles, warps_per_block))
+
+    def set_chunk_shape(self, width_tiles: int, height_tiles: int) -> None:
+        """Rectangular chunks of width_tiles x height_tiles 4x4 tiles (after set_tuning)."""
+        _check(_lib.swr_batch_set_chunk_shape(self.h, width_tiles, height_tiles))
 
     def render(self) -> None:
         _check(_lib.swr_batch_render(self.h))

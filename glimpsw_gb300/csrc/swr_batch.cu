@@ -90,7 +90,7 @@ struct swr_batch_t {
     uint32_t* dViewStart = nullptr;
     uint16_t* dBitmaps = nullptr;
     DrawScratch scratch = {};
-    uint32_t chunkTiles = 0, warpsPerBlock = 0;
+    uint32_t chunkTiles = 0, chunkTilesY = 0, warpsPerBlock = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     unsigned long long kernelNodes = 0;
@@ -186,6 +186,7 @@ swr_status capture(swr_batch b) {
         a.viewStart = b->dViewStart;
         a.numViews = nv;
         a.chunkTiles = b->chunkTiles;
+        a.chunkTilesY = b->chunkTilesY;
         a.warpsPerBlock = b->warpsPerBlock;
         launch_draw(a, cs, sm_count());
         e = cudaStreamEndCapture(cs, &b->graph);
@@ -277,8 +278,18 @@ swr_status swr_batch_set_tuning(swr_batch b, uint32_t chunk_tiles, uint32_t warp
         return swr_internal_fail(SWR_EINVAL, "swr_batch_set_tuning: chunk_tiles must be 2, 4, 8 or 16 (8-64 px bins)");
     if (warps_per_block && warps_per_block != 4 && warps_per_block != 8 && warps_per_block != 16)
         return swr_internal_fail(SWR_EINVAL, "swr_batch_set_tuning: warps_per_block must be 4, 8 or 16");
-    if (chunk_tiles != b->chunkTiles || warps_per_block != b->warpsPerBlock) drop_graph(b);
-    b->chunkTiles = chunk_tiles, b->warpsPerBlock = warps_per_block;
+    if (chunk_tiles != b->chunkTiles || b->chunkTilesY != 0 || warps_per_block != b->warpsPerBlock) drop_graph(b);
+    b->chunkTiles = chunk_tiles, b->chunkTilesY = 0, b->warpsPerBlock = warps_per_block;
+    return SWR_OK;
+}
+
+swr_status swr_batch_set_chunk_shape(swr_batch b, uint32_t chunk_w_tiles, uint32_t chunk_h_tiles) {
+    if (!b) return swr_internal_fail(SWR_EINVAL, "swr_batch_set_chunk_shape: NULL batch");
+    auto valid = [](uint32_t c) { return c == 2 || c == 4 || c == 8 || c == 16; };
+    if (!valid(chunk_w_tiles) || !valid(chunk_h_tiles))
+        return swr_internal_fail(SWR_EINVAL, "swr_batch_set_chunk_shape: chunk sides must be 2, 4, 8 or 16 tiles (8-64 px)");
+    if (chunk_w_tiles != b->chunkTiles || chunk_h_tiles != b->chunkTilesY) drop_graph(b);
+    b->chunkTiles = chunk_w_tiles, b->chunkTilesY = chunk_h_tiles;
     return SWR_OK;
 }
 

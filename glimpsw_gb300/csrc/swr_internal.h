@@ -152,8 +152,9 @@ struct DrawArgs {
     const ViewParams* views;
     const uint32_t* viewStart;
     uint32_t numViews;
-    // tuning: chunk edge in 4x4 tiles (0 = 8) and warps per block (0 = 8)
+    // tuning: chunk width in 4x4 tiles (0 = 8), chunk height (0 = the width) and warps per block (0 = 8)
     uint32_t chunkTiles;
+    uint32_t chunkTilesY;
     uint32_t warpsPerBlock;
     // OverdrawShader draws (single view): per-pixel counters (covered << 32 | other samples of
     // covered tiles), keys hold the maximum depth; nullptr for vis-buffer draws

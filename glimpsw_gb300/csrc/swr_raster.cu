@@ -43,6 +43,12 @@ constexpr int kPacketTiles = 128;  // in-warp tile budget of a 32-triangle step
 constexpr int kSpreadTiles = 4;    // over budget, triangles above this many tiles are queued
 constexpr int kChunkTiles = 8;  // chunk = 8x8 tiles = 32x32 pixels
 
+// A draw's chunk shape as passed to the queue and chunk stage: width | height << 8, in tiles.
+__host__ __device__ __forceinline__ uint32_t chunk_shape(const DrawArgs& a) {
+    const uint32_t w = a.chunkTiles ? a.chunkTiles : (uint32_t)kChunkTiles;
+    return w | ((a.chunkTilesY ? a.chunkTilesY : w) << 8);
+}
+
 // ShadeMeshlet's vertex transform (Shading.cpp:295-298): the clip position of a vertex slot; slots
 // past the 16-vertex chunks up to NumVertices are zero.
 __device__ __forceinline__ float4 clip_position(float x, float y, float z, bool live, const ViewParams& vp) {
@@ -168,8 +174,8 @@ __device__ __noinline__ void raster_serial(const TriRec& r, unsigned long long* 
 __device__ __forceinline__ bool enqueue_big(const TriRec& r, const DrawArgs& a, uint32_t chunk) {
     int tilesX = ((r.bbMax & 0xFFFF) - (r.bbMin & 0xFFFF)) >> 2;
     int tilesY = ((r.bbMax >> 16) - (r.bbMin >> 16)) >> 2;
-    unsigned long long chunks = (unsigned long long)((tilesX + chunk - 1) / chunk) *
-                                (unsigned long long)((tilesY + chunk - 1) / chunk);
+    const uint32_t cw = chunk & 0xFF, ch = chunk >> 8;
+    unsigned long long chunks = (unsigned long long)((tilesX + cw - 1) / cw) * (unsigned long long)((tilesY + ch - 1) / ch);
     unsigned long long old = atomicAdd(&a.s.control[1], (1ull << 40) | chunks);
     unsigned long long slot = old >> 40;
     if (slot < a.s.bigCapacity) {
@@ -316,8 +322,8 @@ __device__ __noinline__ void raster_serial_alpha(const TriRec& r, const AlphaExt
 __device__ __forceinline__ bool enqueue_alpha(const TriRec& r, const AlphaExt& x, const DrawArgs& a, uint32_t chunk) {
     const int tilesX = ((r.bbMax & 0xFFFF) - (r.bbMin & 0xFFFF)) >> 2;
     const int tilesY = ((r.bbMax >> 16) - (r.bbMin >> 16)) >> 2;
-    const unsigned long long chunks = (unsigned long long)((tilesX + chunk - 1) / chunk) *
-                                      (unsigned long long)((tilesY + chunk - 1) / chunk);
+    const uint32_t cw = chunk & 0xFF, ch = chunk >> 8;
+    const unsigned long long chunks = (unsigned long long)((tilesX + cw - 1) / cw) * (unsigned long long)((tilesY + ch - 1) / ch);
     const unsigned long long old = atomicAdd(&a.s.control[1], (2ull << 40) | chunks);
     const unsigned long long slot = old >> 40, base = old & ((1ull << 40) - 1);
     if (slot + 1 < a.s.bigCapacity) {
@@ -718,7 +724,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     const uint8_t* idxBytes = (const uint8_t*)S.idx;
     TriRec* tris = S.tris;
     const ViewParams& vp = S.view;
-    const uint32_t chunk = a.chunkTiles ? a.chunkTiles : kChunkTiles;
+    const uint32_t chunk = chunk_shape(a);
     const bool multi = a.views != nullptr;
     // Work positions. Position p of a view draws its meshlet draw_order(p) (order_stride); a batched
     // draw concatenates its views' positions, padded to multiples of kBatchGroup (viewStart); the
@@ -1037,7 +1043,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     }
 }
 
-// Chunk stage: warps take runs of up to kChunkRun consecutive chunks (chunk x chunk tiles) of the queued
+// Chunk stage: warps take runs of up to kChunkRun consecutive chunks (chunk_shape: w x h tiles) of the queued
 // triangles from a global cursor (control[8], zeroed by the mesh stage), locate the run's first
 // chunk by binary search over the queue's chunk prefix and walk the rest sequentially. A queued
 // triangle carries its view in pad (batched draws) or belongs to the single view; an alpha-tested
@@ -1071,8 +1077,8 @@ __global__ void __launch_bounds__(256, 5) k_raster_big(const TriRec* __restrict_
     const TriRec& last = big[n - 1];
     const int lastTX = (int)(((last.bbMax & 0xFFFF) - (last.bbMin & 0xFFFF)) >> 2);
     const int lastTY = (int)(((last.bbMax >> 16) - (last.bbMin >> 16)) >> 2);
-    const unsigned long long total = bigBase[n - 1] + (unsigned long long)((lastTX + chunk - 1) / chunk) *
-                                                          ((lastTY + chunk - 1) / chunk);
+    const uint32_t cw = chunk & 0xFF, ch = chunk >> 8;
+    const unsigned long long total = bigBase[n - 1] + (unsigned long long)((lastTX + cw - 1) / cw) * ((lastTY + ch - 1) / ch);
     // a sparse queue (few big triangles) is spread with shorter runs so that every warp gets work
     const unsigned long long warps = (unsigned long long)gridDim.x * (blockDim.x >> 5);
     const unsigned long long run = max(1ull, min((unsigned long long)kChunkRun, total / (warps * kRunsPerWarp)));
@@ -1107,10 +1113,10 @@ __global__ void __launch_bounds__(256, 5) k_raster_big(const TriRec* __restrict_
             }
             const uint32_t c = (uint32_t)(w - base);
             const uint32_t minX = r.bbMin & 0xFFFF, minY = r.bbMin >> 16, maxX = r.bbMax & 0xFFFF, maxY = r.bbMax >> 16;
-            const uint32_t chunksX = (((maxX - minX) >> 2) + chunk - 1) / chunk;
+            const uint32_t chunksX = (((maxX - minX) >> 2) + cw - 1) / cw;
             const uint32_t cy = c / chunksX, cx = c - cy * chunksX;
-            const uint32_t x0 = minX + cx * (chunk * 4), y0 = minY + cy * (chunk * 4);
-            const uint32_t x1 = min(x0 + chunk * 4, maxX), y1 = min(y0 + chunk * 4, maxY);
+            const uint32_t x0 = minX + cx * (cw * 4), y0 = minY + cy * (ch * 4);
+            const uint32_t x1 = min(x0 + cw * 4, maxX), y1 = min(y0 + ch * 4, maxY);
             // Empty and hidden tiles of the chunk are rejected inside raster_region.
             if constexpr (kOver) {
                 raster_region_overdraw(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys, counts, vwidth, lane);
@@ -1242,7 +1248,7 @@ void launch_draw(const DrawArgs& args, cudaStream_t st, int numSMs) {
                          a.counts ? (const void*)k_draw_meshlets<kPassOverdraw> : (const void*)k_draw_meshlets<kPassOpaque>,
                          smem);
     if (a.s.alphaList && smemAlpha > 48 * 1024) raise_smem_limit(kPassAlpha, (const void*)k_draw_meshlets<kPassAlpha>, smemAlpha);
-    const uint32_t chunk = a.chunkTiles ? a.chunkTiles : kChunkTiles;
+    const uint32_t chunk = chunk_shape(a);
     const int grid = numSMs * (32 / warps);  // 64 registers a thread leave room for 32 resident warps per SM
     if (a.counts) {  // OverdrawShader: one pass, every meshlet
         {

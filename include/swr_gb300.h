@@ -260,6 +260,10 @@ swr_status swr_batch_set_views(swr_batch b, const swr_view_desc* views, uint32_t
 /* Chunk (bin) edge in 4x4 tiles: 2, 4, 8, 16 (8-64 pixels); warps per mesh-stage block: 4, 8, 16;
  * 0 = default (8, 8). Changing them re-captures the graph at the next render. */
 swr_status swr_batch_set_tuning(swr_batch b, uint32_t chunk_tiles, uint32_t warps_per_block);
+/* Rectangular chunks (bins) of the chunk rasterizer: chunk_w_tiles x chunk_h_tiles 4x4 tiles, each
+ * 2, 4, 8 or 16 (8-64 pixels); keeps the warps per block. swr_batch_set_tuning sets square chunks.
+ * The image never depends on the shape. */
+swr_status swr_batch_set_chunk_shape(swr_batch b, uint32_t chunk_w_tiles, uint32_t chunk_h_tiles);
 swr_status swr_batch_render(swr_batch b);
 swr_status swr_batch_get_counters(swr_batch b, uint64_t out[SWR_NUM_COUNTERS]);
 swr_status swr_batch_reset_counters(swr_batch b);

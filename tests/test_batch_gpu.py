@@ -47,11 +47,14 @@ def check_all(api, sc, scene, rast, fbs):
             assert np.array_equal(fb.get_pixels(0), ref.get_pixels(0)), "surface ids differ"
 
 
-@pytest.mark.parametrize("tuning", [(0, 0), (2, 4), (16, 16), (4, 8)])
+@pytest.mark.parametrize("tuning", [(0, 0), (2, 4), (16, 16), (4, 8), (16, 8, 2), (2, 16, 8), (8, 4, 16)])
 def test_batch_equals_per_view_draws(setup, tuning):
+    """Any chunk size, chunk shape (width x height tiles) and warps per block gives the same views."""
     from glimpsw_gb300 import api
     sc, scene, rast, fbs, views, batch = setup
-    batch.set_tuning(*tuning)
+    batch.set_tuning(*tuning[:2])
+    if len(tuning) == 3:
+        batch.set_chunk_shape(tuning[0], tuning[2])
     batch.render()
     check_all(api, sc, scene, rast, fbs)
 
@@ -82,7 +85,11 @@ def test_batch_counts_kernels_and_autotunes(setup, tmp_path, monkeypatch):
     sc, scene, rast, fbs, views, batch = setup
     monkeypatch.setenv("SWR_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
     best, timings = autotune.tune(batch, key="test", repeats=1)
-    assert best in autotune.CANDIDATES and len(timings) == len(autotune.CANDIDATES)
+    squares = [(c, w, c) for c, w in autotune.CANDIDATES]
+    assert all(s in timings for s in squares) and best in timings
+    c0, w0, _ = min(squares, key=timings.get)
+    assert len(timings) == len(squares) + len(autotune.shape_candidates(c0))
+    assert any(cw != ch for cw, _, ch in timings)  # rectangular chunks were timed
     best2, _ = autotune.tune(batch, key="test")  # cached
     assert best2 == best
     n0 = api.launch_count()
