@@ -128,26 +128,26 @@ __device__ __forceinline__ void shade_tiny(const TriRec& r, const TinyBox& b, un
 
 // Upper bound of the depth tile_pixel_key computes for any sample of the 4x4 tile at (px, py).
 // The exact depth Z0 + Z10 e1 + Z20 e2 is affine in the pixel (the edge values are exact
-// integers), so its maximum over the tile is at a corner. A computed depth differs from the exact
-// one by at most 4u (|Z0| + |Z10 e1| + |Z20 e2|), u = 2^-24 (two conversions, two fma roundings),
-// and |e| is largest at a corner too, so corner value + 2^-20 * that sum bounds every sample.
-// NaN anywhere gives +inf (never culled).
+// integers): it is the first sample's plus i Gx + j Gy at sample (i, j), with the per-pixel steps
+// Gx = Z10 A20 + Z20 A01 and Gy = Z10 B20 + Z20 B01, so its maximum over the tile is the first
+// sample's plus 3 max(Gx, 0) + 3 max(Gy, 0). A computed sample depth differs from the exact one by
+// at most 4u S, u = 2^-24, S = |Z0| + |Z10| max|e1| + |Z20| max|e2| (two conversions, two fma
+// roundings), and the bound's own evaluation by at most 10u S more; 2^-18 S covers both four times
+// over. max|e| over the tile is at most |e(first)| + 3 (|A| + |B|). A NaN or infinite term gives +inf
+// (never culled).
 __device__ __forceinline__ float tile_depth_bound(const TriRec& r, uint32_t px, uint32_t py) {
-    float dmax = -FLT_MAX, a1 = 0.0f, a2 = 0.0f;
-    bool nan = false;
-#pragma unroll
-    for (int c = 0; c < 4; c++) {
-        const uint32_t x = px + (c & 1) * 3, y = py + (c >> 1) * 3;
-        const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * x + (uint32_t)r.B20 * y);
-        const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * x + (uint32_t)r.B01 * y);
-        const float f1 = __int2float_rn(e1), f2 = __int2float_rn(e2);
-        const float d = ffma(f1, r.Z10, ffma(f2, r.Z20, r.Z0));
-        nan |= d != d;
-        dmax = d > dmax ? d : dmax;
-        a1 = fmaxf(a1, fabsf(f1)), a2 = fmaxf(a2, fabsf(f2));
-    }
+    const int32_t e1 = (int32_t)((uint32_t)r.E1 + (uint32_t)r.A20 * px + (uint32_t)r.B20 * py);
+    const int32_t e2 = (int32_t)((uint32_t)r.E2 + (uint32_t)r.A01 * px + (uint32_t)r.B01 * py);
+    const float f1 = __int2float_rn(e1), f2 = __int2float_rn(e2);
+    const float d = ffma(f1, r.Z10, ffma(f2, r.Z20, r.Z0));
+    const float gx = ffma(r.Z10, (float)r.A20, fmul(r.Z20, (float)r.A01));
+    const float gy = ffma(r.Z10, (float)r.B20, fmul(r.Z20, (float)r.B01));
+    const float dmax = fadd(d, fmul(3.0f, fadd(fmaxf(gx, 0.0f), fmaxf(gy, 0.0f))));
+    const float a1 = fadd(fabsf(f1), fmul(3.0f, (float)(abs(r.A20) + abs(r.B20))));
+    const float a2 = fadd(fabsf(f2), fmul(3.0f, (float)(abs(r.A01) + abs(r.B01))));
     const float s = fadd(fabsf(r.Z0), fadd(fmul(fabsf(r.Z10), a1), fmul(fabsf(r.Z20), a2)));
-    return nan ? __int_as_float(0x7F800000) : fadd(dmax, fmul(s, 0x1p-20f));
+    const float b = fadd(dmax, fmul(s, 0x1p-18f));
+    return b == b ? b : __int_as_float(0x7F800000);
 }
 
 // Raises the tile's depth bound to the minimum of the values its 16 pixels reported (the two
