@@ -180,8 +180,9 @@ constexpr uint32_t kShadedSize = 1472, kShadedIndices = 64, kShadedPositions = 4
 // spatially coherent order (meshlets built from a mesh, a grid) a fetch of 32 positions can
 // otherwise be 32 visible neighbours close to the camera, all for one warp, and concurrent warps
 // contend for the same pixels' keys. Keys are order-independent, so the image is the same for
-// every order. Work is fetched kDrawGroup positions at a time in single-view draws, kBatchGroup in
-// batches (whose views' position ranges are padded to multiples of it).
+// every order. Work is fetched kBatchGroup positions at a time in batches (whose views' position
+// ranges are padded to multiples of it); single-view draws start at kDrawGroup positions and adapt
+// the group to the share of visible meshlets, and the alpha pass takes kDrawGroup list entries.
 constexpr uint32_t kDrawGroup = 4, kBatchGroup = 32;
 uint32_t order_stride(uint32_t count);
 

@@ -749,14 +749,15 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     unsigned long long nProcessed = 0, nRaster = 0, nClipped = 0;
     if (!kAlpha && blockIdx.x == 0 && threadIdx.x == 0) a.s.control[8] = 0;  // the chunk stage's cursor (runs later)
 
-    // Work items are fetched a group at a time: one contended atomic per group. Batched draws,
-    // most of whose (view, meshlet) items are culled, fetch groups of 32 and test the 32 cull bits
-    // at once (one item per lane), then walk the visible ones. A work item is viewStart[view] + m
-    // (m alone in single-view draws), as the alpha list records it.
-    uint32_t fetchPos = 0, fetchLeft = 0;  // single view and alpha pass: next position, positions left
-    uint32_t laneMeshlet = 0;              // batched draws: the meshlet of this lane's position in the group
-    uint32_t fetchView = 0;
-    unsigned fetchMask = 0;                // batched draws: lanes whose meshlet is visible
+    // Work items are fetched a group at a time: one contended atomic per group. A group's cull
+    // bits are tested at once (one position per lane), then the warp walks the visible ones.
+    // Batched draws, most of whose (view, meshlet) items are culled, fetch groups of 32. A work
+    // item is viewStart[view] + m (m alone in single-view draws), as the alpha list records it.
+    uint32_t fetchPos = 0, fetchLeft = 0;  // alpha pass: next position, positions left
+    uint32_t laneMeshlet = 0;              // the meshlet of this lane's position in the group
+    uint32_t fetchView = 0;                // batched draws: the view of the fetched group
+    unsigned fetchMask = 0;                // lanes of the fetched group whose meshlet is visible
+    uint32_t fetchGroup = kDrawGroup;      // single view: positions per fetch
     while (true) {
         uint32_t m, view = 0, item;
         if constexpr (kAlpha) {
@@ -801,16 +802,29 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                 fetchMask &= fetchMask - 1;
                 item = a.viewStart[view] + m;
             } else {
-                if (fetchLeft == 0) {
+                // Single view: groups of fetchGroup positions (2 to 32), their cull bits tested at
+                // once (one position per lane). The group grows while groups come back empty (a
+                // sparse view fetches 32 positions per atomic) and shrinks while they hold more than
+                // one visible meshlet (a dense view fetches about one visible meshlet at a time, so
+                // the last work items spread evenly over the warps).
+                if (fetchMask == 0) {
                     uint32_t b = 0;
-                    if (lane == 0) b = (uint32_t)atomicAdd(cursor, (unsigned long long)kDrawGroup);
-                    fetchPos = __shfl_sync(0xFFFFFFFFu, b, 0);
-                    fetchLeft = kDrawGroup;
+                    if (lane == 0) b = (uint32_t)atomicAdd(cursor, (unsigned long long)fetchGroup);
+                    const uint32_t base = __shfl_sync(0xFFFFFFFFu, b, 0);
+                    if (base >= totalItems) break;
+                    const uint32_t q = base + lane;
+                    bool vis = false;
+                    if (lane < fetchGroup && q < totalItems) {
+                        laneMeshlet = draw_order(q, a.count, a.orderStride);
+                        vis = a.cullBitmap == nullptr || ((a.cullBitmap[laneMeshlet >> 4] >> (laneMeshlet & 15)) & 1);
+                    }
+                    fetchMask = __ballot_sync(0xFFFFFFFFu, vis);
+                    const int got = __popc(fetchMask);
+                    fetchGroup = got == 0 ? min(fetchGroup * 2, 32u) : (got > 1 ? max(fetchGroup / 2, 2u) : fetchGroup);
+                    if (fetchMask == 0) continue;
                 }
-                const uint32_t p = fetchPos++;
-                fetchLeft--;
-                if (p >= totalItems) break;
-                m = draw_order(p, a.count, a.orderStride);
+                m = __shfl_sync(0xFFFFFFFFu, laneMeshlet, __ffs(fetchMask) - 1);
+                fetchMask &= fetchMask - 1;
                 item = m;
             }
         }
@@ -820,7 +834,8 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
             __syncwarp();
             curView = view;
         }
-        if (vp.cullBitmap != nullptr && !((vp.cullBitmap[m >> 4] >> (m & 15)) & 1)) continue;  // Shading.cpp:282-289
+        // (the fetch skipped meshlets whose cull bit is clear, Shading.cpp:282-289; the alpha list
+        // holds visible ones only)
 
         const uint32_t g = vp.meshletOffset + m;
         const uint8_t* mp = a.meshlets + (size_t)g * kMeshletSize;
