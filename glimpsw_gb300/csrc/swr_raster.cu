@@ -884,31 +884,38 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
         __syncwarp();
 
         // About half of a closed meshlet's triangles face away. The face test runs first for all of
-        // them and compacts the rest into S.live, so the setup and binning below run on full
-        // 32-triangle steps. Each triangle keeps its index p (its rank), so the keys do not change.
+        // them and compacts the rest into S.live (index p, and bit 7 for a triangle that needs
+        // clipping), so the setup and binning below run on full 32-triangle steps. Each triangle
+        // keeps its index p (its rank), so the keys do not change.
         uint32_t nLive = 0;
         for (uint32_t base = 0; base < nt; base += 32) {
             const uint32_t p = base + lane;
             const LaneTri lt = lane_triangle(S.ndc, S.code, idxBytes, p, p < nt);
             if (a.countClipped) nClipped += __popc(__ballot_sync(0xFFFFFFFFu, lt.nontriv)) * (lane == 0);
-            const bool live = (lt.nontriv && a.clipMode) || (lt.acc && front_facing(lt.n0, lt.n1, lt.n2, cullMode));
+            const bool clip = lt.nontriv && a.clipMode;
+            const bool live = clip || (lt.acc && front_facing(lt.n0, lt.n1, lt.n2, cullMode));
             const unsigned liveMask = __ballot_sync(0xFFFFFFFFu, live);
-            if (live) S.live[nLive + __popc(liveMask & ((1u << lane) - 1u))] = (uint8_t)p;
+            if (live) S.live[nLive + __popc(liveMask & ((1u << lane) - 1u))] = (uint8_t)(p | (clip ? 0x80u : 0u));
             nLive += __popc(liveMask);
         }
         __syncwarp();
 
         for (uint32_t base = 0; base < nLive; base += 32) {
             const bool valid = base + lane < nLive;
-            const uint32_t p = valid ? S.live[base + lane] : 0u;
-            const LaneTri lt = lane_triangle(S.ndc, S.code, idxBytes, p, valid);
+            const uint32_t e = valid ? S.live[base + lane] : 0u;
+            const uint32_t p = e & 127u;
+            const bool accepted = valid && !(e & 0x80u), clipped = valid && (e & 0x80u);
 
             int myTiles = 0;     // tiles of this lane's small triangle (0 if none)
             bool overflow = false;
-            if (lt.acc) {
+            if (accepted) {  // trivially accepted and front-facing (the first pass's face test)
                 Setup t;
                 uint32_t bbMin, bbMax;
-                if (tri_setup_ndc(lt.n0, lt.n1, lt.n2, vp.halfW, vp.halfH, cullMode, t, bbMin, bbMax)) {
+                const uint32_t i0 = preload64_index(idxBytes[p]), i1 = preload64_index(idxBytes[128 + p]),
+                               i2 = preload64_index(idxBytes[256 + p]);
+                const float4 q0 = S.ndc[i0], q1 = S.ndc[i1], q2 = S.ndc[i2];
+                if (tri_setup_ndc_facing({ q0.x, q0.y, q0.z, q0.w }, { q1.x, q1.y, q1.z, q1.w }, { q2.x, q2.y, q2.z, q2.w },
+                                         vp.halfW, vp.halfH, t, bbMin, bbMax)) {
                     TriRec r;
                     float rcpArea;
                     const int32_t det = edge_setup(t, vp.halfW, vp.halfH, bbMin, bbMax, make_rank(g, p, 0, 0), r, &rcpArea);
@@ -946,14 +953,16 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                     }
                 }
             }
-            if (lt.nontriv && a.clipMode) {  // rare: the clip-space vertices are transformed again
+            if (clipped) {  // rare: the clip-space vertices are transformed again
+                const uint32_t i0 = preload64_index(idxBytes[p]), i1 = preload64_index(idxBytes[128 + p]),
+                               i2 = preload64_index(idxBytes[256 + p]);
+                const uint32_t partial = (S.code[i0] | S.code[i1] | S.code[i2]) & 0x3Fu;
                 auto clip_vertex = [&](uint32_t v) {
                     const float4 c = kShaded ? make_float4(P[v], P[64 + v], P[128 + v], P[192 + v])
                                              : clip_position(P[v], P[64 + v], P[128 + v], v < nvr, vp);
                     return Vtx{ c.x, c.y, c.z, c.w };
                 };
-                clip_and_queue(clip_vertex(preload64_index(idxBytes[p])), clip_vertex(preload64_index(idxBytes[128 + p])),
-                               clip_vertex(preload64_index(idxBytes[256 + p])), lt.partial, a, vp, view, chunk, cullMode, g, p,
+                clip_and_queue(clip_vertex(i0), clip_vertex(i1), clip_vertex(i2), partial, a, vp, view, chunk, cullMode, g, p,
                                nRaster, kAlpha ? matId : ~0u, mp, idxBytes);
             }
             __syncwarp();

@@ -85,6 +85,23 @@ __device__ __forceinline__ bool tri_setup_ndc(const Ndc& n0, const Ndc& n1, cons
     return keep;
 }
 
+// tri_setup_ndc for a triangle already known to pass the face test (front_facing true): the same
+// positions and bounding box; the keep bit is the box test alone.
+__device__ __forceinline__ bool tri_setup_ndc_facing(const Ndc& n0, const Ndc& n1, const Ndc& n2, int halfW, int halfH,
+                                                     Setup& t, uint32_t& bbMin, uint32_t& bbMax) {
+    const float fsx = (float)(halfW * 16), fsy = (float)(halfH * 16);
+    const int32_t ix0 = round2i(fmul(n0.x, fsx)), iy0 = round2i(fmul(n0.y, fsy));
+    const int32_t ix1 = round2i(fmul(n1.x, fsx)), iy1 = round2i(fmul(n1.y, fsy));
+    const int32_t ix2 = round2i(fmul(n2.x, fsx)), iy2 = round2i(fmul(n2.y, fsy));
+    t.Pos0 = ((uint32_t)ix0 & 0xFFFF) | ((uint32_t)iy0 << 16);
+    t.Pos1 = ((uint32_t)ix1 & 0xFFFF) | ((uint32_t)iy1 << 16);
+    t.Pos2 = ((uint32_t)ix2 & 0xFFFF) | ((uint32_t)iy2 << 16);
+    render_bbox(t, halfW, halfH, bbMin, bbMax);
+    t.Z0 = n0.z, t.Z1 = n1.z, t.Z2 = n2.z;
+    t.W0 = n0.rw, t.W1 = n1.rw, t.W2 = n2.rw;
+    return lo16(bbMin) < lo16(bbMax) && hi16(bbMin) < hi16(bbMax);
+}
+
 // TrianglePacket::Setup from clip-space vertices (the clipper's output triangles).
 __device__ __forceinline__ bool tri_setup(Vtx v0, Vtx v1, Vtx v2, int halfW, int halfH, int cullMode, Setup& t,
                                           uint32_t& bbMin, uint32_t& bbMax) {
