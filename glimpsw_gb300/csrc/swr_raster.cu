@@ -126,6 +126,14 @@ __device__ __forceinline__ void shade_tiny(const TriRec& r, const TinyBox& b, un
         }
 }
 
+// ceil(256 / n) for n = 1..16, the multiplier of the small triangles' tile -> row multiply-shift:
+// ceil(256 / n) - 1 packed 8 bits per entry in two words (an integer divide per triangle costs more
+// than the rest of its tile bookkeeping).
+__device__ __forceinline__ uint32_t row_magic(int n) {
+    const unsigned long long t = n <= 8 ? 0x1f242a333f557fffull : 0xf1112131517191cull;
+    return (uint32_t)((t >> (8 * ((n - 1) & 7))) & 0xFF) + 1u;
+}
+
 // Upper bound of the depth tile_pixel_key computes for any sample of the 4x4 tile at (px, py).
 // The exact depth Z0 + Z10 e1 + Z20 e2 is affine in the pixel (the edge values are exact
 // integers): it is the first sample's plus i Gx + j Gy at sample (i, j), with the per-pixel steps
@@ -931,7 +939,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                         shade_tiny(r, tb, vp.keys, vp.width);
                     } else if (tilesX * tilesY <= kSmallTiles) {
                         // tile index -> row by a multiply-shift (exact for tile < 16, tilesX <= 16)
-                        r.pad = (uint32_t)tilesX | ((uint32_t)((256 + tilesX - 1) / tilesX) << 8);
+                        r.pad = (uint32_t)tilesX | (row_magic(tilesX) << 8);
                         tris[lane] = r;
                         if constexpr (kAlpha) S.exts[lane] = x;
                         myTiles = tilesX * tilesY;
