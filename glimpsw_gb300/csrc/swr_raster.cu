@@ -43,6 +43,16 @@ constexpr int kPacketTiles = 128;  // in-warp tile budget of a 32-triangle step
 constexpr int kSpreadTiles = 4;    // over budget, triangles above this many tiles are queued
 constexpr int kChunkTiles = 8;  // chunk = 8x8 tiles = 32x32 pixels
 
+// A record in a warp's shared memory padded to 80 bytes. TriRec and AlphaExt are 64 bytes; with a
+// 64-byte stride the 16-byte loads of one field by lanes holding different triangles (the tile
+// tests) fall into two of the eight 16-byte bank groups of a quarter warp, with an 80-byte stride
+// into eight. The loads stay 16-byte vectors.
+template <class T>
+struct __align__(16) Padded {
+    T v;
+    uint4 pad;
+};
+
 // A draw's chunk shape as passed to the queue and chunk stage: width | height << 8, in tiles.
 __host__ __device__ __forceinline__ uint32_t chunk_shape(const DrawArgs& a) {
     const uint32_t w = a.chunkTiles ? a.chunkTiles : (uint32_t)kChunkTiles;
@@ -460,9 +470,10 @@ __device__ __forceinline__ void shade_live_tiles(Rec&& rec, uint32_t rsel, unsig
 }
 
 // shade_live_tiles for alpha-tested triangles of one material (texture tex, cutoff << 24): a
-// candidate's triangle is tris[rsel], its alpha terms exts[rsel] (the two tiles of a step may
-// belong to different triangles).
-__device__ __forceinline__ void shade_live_tiles_alpha(const TriRec* tris, const AlphaExt* exts, uint32_t rsel,
+// candidate's triangle is rec(rsel), its alpha terms ext(rsel) (the two tiles of a step may belong
+// to different triangles).
+template <class Rec, class Ext>
+__device__ __forceinline__ void shade_live_tiles_alpha(Rec&& rec, Ext&& ext, uint32_t rsel,
                                                        const DevTexture& tex, uint32_t cutoff, unsigned mask,
                                                        uint32_t tpx, uint32_t tpy, uint32_t tmin,
                                                        unsigned long long* keys, uint32_t* tileMin, uint32_t width,
@@ -478,7 +489,7 @@ __device__ __forceinline__ void shade_live_tiles_alpha(const TriRec* tris, const
         const uint32_t qy = __shfl_sync(0xFFFFFFFFu, tpy, src & 31);
         const uint32_t qm = __shfl_sync(0xFFFFFFFFu, tmin, src & 31);
         const uint32_t qr = __shfl_sync(0xFFFFFFFFu, rsel, src & 31);
-        const uint32_t obs = shade_tile_pixel_alpha(tris[qr], exts[qr], tex, cutoff, qx, qy, src >= 0, lane, keys, width);
+        const uint32_t obs = shade_tile_pixel_alpha(rec(qr), ext(qr), tex, cutoff, qx, qy, src >= 0, lane, keys, width);
         if (tileMin) update_tile_min(obs, tileMin, (qy >> 2) * tw + (qx >> 2), qm, src >= 0, lane);
     }
 }
@@ -520,7 +531,9 @@ __device__ __forceinline__ void raster_region_alpha(const TriRec* rp, const Alph
                                                     unsigned long long* keys, uint32_t* tileMin, uint32_t width, int lane) {
     raster_region_with(*rp, x0, y0, tilesX, tilesY, tileMin, width, lane,
                        [&](unsigned mask, uint32_t tpx, uint32_t tpy, uint32_t tmin) {
-                           shade_live_tiles_alpha(rp, xp, 0, tex, cutoff, mask, tpx, tpy, tmin, keys, tileMin, width, lane);
+                           shade_live_tiles_alpha([&](uint32_t) -> const TriRec& { return *rp; },
+                                                  [&](uint32_t) -> const AlphaExt& { return *xp; }, 0, tex, cutoff, mask, tpx,
+                                                  tpy, tmin, keys, tileMin, width, lane);
                        });
 }
 
@@ -684,7 +697,7 @@ __device__ __forceinline__ LaneTri lane_triangle(const float4* ndc, const uint8_
 struct WarpSmem {
     float4 ndc[64];      // projected vertices: x/w, y/w, z/w, 1/w
     uint32_t idx[96];
-    TriRec tris[32];
+    Padded<TriRec> tris[32];
     ViewParams view;
     uint8_t owner[32 * kSmallTiles];
     uint8_t code[64];    // vertex_code
@@ -692,7 +705,7 @@ struct WarpSmem {
     float zmax[32];      // each small triangle's depth bound (triangle_depth_bound)
 };
 struct WarpSmemAlpha : WarpSmem {
-    AlphaExt exts[32];
+    Padded<AlphaExt> exts[32];
 };
 
 // Mesh stage. A work item is one meshlet of one view: a single-view draw numbers its meshlets
@@ -730,7 +743,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     Smem& S = ((Smem*)smemRaw)[warp];
     const uint8_t* idxBytes = (const uint8_t*)S.idx;
-    TriRec* tris = S.tris;
+    Padded<TriRec>* tris = S.tris;
     const ViewParams& vp = S.view;
     const uint32_t chunk = chunk_shape(a);
     const bool multi = a.views != nullptr;
@@ -940,8 +953,8 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                     } else if (tilesX * tilesY <= kSmallTiles) {
                         // tile index -> row by a multiply-shift (exact for tile < 16, tilesX <= 16)
                         r.pad = (uint32_t)tilesX | (row_magic(tilesX) << 8);
-                        tris[lane] = r;
-                        if constexpr (kAlpha) S.exts[lane] = x;
+                        tris[lane].v = r;
+                        if constexpr (kAlpha) S.exts[lane].v = x;
                         myTiles = tilesX * tilesY;
                         S.zmax[lane] = triangle_depth_bound(t);
                     } else {
@@ -949,13 +962,13 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                         if constexpr (kAlpha) {
                             r.pad = view | kTriAlpha;
                             queued = enqueue_alpha(r, x, a, chunk);
-                            if (!queued) S.exts[lane] = x;
+                            if (!queued) S.exts[lane].v = x;
                         } else {
                             r.pad = view;
                             queued = enqueue_big(r, a, chunk);
                         }
                         if (!queued) {
-                            tris[lane] = r;
+                            tris[lane].v = r;
                             overflow = true;
                         }
                     }
@@ -989,11 +1002,11 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                 spread = __shfl_sync(0xFFFFFFFFu, idle, 0) * 2 >= numWarps;
             }
             if (spread && myTiles > kSpreadTiles) {
-                TriRec r = tris[lane];
+                TriRec r = tris[lane].v;
                 bool queued;
                 if constexpr (kAlpha) {
                     r.pad = view | kTriAlpha;
-                    queued = enqueue_alpha(r, S.exts[lane], a, chunk);
+                    queued = enqueue_alpha(r, S.exts[lane].v, a, chunk);
                 } else {
                     r.pad = view;
                     queued = enqueue_big(r, a, chunk);
@@ -1023,7 +1036,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                 bool live = false;
                 uint32_t tpx = 0, tpy = 0, tmin = 0;
                 if (t < total) {
-                    const TriRec& r = tris[own];
+                    const TriRec& r = tris[own].v;
                     const int tile = t - ownerExcl;
                     const int tilesX = r.pad & 0xFF, magic = r.pad >> 8;
                     const int ty = (tile * magic) >> 8, tx = tile - ty * tilesX;
@@ -1033,13 +1046,15 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                 const unsigned liveMask = __ballot_sync(0xFFFFFFFFu, live);
                 if constexpr (kAlpha) {
                     const DevMaterial& mt = a.materials[matId];
-                    shade_live_tiles_alpha(tris, S.exts, own, mt.tex, mt.alpha_cutoff << 24, liveMask, tpx, tpy, tmin,
-                                           vp.keys, vp.tileMin, vp.width, lane);
+                    shade_live_tiles_alpha([&](uint32_t q) -> const TriRec& { return tris[q].v; },
+                                           [&](uint32_t q) -> const AlphaExt& { return S.exts[q].v; }, own, mt.tex,
+                                           mt.alpha_cutoff << 24, liveMask, tpx, tpy, tmin, vp.keys, vp.tileMin, vp.width,
+                                           lane);
                 } else if constexpr (kOver) {
-                    shade_live_tiles_overdraw([&](uint32_t q) -> const TriRec& { return tris[q]; }, own, liveMask, tpx, tpy,
+                    shade_live_tiles_overdraw([&](uint32_t q) -> const TriRec& { return tris[q].v; }, own, liveMask, tpx, tpy,
                                               vp.keys, a.counts, vp.width, lane);
                 } else {
-                    shade_live_tiles([&](uint32_t q) -> const TriRec& { return tris[q]; }, own, liveMask, tpx, tpy, tmin,
+                    shade_live_tiles([&](uint32_t q) -> const TriRec& { return tris[q].v; }, own, liveMask, tpx, tpy, tmin,
                                      vp.keys, vp.tileMin, vp.width, lane, a.keyReadTiles);
                 }
             }
@@ -1048,12 +1063,12 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
             while (ovMask) {
                 const int src = __ffs(ovMask) - 1;
                 ovMask &= ovMask - 1;
-                const TriRec r = tris[src];
+                const TriRec r = tris[src].v;
                 const uint32_t x0 = r.bbMin & 0xFFFF, y0 = r.bbMin >> 16;
                 const int tx = (int)(((r.bbMax & 0xFFFF) - x0) >> 2), ty = (int)(((r.bbMax >> 16) - y0) >> 2);
                 if constexpr (kAlpha) {
                     const DevMaterial& mt = a.materials[matId];
-                    raster_region_alpha(&tris[src], &S.exts[src], mt.tex, mt.alpha_cutoff << 24, x0, y0, tx, ty, vp.keys,
+                    raster_region_alpha(&tris[src].v, &S.exts[src].v, mt.tex, mt.alpha_cutoff << 24, x0, y0, tx, ty, vp.keys,
                                         vp.tileMin, vp.width, lane);
                 } else if constexpr (kOver) {
                     raster_region_overdraw(r, x0, y0, tx, ty, vp.keys, a.counts, vp.width, lane);
