@@ -626,7 +626,7 @@ __device__ __noinline__ void raster_serial_overdraw(const TriRec& r, unsigned lo
 // bytes idxBytes).
 __device__ __noinline__ void clip_and_queue(Vtx v0, Vtx v1, Vtx v2, uint32_t outcodes, const DrawArgs& a,
                                             const ViewParams& vp, uint32_t viewIndex, uint32_t chunk, int cullMode,
-                                            uint32_t gMeshlet, uint32_t prim, unsigned long long& nRaster,
+                                            uint32_t gMeshlet, uint32_t prim, uint32_t& nRaster,
                                             uint32_t alphaMat, const uint8_t* mp, const uint8_t* idxBytes) {
     const bool alpha = alphaMat != ~0u;
     ClipPoly P;
@@ -767,7 +767,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
         curView = 0;
         __syncwarp();
     }
-    unsigned long long nProcessed = 0, nRaster = 0, nClipped = 0;
+    uint32_t nProcessed = 0, nRaster = 0, nClipped = 0;  // per warp, within 32 bits (< 2^21 meshlets x 128)
     if (!kAlpha && blockIdx.x == 0 && threadIdx.x == 0) a.s.control[8] = 0;  // the chunk stage's cursor (runs later)
 
     // Work items are fetched a group at a time: one contended atomic per group. A group's cull
@@ -1081,12 +1081,12 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
         __syncwarp();
     }
     // perf counters (Rasterizer.h:366-370)
-    nRaster = __reduce_add_sync(0xFFFFFFFFu, (unsigned)nRaster);
+    nRaster = __reduce_add_sync(0xFFFFFFFFu, nRaster);
     if (lane == 0) {
         atomicAdd(idleWarps, 1ull);
-        if (nProcessed) atomicAdd(&a.s.control[3], nProcessed);
-        if (nRaster) atomicAdd(&a.s.control[4], nRaster);
-        if (nClipped) atomicAdd(&a.s.control[5], nClipped);
+        if (nProcessed) atomicAdd(&a.s.control[3], (unsigned long long)nProcessed);
+        if (nRaster) atomicAdd(&a.s.control[4], (unsigned long long)nRaster);
+        if (nClipped) atomicAdd(&a.s.control[5], (unsigned long long)nClipped);
     }
 }
 
