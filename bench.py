@@ -17,7 +17,8 @@ API with the scene uploaded from pinned host memory and the colour image read ba
 inside the timed region. Host-to-device copies run at about 210 GB/s on the GB300's host link
 (0.82 ms for the 172.8 MB scene), so the end-to-end frame draws in batches of 12,000, 44,000 and
 44,000 meshlets whose uploads go up on a copy stream while the batches before them draw: only the
-first batch's 20.7 MB upload is not overlapped. The device-timed frame keeps the frame driver's
+first batch's 20.7 MB upload is not overlapped. The image goes back while the Hi-Z pyramid builds,
+written straight into the pinned host buffer by the de-tiling kernel. The device-timed frame keeps the frame driver's
 65,536-meshlet batches; both give the same image (checked). `--impl reference` times the reference's CPU algorithm (the oracle
 restatement; the reference itself cannot be compiled here) on the host cores.
 """
@@ -71,10 +72,9 @@ def parse():
     p.add_argument("--neural-height", type=int, default=1440)
     p.add_argument("--no-alpha", action="store_true")
     p.add_argument("--no-cone", action="store_true")
-    p.add_argument("--e2e-batch", type=int, default=44000,
-                   help="meshlets per draw batch of the end-to-end frame (each batch's upload overlaps the draws before)")
-    p.add_argument("--e2e-first", type=int, default=12000,
-                   help="meshlets of the end-to-end frame's first batch, whose upload nothing overlaps (0: --e2e-batch)")
+    p.add_argument("--e2e-batches", default="12000,44000",
+                   help="meshlets per draw batch of the end-to-end frame, comma-separated; the last size repeats "
+                        "until the scene is covered (each batch's upload overlaps the draws before it)")
     p.add_argument("--multiview-cameras", type=int, default=58,
                    help="cameras besides the 6 cube faces of the multi-view workload")
     p.add_argument("--only", default="all", choices=["all", "neural", "multiview"],
@@ -858,9 +858,10 @@ def run_ours(args):
         rctx = api.ShadingContext(scene, view.world_to_clip, world_to_clip=view.world_to_clip, skybox=env,
                                   view_pos=view.eye, lights=lights)
 
-        def run(uploaded=None):
+        def run(uploaded=None, resolved=None):
             """uploaded: per batch, an event after which its records are on the device, or None
-            (their upload then overlaps the culling and drawing of the batches before)."""
+            (their upload then overlaps the culling and drawing of the batches before). resolved:
+            an event recorded once the colour image is complete (before the Hi-Z build)."""
             fb.clear(0xFF000000, 0.0)
             for k, ((off, cnt), bm, ctx) in enumerate(zip(blist, bms, ctxs)):
                 if uploaded is not None and uploaded[k] is not None:
@@ -868,6 +869,8 @@ def run_ours(args):
                 api.cull_meshlets(scene, off, cnt, bm, *mats, W, H, hiz_in)
                 rast.draw_meshlets(fb, cnt, ctx)
             rctx.resolve(rast, fb)
+            if resolved is not None:
+                resolved.record(stream)
             api.downsample_depth(fb, hiz_out)
         return run
 
@@ -945,14 +948,21 @@ def run_ours(args):
     pinned = torch.empty(sc.meshlets.nbytes, dtype=torch.uint8).pin_memory()
     pinned.numpy()[:] = sc.meshlets.view(np.uint8).reshape(-1)
     host_img = torch.empty((H, W), dtype=torch.int32).pin_memory()
-    # The frame draws in batches of e2e_batch meshlets. The first batch's records go up on the
-    # frame's stream; the others' on a copy stream, each followed by an event that its batch's
-    # culling waits for, so each upload overlaps the culling and drawing of the batches before
-    # (every byte of the scene is still copied every step).
-    first = min(args.e2e_first or args.e2e_batch, n)
-    eb = [(0, first)] + [(off, min(args.e2e_batch, n - off)) for off in range(first, n, args.e2e_batch)]
+    # The frame draws in batches (--e2e-batches). The first batch's records go up on the frame's
+    # stream; the others' on a copy stream behind it (the host link is the limit, so sharing it
+    # would only delay the first batch), each followed by an event that its batch's culling waits
+    # for, so each upload overlaps the culling and drawing of the batches before (every byte of the
+    # scene is still copied every step). The colour image goes back on the copy stream while the
+    # frame's stream builds the Hi-Z pyramid.
+    sizes = [int(x) for x in args.e2e_batches.split(",")]
+    eb, off = [], 0
+    while off < n:
+        cnt = min(sizes[min(len(eb), len(sizes) - 1)], n - off)
+        eb.append((off, cnt))
+        off += cnt
     e2e_frame = frame_fn(v0, v0, None, hiz[0], eb)
     copy_stream = torch.cuda.Stream()
+    first_up, resolved = torch.cuda.Event(), torch.cuda.Event()
     uploaded = [None] + [torch.cuda.Event() for _ in eb[1:]]
     headline()
     expected = fb.get_pixels(0)  # the image the overlapped upload must reproduce
@@ -963,14 +973,20 @@ def run_ours(args):
         off0, cnt0 = eb[0]
         api._check(api._lib.swr_scene_upload_meshlets(scene.h, C.c_void_p(pinned.data_ptr() + off0 * MESHLET_BYTES),
                                                       off0, cnt0))
+        first_up.record(stream)
+        copy_stream.wait_event(first_up)
         api.set_stream(copy_stream.cuda_stream)
         for (off, cnt), ev in zip(eb[1:], uploaded[1:]):
             api._check(api._lib.swr_scene_upload_meshlets(scene.h, C.c_void_p(pinned.data_ptr() + off * MESHLET_BYTES),
                                                           off, cnt))
             ev.record(copy_stream)
         api.set_stream(stream.cuda_stream)
-        e2e_frame(uploaded)
+        e2e_frame(uploaded, resolved)
+        copy_stream.wait_event(resolved)
+        api.set_stream(copy_stream.cuda_stream)
         api._check(api._lib.swr_framebuffer_get_pixels(fb.h, 0, C.c_void_p(host_img.data_ptr()), W))
+        api.set_stream(stream.cuda_stream)
+        stream.synchronize()  # the Hi-Z build
         if i >= args.warmup:
             e2e_ms.append((time.perf_counter() - t0) * 1e3)
     if not np.array_equal(host_img.numpy().view(np.uint32).reshape(-1), np.asarray(expected).view(np.uint32).reshape(-1)):

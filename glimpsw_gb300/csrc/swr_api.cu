@@ -345,7 +345,7 @@ swr_status swr_framebuffer_get_pixels_device(swr_framebuffer fb, uint32_t layer,
         return fail(SWR_EINVAL, "swr_framebuffer_get_pixels_device: bad argument");
     swr_status st = swr_internal_finalize(fb);
     if (st != SWR_OK) return st;
-    launch_detile(fb->layers + (size_t)layer * fb->layer_stride, dest_device, fb->width, fb->height, t_stream);
+    launch_detile(fb->layers + (size_t)layer * fb->layer_stride, dest_device, fb->width, fb->height, fb->width, t_stream);
     SWR_CHECK_LAUNCH("swr_framebuffer_get_pixels_device");
     return SWR_OK;
 }
@@ -355,9 +355,21 @@ swr_status swr_framebuffer_get_pixels(swr_framebuffer fb, uint32_t layer, uint32
         return fail(SWR_EINVAL, "swr_framebuffer_get_pixels: bad argument");
     swr_status st = swr_internal_finalize(fb);
     if (st != SWR_OK) return st;
+    const uint32_t* src = fb->layers + (size_t)layer * fb->layer_stride;
+    // Pinned host memory the device can address is written by the detiling kernel itself, over the
+    // host link, with no staging copy; other memory goes through a device buffer and a copy.
+    cudaPointerAttributes pa = {};
+    if (cudaPointerGetAttributes(&pa, dest) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+        launch_detile(src, (uint32_t*)pa.devicePointer, fb->width, fb->height, stride, t_stream);
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaStreamSynchronize(t_stream);
+        if (e != cudaSuccess) return cuda_fail(e, "swr_framebuffer_get_pixels");
+        return SWR_OK;
+    }
+    cudaGetLastError();  // an unregistered pointer is not an error
     uint32_t* tmp = nullptr;
     SWR_CUDA(cudaMallocAsync(&tmp, (size_t)fb->width * fb->height * 4, t_stream));
-    launch_detile(fb->layers + (size_t)layer * fb->layer_stride, tmp, fb->width, fb->height, t_stream);
+    launch_detile(src, tmp, fb->width, fb->height, fb->width, t_stream);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess)
         e = cudaMemcpy2DAsync(dest, (size_t)stride * 4, tmp, (size_t)fb->width * 4, (size_t)fb->width * 4, fb->height,

@@ -2,7 +2,11 @@
 // (GenerateIrradianceMap / PrefilterDiffuseIrradiance), the GGX-prefiltered radiance map with one
 // roughness per mip level (GenerateRadianceMap / PrefilterEnvMap, Karis 2014) and the split-sum
 // environment BRDF table (GenerateEnvBRDFLut / IntegrateBRDF). The reference computes them on the
-// CPU and its frame driver never calls them; here each output texel is one GPU thread.
+// CPU and its frame driver never calls them. The radiance map has enough texels for one GPU thread
+// each. The irradiance map (4,096 texels of 32,400 samples at 64x64) and the BRDF table have too few
+// to fill the GPU that way, so their blocks work on 32 texels (one per lane) at a time: all warps but
+// the first compute sample terms of those texels into shared memory and the first adds them in
+// sample order.
 //
 // Exactness: every texel is an independent sum in the reference's order (its 16-lane tile
 // decisions, `any(NoL > 0)` and SampleOctLevel's `any(mipFrac > 0)`, give the same value as a
@@ -128,28 +132,66 @@ __device__ __forceinline__ float approx_log2(float x) {
     return fmaf(__uint2float_rn(__float_as_uint(x)), 1.1920928955078125e-7f, -126.94269504f);
 }
 
-// GenerateIrradianceMap (Shading.cpp:177-186) with PrefilterDiffuseIrradiance (72-102): level 0 of out.
-__global__ void k_ibl_irradiance(DevTexture env, DevTexture out, uint32_t* outData, IblTables tb) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= out.width * out.height) return;
+// Sums n sample terms of C channels for the block's 32 texels (lane l = texel l) in sample order.
+// Warps 1 to W - 1 compute the terms k = base + j * (W - 1) + warp - 1 (j < S) of each chunk of
+// (W - 1) * S samples into one of two shared buffers; after the chunk's barrier warp 0 adds them in
+// order while the others compute the next chunk. Warp 0 only adds: its 3 dependent adds a term take
+// a small fraction of the time the other warps spend on a chunk, so it never holds up a barrier. A
+// buffer is written again two chunks later, after the next barrier, which warp 0 reaches only when
+// it has added it. Returns the sums in warp 0's lanes.
+template <int W, int S, int C, class TermFn>
+__device__ __forceinline__ void ordered_block_sum(uint32_t n, TermFn term, float (&acc)[C], float* buf) {
+    constexpr uint32_t K = (W - 1) * S;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int c = 0; c < C; c++) acc[c] = 0.0f;
+    for (uint32_t base = 0, it = 0; base < n; base += K, it++) {
+        float* b = buf + (it & 1) * (K * C * 32);
+        if (warp > 0) {
+            for (uint32_t j = 0; j < S; j++) {
+                const uint32_t r = j * (W - 1) + warp - 1;
+                if (base + r < n) {
+                    float t[C];
+                    term(base + r, t);
+                    for (int c = 0; c < C; c++) b[(r * C + c) * 32 + lane] = t[c];
+                }
+            }
+        }
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t m = min(K, n - base);
+            for (uint32_t r = 0; r < m; r++)
+                for (int c = 0; c < C; c++) acc[c] = acc[c] + b[(r * C + c) * 32 + lane];
+        }
+    }
+}
+
+constexpr int kIrrWarps = 32, kIrrSteps = 2, kBrdfWarps = 8, kBrdfSteps = 4;
+
+// GenerateIrradianceMap (Shading.cpp:177-186) with PrefilterDiffuseIrradiance (72-102): level 0 of
+// out. Sample k is phi step k / numTheta, theta step k % numTheta; its term s * cos(theta) *
+// sin(theta) is added to the texel's sum in that order, as the reference's nested loops do.
+__global__ void __launch_bounds__(kIrrWarps * 32) k_ibl_irradiance(DevTexture env, DevTexture out, uint32_t* outData, IblTables tb) {
+    __shared__ float buf[2 * (kIrrWarps - 1) * kIrrSteps * 3 * 32];
+    const uint32_t n = out.width * out.height;
+    const uint32_t i = min(blockIdx.x * 32 + (threadIdx.x & 31), n - 1);  // lanes past the end repeat the last texel
     const uint32_t x = i % out.width, y = i / out.width;
     const float u = ((float)x + 0.5f) * (1.0f / (float)out.width), v = ((float)y + 0.5f) * (1.0f / (float)out.height);
     const F3 N = unmap_oct(u, v);
     F3 right, up;
     tangent_frame(N, right, up);
-    F3 color = { 0.0f, 0.0f, 0.0f };
-    for (uint32_t p = 0; p < tb.numPhi; p++) {
+    float color[3];
+    ordered_block_sum<kIrrWarps, kIrrSteps, 3>(tb.numPhi * tb.numTheta, [&](uint32_t k, float (&t)[3]) {
+        const uint32_t p = k / tb.numTheta, q = k - p * tb.numTheta;
         const float cp = tb.cosPhi[p], sp = tb.sinPhi[p];
         const F3 tmp = { cp * right.x + sp * up.x, cp * right.y + sp * up.y, cp * right.z + sp * up.z };
-        for (uint32_t q = 0; q < tb.numTheta; q++) {
-            const float ct = tb.cosTheta[q], st = tb.sinTheta[q];
-            const F3 dir = { ct * N.x + st * tmp.x, ct * N.y + st * tmp.y, ct * N.z + st * tmp.z };
-            const F3 s = tonemap_sample(sample_oct_level(env, dir, 2.0f), 1.0f);
-            color = { color.x + s.x * ct * st, color.y + s.y * ct * st, color.z + s.z * ct * st };
-        }
-    }
+        const float ct = tb.cosTheta[q], st = tb.sinTheta[q];
+        const F3 dir = { ct * N.x + st * tmp.x, ct * N.y + st * tmp.y, ct * N.z + st * tmp.z };
+        const F3 s = tonemap_sample(sample_oct_level(env, dir, 2.0f), 1.0f);
+        t[0] = s.x * ct * st, t[1] = s.y * ct * st, t[2] = s.z * ct * st;
+    }, color, buf);
+    if (threadIdx.x >= 32 || blockIdx.x * 32 + threadIdx.x >= n) return;
     const float k = tb.irradianceScale;
-    const F3 r = tonemap_sample({ color.x * k, color.y * k, color.z * k }, -1.0f);
+    const F3 r = tonemap_sample({ color[0] * k, color[1] * k, color[2] * k }, -1.0f);
     outData[out.mip_offsets[0] + texel_offset((int32_t)x, (int32_t)y, (int32_t)out.row_shift)] = pack_r11g11b10(r);
 }
 
@@ -192,23 +234,26 @@ __global__ void k_ibl_radiance(DevTexture env, DevTexture out, uint32_t* outData
 }
 
 // GenerateEnvBRDFLut (Shading.cpp:202-210) with IntegrateBRDF (149-175, 1024 samples): RG16f texel
-// (scale, bias) at NoV = u, roughness = v.
-__global__ void k_ibl_env_brdf(DevTexture out, uint32_t* outData, IblTables tb) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= out.width * out.height) return;
+// (scale, bias) at NoV = u, roughness = v. A sample with NoL <= 0 adds +0, as the reference's lanes
+// with Gv = 0 do (Shading.cpp:167).
+__global__ void __launch_bounds__(kBrdfWarps * 32) k_ibl_env_brdf(DevTexture out, uint32_t* outData, IblTables tb) {
+    __shared__ float buf[2 * (kBrdfWarps - 1) * kBrdfSteps * 2 * 32];
+    const uint32_t n = out.width * out.height;
+    const uint32_t i = min(blockIdx.x * 32 + (threadIdx.x & 31), n - 1);
     const uint32_t x = i % out.width, y = i / out.width;
     const float NoV = ((float)x + 0.5f) * (1.0f / (float)out.width), roughness = ((float)y + 0.5f) * (1.0f / (float)out.height);
     const F3 N = { 0.0f, 0.0f, 1.0f };
     const F3 V = { __fsqrt_rn(1.0f - NoV * NoV), 0.0f, NoV };
     F3 tx, ty;
     tangent_frame(N, tx, ty);
-    float rx = 0.0f, ry = 0.0f;
     const uint32_t sampleCount = 1024;
-    for (uint32_t s = 0; s < sampleCount; s++) {
+    float acc[2];
+    ordered_block_sum<kBrdfWarps, kBrdfSteps, 2>(sampleCount, [&](uint32_t s, float (&t)[2]) {
         const F3 H = importance_sample_ggx(tb.ham[3 * s], tb.ham[3 * s + 1], tb.ham[3 * s + 2], roughness, N, tx, ty);
         const float VdH = dot3(V, H);
         const F3 L = { 2.0f * VdH * H.x - V.x, 2.0f * VdH * H.y - V.y, 2.0f * VdH * H.z - V.z };
         const float VoH = vmax(0.0f, VdH), NoL = vmax(0.0f, L.z), NoH = vmax(0.0f, H.z);
+        t[0] = 0.0f, t[1] = 0.0f;
         if (NoL > 0.0f) {
             // V_SmithGGXCorrelatedFast (Shading.cpp:24-28) with roughness^2
             const float r2 = roughness * roughness;
@@ -217,12 +262,12 @@ __global__ void k_ibl_env_brdf(DevTexture out, uint32_t* outData, IblTables tb) 
             const float Gv = G * 4.0f * VoH * NoL / NoH;
             const float om = 1.0f - VoH;
             const float Fc = (om * om) * (om * om) * om;  // pow5
-            rx += Gv * (1.0f - Fc);
-            ry += Gv * Fc;
+            t[0] = Gv * (1.0f - Fc), t[1] = Gv * Fc;
         }
-    }
-    const uint32_t hx = __half_as_ushort(__float2half_rn(rx * (1.0f / sampleCount)));
-    const uint32_t hy = __half_as_ushort(__float2half_rn(ry * (1.0f / sampleCount)));
+    }, acc, buf);
+    if (threadIdx.x >= 32 || blockIdx.x * 32 + threadIdx.x >= n) return;
+    const uint32_t hx = __half_as_ushort(__float2half_rn(acc[0] * (1.0f / sampleCount)));
+    const uint32_t hy = __half_as_ushort(__float2half_rn(acc[1] * (1.0f / sampleCount)));
     outData[out.mip_offsets[0] + texel_offset((int32_t)x, (int32_t)y, (int32_t)out.row_shift)] = hx | (hy << 16);
 }
 
@@ -313,7 +358,7 @@ swr_status swr_ibl_irradiance_map(swr_texture env, swr_texture out) {
     const uint32_t n = out->d.width * out->d.height;
     {
         LaunchScope ls("k_ibl_irradiance", st);
-        k_ibl_irradiance<<<(n + 63) / 64, 64, 0, st>>>(env->d, out->d, (uint32_t*)out->d.data, tb);
+        k_ibl_irradiance<<<(n + 31) / 32, kIrrWarps * 32, 0, st>>>(env->d, out->d, (uint32_t*)out->d.data, tb);
     }
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(dcp, st), cudaFreeAsync(dsp, st), cudaFreeAsync(dct, st), cudaFreeAsync(dst, st);
@@ -353,7 +398,7 @@ swr_status swr_ibl_env_brdf_lut(swr_texture out) {
     const uint32_t n = out->d.width * out->d.height;
     {
         LaunchScope ls("k_ibl_env_brdf", st);
-        k_ibl_env_brdf<<<(n + 127) / 128, 128, 0, st>>>(out->d, (uint32_t*)out->d.data, tb);
+        k_ibl_env_brdf<<<(n + 31) / 32, kBrdfWarps * 32, 0, st>>>(out->d, (uint32_t*)out->d.data, tb);
     }
     cudaError_t e = cudaGetLastError();
     cudaFreeAsync(dh, st);

@@ -194,7 +194,7 @@ void launch_fill(uint32_t* dst, uint32_t n, uint32_t value, cudaStream_t st);
 void launch_finalize(const unsigned long long* keys, uint32_t* layer0, uint32_t* layer1, uint32_t n, cudaStream_t st);
 void launch_finalize_overdraw(const unsigned long long* keys, const unsigned long long* counts, uint32_t* layer0,
                               uint32_t* layer1, uint32_t n, cudaStream_t st);
-void launch_detile(const uint32_t* src, uint32_t* dst, uint32_t width, uint32_t height, cudaStream_t st);
+void launch_detile(const uint32_t* src, uint32_t* dst, uint32_t width, uint32_t height, uint32_t stride, cudaStream_t st);
 
 }  // namespace swr
 

@@ -1245,11 +1245,12 @@ __global__ void k_finalize_overdraw(const unsigned long long* __restrict__ keys,
 }
 
 // Framebuffer::GetPixels de-tiling (ImageHelpers.cpp:109-147) into a row-major device buffer.
-__global__ void k_detile(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, uint32_t width, uint32_t height) {
+__global__ void k_detile(const uint32_t* __restrict__ src, uint32_t* __restrict__ dst, uint32_t width, uint32_t height,
+                         uint32_t stride) {
     const uint32_t n = width * height;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
         const uint32_t y = i / width, x = i - y * width;
-        dst[i] = src[pixel_offset(x, y, width)];
+        dst[(size_t)y * stride + x] = src[pixel_offset(x, y, width)];
     }
 }
 
@@ -1363,9 +1364,9 @@ void launch_finalize_overdraw(const unsigned long long* keys, const unsigned lon
     k_finalize_overdraw<<<grid_for(n, 1, 256), 256, 0, st>>>(keys, counts, l0, l1, n);
 }
 
-void launch_detile(const uint32_t* src, uint32_t* dst, uint32_t width, uint32_t height, cudaStream_t st) {
+void launch_detile(const uint32_t* src, uint32_t* dst, uint32_t width, uint32_t height, uint32_t stride, cudaStream_t st) {
     LaunchScope ls("k_detile", st);
-    k_detile<<<grid_for(width * height, 1, 256), 256, 0, st>>>(src, dst, width, height);
+    k_detile<<<grid_for(width * height, 1, 256), 256, 0, st>>>(src, dst, width, height, stride);
 }
 
 }  // namespace swr

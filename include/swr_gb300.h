@@ -275,7 +275,8 @@ swr_status swr_framebuffer_create(uint32_t width, uint32_t height, uint32_t num_
 swr_status swr_framebuffer_destroy(swr_framebuffer fb);
 swr_status swr_framebuffer_clear(swr_framebuffer fb, uint32_t color, float depth);       /* Clear */
 swr_status swr_framebuffer_clear_layer(swr_framebuffer fb, uint32_t layer, uint32_t value); /* ClearLayer */
-/* GetPixels(layer, dest, stride): de-tiles a layer into host memory (stride in pixels). */
+/* GetPixels(layer, dest, stride): de-tiles a layer into host memory (stride in pixels). Pinned
+ * (page-locked) destinations are written by the de-tiling kernel directly over the host link. */
 swr_status swr_framebuffer_get_pixels(swr_framebuffer fb, uint32_t layer, uint32_t* dest, uint32_t stride);
 /* Device copy of a de-tiled layer (row-major, width*height words); no host synchronisation. */
 swr_status swr_framebuffer_get_pixels_device(swr_framebuffer fb, uint32_t layer, uint32_t* dest_device);

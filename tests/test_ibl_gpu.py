@@ -37,6 +37,20 @@ def test_irradiance_map_bit_exact(env):
     assert len(np.unique(exp)) > 100
 
 
+@pytest.mark.parametrize("w,h", [(8, 4), (16, 8)])
+def test_small_irradiance_maps_bit_exact(env, w, h):
+    """The smallest map (8x4: one block of 32 texels) and a non-square one, every texel."""
+    from glimpsw_gb300 import api
+    from oracle import oracle as O
+    out = api.Texture2D(api.FORMAT_R11G11B10F, w, h, 1, 1)
+    api._check(api._lib.swr_ibl_irradiance_map(env.g.h, out.h))
+    data = out.get_data()
+    rs = int(np.log2(w))
+    got = np.array([[data[_tiled(x, y, rs)] for x in range(w)] for y in range(h)], np.uint32)
+    exp = np.array([[O.ibl_irradiance_texel(env.o, x, y, w, h) for x in range(w)] for y in range(h)], np.uint32)
+    assert np.array_equal(got, exp), f"{(got != exp).sum()} of {w * h} texels differ"
+
+
 def test_radiance_map_bit_exact(env):
     from glimpsw_gb300 import api
     from oracle import oracle as O

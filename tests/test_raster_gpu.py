@@ -137,6 +137,28 @@ def test_clear_values_and_layers(grid):
         assert_visbuffer_equal(gfb, ofb)
 
 
+def test_get_pixels_into_pinned_memory(grid):
+    """GetPixels into page-locked memory (written by the de-tiling kernel over the host link) with a
+    row stride wider than the frame: the same words as the staged copy into pageable memory, and
+    the padding words between rows untouched."""
+    import ctypes as C
+
+    import torch
+
+    from glimpsw_gb300 import api
+    sc, g = grid
+    v = sc.views[0]
+    gfb, _ = g.render(v.world_to_clip, v.width, v.height)
+    stride = v.width + 12
+    for layer in (0, 1):
+        ref = gfb.get_pixels(layer)
+        pinned = torch.full((v.height, stride), -1, dtype=torch.int32).pin_memory()
+        api._check(api._lib.swr_framebuffer_get_pixels(gfb.h, layer, C.c_void_p(pinned.data_ptr()), stride))
+        got = pinned.numpy().view(np.uint32)
+        assert np.array_equal(got[:, :v.width], ref)
+        assert np.all(got[:, v.width:] == 0xFFFFFFFF)
+
+
 @pytest.mark.parametrize("capacity", [1, 64])
 def test_full_queue_gives_the_same_image(inside, capacity):
     """With a tiny large-triangle queue the mesh stage rasterizes the overflow itself (and clipped
