@@ -46,29 +46,46 @@ __global__ void k_clear_views(const BatchView* __restrict__ views, uint32_t colo
 }
 
 // CullMeshlets without a depth map (Shading.cpp:797-809, 865): frustum planes 0..4 and, when enabled,
-// the backface-cone test (cone_culled), one meshlet per thread, the view in blockIdx.y; a warp's
-// ballot gives two 16-bit masks.
-__global__ void k_cull_views(const BatchView* __restrict__ views, const uint8_t* __restrict__ meshlets, uint32_t first,
-                             uint32_t count, const DevMaterial* __restrict__ materials, uint32_t numMaterials) {
-    const BatchView& v = views[blockIdx.y];
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    bool visible = i < count;
-    if (visible) {
-        const uint8_t* rec = meshlets + (size_t)(first + i) * kMeshletSize;
-        const float4 s = *(const float4*)rec;
-        if (v.frustum) {
-            for (int k = 0; k < 5; k++) {
-                float dist = fadd(ffma(s.x, v.planes[k][0], ffma(s.y, v.planes[k][1], fmul(s.z, v.planes[k][2]))), v.planes[k][3]);
-                visible = visible && (dist > -s.w);
-            }
-        }
-        if (v.cone && visible) visible = !cone_culled(rec, v.eye[0], v.eye[1], v.eye[2], materials, numMaterials);
-    }
-    const unsigned m = __ballot_sync(0xFFFFFFFFu, visible);
+// the backface-cone test (cone_culled). One meshlet per thread for every view: its bounding sphere
+// is loaded once and tested against each view's planes, kept in shared memory kCullViews views at
+// a time; a warp's ballot gives the view's two 16-bit masks, which the lane numbered after the
+// view stores.
+constexpr uint32_t kCullViews = 32;
+
+__global__ void __launch_bounds__(256) k_cull_views(const BatchView* __restrict__ views, uint32_t numViews,
+                                                    const uint8_t* __restrict__ meshlets, uint32_t first, uint32_t count,
+                                                    const DevMaterial* __restrict__ materials, uint32_t numMaterials) {
+    __shared__ BatchView sv[kCullViews];
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31;
+    const bool valid = i < count;
+    const uint8_t* rec = meshlets + (size_t)(first + (valid ? i : 0)) * kMeshletSize;
+    const float4 s = valid ? *(const float4*)rec : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
     const uint32_t w0 = i & ~31u;
-    if ((threadIdx.x & 31) == 0 && w0 < count) {
-        v.bitmap[w0 / 16] = (uint16_t)(m & 0xFFFF);
-        if (w0 + 16 < count) v.bitmap[w0 / 16 + 1] = (uint16_t)(m >> 16);
+    for (uint32_t v0 = 0; v0 < numViews; v0 += kCullViews) {
+        const uint32_t nv = min(kCullViews, numViews - v0);
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < nv * (uint32_t)(sizeof(BatchView) / 4); k += blockDim.x)
+            ((uint32_t*)sv)[k] = ((const uint32_t*)(views + v0))[k];
+        __syncthreads();
+        unsigned mine = 0;  // the masks of view v0 + lane
+        for (uint32_t j = 0; j < nv; j++) {
+            const BatchView& v = sv[j];
+            bool visible = valid;
+            if (visible && v.frustum) {
+                for (int k = 0; k < 5; k++) {
+                    float dist = fadd(ffma(s.x, v.planes[k][0], ffma(s.y, v.planes[k][1], fmul(s.z, v.planes[k][2]))), v.planes[k][3]);
+                    visible = visible && (dist > -s.w);
+                }
+            }
+            if (v.cone && visible) visible = !cone_culled(rec, v.eye[0], v.eye[1], v.eye[2], materials, numMaterials);
+            const unsigned m = __ballot_sync(0xFFFFFFFFu, visible);
+            if (lane == j) mine = m;
+        }
+        if (lane < nv && w0 < count) {
+            uint16_t* bm = sv[lane].bitmap;
+            bm[w0 / 16] = (uint16_t)(mine & 0xFFFF);
+            if (w0 + 16 < count) bm[w0 / 16 + 1] = (uint16_t)(mine >> 16);
+        }
     }
 }
 
@@ -161,19 +178,35 @@ swr_status capture(swr_batch b) {
         b->scratch.alphaCapacity = std::max(items, 1u);
     }
     b->sceneVersion = b->scene->version;
-    cudaStream_t cs;
+    // The clear (bound by HBM writes) and the cull (by the records' sphere loads) are independent:
+    // they run as two branches of the graph, joined before the mesh stage.
+    cudaStream_t cs = nullptr, cs2 = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_batch: stream");
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&cs2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&fork, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&join, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        if (cs) cudaStreamDestroy(cs);
+        if (cs2) cudaStreamDestroy(cs2);
+        if (fork) cudaEventDestroy(fork);
+        return swr_internal_cuda_fail(e, "swr_batch: capture streams");
+    }
     const bool prof = swr_internal_set_profiling(false);
     e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    const bool began = e == cudaSuccess;
+    if (e == cudaSuccess) e = cudaEventRecord(fork, cs);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(cs2, fork, 0);
     if (e == cudaSuccess) {
         const uint32_t nv = b->numViews;
         const int blocksX = (int)std::min<uint32_t>((b->maxPixels + 255) / 256, 1024u);
-        k_clear_views<<<dim3(blocksX, nv), 256, 0, cs>>>(b->dBatch, 0xFF000000u, 0u);
+        k_clear_views<<<dim3(blocksX, nv), 256, 0, cs2>>>(b->dBatch, 0xFF000000u, 0u);
+        e = cudaEventRecord(join, cs2);
         if (b->cullFlags && b->count)
-            k_cull_views<<<dim3((b->count + 255) / 256, nv), 256, 0, cs>>>(b->dBatch, b->scene->meshlets, b->first, b->count,
-                                                                          b->scene->materials, b->scene->num_materials);
+            k_cull_views<<<(b->count + 255) / 256, 256, 0, cs>>>(b->dBatch, nv, b->scene->meshlets, b->first, b->count,
+                                                                b->scene->materials, b->scene->num_materials);
         cudaMemsetAsync(b->scratch.control, 0, 3 * sizeof(unsigned long long), cs);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, join, 0);
         DrawArgs a = {};
         a.meshlets = b->scene->meshlets;
         a.materials = b->scene->materials;
@@ -189,7 +222,13 @@ swr_status capture(swr_batch b) {
         a.chunkTilesY = b->chunkTilesY;
         a.warpsPerBlock = b->warpsPerBlock;
         launch_draw(a, cs, sm_count());
-        e = cudaStreamEndCapture(cs, &b->graph);
+    }
+    if (began) {  // a failed step still ends the capture before the streams go
+        cudaGraph_t g = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(cs, &g);
+        if (e == cudaSuccess) e = ec;
+        if (e == cudaSuccess) b->graph = g;
+        else if (g) cudaGraphDestroy(g);
     }
     swr_internal_set_profiling(prof);
     if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
@@ -205,6 +244,9 @@ swr_status capture(swr_batch b) {
         }
     }
     cudaStreamDestroy(cs);
+    cudaStreamDestroy(cs2);
+    cudaEventDestroy(fork);
+    cudaEventDestroy(join);
     if (e != cudaSuccess) return swr_internal_cuda_fail(e, "swr_batch: graph capture");
     return SWR_OK;
 }
