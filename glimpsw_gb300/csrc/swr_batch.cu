@@ -24,7 +24,7 @@ struct BatchView {              // device table for the batched clear and cull k
     uint32_t* layer0;
     uint32_t* layer1;
     unsigned long long* keys;
-    uint16_t* bitmap;
+    uint32_t* groupMasks;       // one word per 32 draw positions (ViewParams::groupMasks)
     uint32_t pixels;            // width * height
     uint32_t* tileMin;          // per 4x4 tile depth bound
     uint32_t frustum, cone;     // tests of the batched cull: frustum planes, backface cone
@@ -46,28 +46,30 @@ __global__ void k_clear_views(const BatchView* __restrict__ views, uint32_t colo
 }
 
 // CullMeshlets without a depth map (Shading.cpp:797-809, 865): frustum planes 0..4 and, when enabled,
-// the backface-cone test (cone_culled). One meshlet per thread for every view: its bounding sphere
-// is loaded once and tested against each view's planes, kept in shared memory kCullViews views at
-// a time; a warp's ballot gives the view's two 16-bit masks, which the lane numbered after the
-// view stores.
+// the backface-cone test (cone_culled). One draw position per thread for every view (all views of
+// a batch draw the same meshlets in the same order): its meshlet's bounding sphere is loaded once
+// and tested against each view's planes, kept in shared memory kCullViews views at a time. A warp's
+// ballot is the view's mask of 32 consecutive positions, stored by the lane numbered after the view,
+// so the mesh stage tests a fetched group with one word.
 constexpr uint32_t kCullViews = 32;
 
 __global__ void __launch_bounds__(256) k_cull_views(const BatchView* __restrict__ views, uint32_t numViews,
                                                     const uint8_t* __restrict__ meshlets, uint32_t first, uint32_t count,
-                                                    const DevMaterial* __restrict__ materials, uint32_t numMaterials) {
+                                                    uint32_t orderStride, const DevMaterial* __restrict__ materials,
+                                                    uint32_t numMaterials) {
     __shared__ BatchView sv[kCullViews];
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31;
-    const bool valid = i < count;
-    const uint8_t* rec = meshlets + (size_t)(first + (valid ? i : 0)) * kMeshletSize;
+    const uint32_t q = blockIdx.x * blockDim.x + threadIdx.x, lane = threadIdx.x & 31;
+    const bool valid = q < count;
+    const uint8_t* rec = meshlets + (size_t)(first + (valid ? draw_order(q, count, orderStride) : 0u)) * kMeshletSize;
     const float4 s = valid ? *(const float4*)rec : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-    const uint32_t w0 = i & ~31u;
+    const uint32_t group = q / 32;
     for (uint32_t v0 = 0; v0 < numViews; v0 += kCullViews) {
         const uint32_t nv = min(kCullViews, numViews - v0);
         __syncthreads();
         for (uint32_t k = threadIdx.x; k < nv * (uint32_t)(sizeof(BatchView) / 4); k += blockDim.x)
             ((uint32_t*)sv)[k] = ((const uint32_t*)(views + v0))[k];
         __syncthreads();
-        unsigned mine = 0;  // the masks of view v0 + lane
+        unsigned mine = 0;  // the mask of view v0 + lane
         for (uint32_t j = 0; j < nv; j++) {
             const BatchView& v = sv[j];
             bool visible = valid;
@@ -81,11 +83,7 @@ __global__ void __launch_bounds__(256) k_cull_views(const BatchView* __restrict_
             const unsigned m = __ballot_sync(0xFFFFFFFFu, visible);
             if (lane == j) mine = m;
         }
-        if (lane < nv && w0 < count) {
-            uint16_t* bm = sv[lane].bitmap;
-            bm[w0 / 16] = (uint16_t)(mine & 0xFFFF);
-            if (w0 + 16 < count) bm[w0 / 16 + 1] = (uint16_t)(mine >> 16);
-        }
+        if (lane < nv && group * 32 < count) sv[lane].groupMasks[group] = mine;
     }
 }
 
@@ -105,7 +103,7 @@ struct swr_batch_t {
     ViewParams* dViews = nullptr;
     BatchView* dBatch = nullptr;
     uint32_t* dViewStart = nullptr;
-    uint16_t* dBitmaps = nullptr;
+    uint32_t* dGroupMasks = nullptr;  // per view: the cull's masks of 32 draw positions
     DrawScratch scratch = {};
     uint32_t chunkTiles = 0, chunkTilesY = 0, warpsPerBlock = 0;
     cudaGraph_t graph = nullptr;
@@ -121,7 +119,7 @@ int sm_count() { return swr_internal_sm_count(); }
 swr_status upload_views(swr_batch b, const swr_view_desc* views) {
     std::vector<ViewParams> vp(b->numViews);
     std::vector<BatchView> bv(b->numViews);
-    const uint32_t words = (b->count + 15) / 16;
+    const uint32_t words = (b->count + 31) / 32;  // group masks per view
     for (uint32_t i = 0; i < b->numViews; i++) {
         const swr_view_desc& d = views[i];
         swr_framebuffer fb = b->fbs[i];
@@ -143,7 +141,7 @@ swr_status upload_views(swr_batch b, const swr_view_desc* views) {
         v.orderStride = order_stride(b->count);
         v.keys = fb->keys;
         v.tileMin = fb->tileMin;
-        v.cullBitmap = b->cullFlags ? b->dBitmaps + (size_t)i * words : nullptr;
+        v.groupMasks = b->cullFlags ? b->dGroupMasks + (size_t)i * words : nullptr;
         BatchView& w = bv[i];
         memset(&w, 0, sizeof(w));
         memcpy(w.planes, planes, sizeof(w.planes));
@@ -151,7 +149,7 @@ swr_status upload_views(swr_batch b, const swr_view_desc* views) {
         w.layer1 = fb->layers + fb->layer_stride;
         w.keys = fb->keys;
         w.tileMin = fb->tileMin;
-        w.bitmap = b->dBitmaps + (size_t)i * words;
+        w.groupMasks = b->dGroupMasks + (size_t)i * words;
         w.pixels = fb->width * fb->height;
         w.frustum = (b->cullFlags & SWR_CULL_FRUSTUM) ? 1u : 0u;
         w.cone = ((b->cullFlags & SWR_CULL_BACKFACE_CONE) && swr_hostmath::cone_camera(objToClip, w.eye)) ? 1u : 0u;
@@ -204,7 +202,8 @@ swr_status capture(swr_batch b) {
         e = cudaEventRecord(join, cs2);
         if (b->cullFlags && b->count)
             k_cull_views<<<(b->count + 255) / 256, 256, 0, cs>>>(b->dBatch, nv, b->scene->meshlets, b->first, b->count,
-                                                                b->scene->materials, b->scene->num_materials);
+                                                                order_stride(b->count), b->scene->materials,
+                                                                b->scene->num_materials);
         cudaMemsetAsync(b->scratch.control, 0, 3 * sizeof(unsigned long long), cs);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(cs, join, 0);
         DrawArgs a = {};
@@ -280,13 +279,13 @@ swr_status swr_batch_create(swr_rasterizer r, swr_scene s, uint32_t first, uint3
         b->maxPixels = std::max(b->maxPixels, views[i].fb->width * views[i].fb->height);
         totalTris += (uint64_t)count * 32;
     }
-    const uint32_t words = (count + 15) / 16;
+    const uint32_t words = (count + 31) / 32;
     std::vector<uint32_t> start(num_views + 1);
     for (uint32_t i = 0; i <= num_views; i++) start[i] = i * (uint32_t)padded;
     cudaError_t e = cudaMalloc(&b->dViews, num_views * sizeof(ViewParams));
     if (e == cudaSuccess) e = cudaMalloc(&b->dBatch, num_views * sizeof(BatchView));
     if (e == cudaSuccess) e = cudaMalloc(&b->dViewStart, (num_views + 1) * sizeof(uint32_t));
-    if (e == cudaSuccess) e = cudaMalloc(&b->dBitmaps, (size_t)num_views * words * sizeof(uint16_t) + 16);
+    if (e == cudaSuccess) e = cudaMalloc(&b->dGroupMasks, (size_t)num_views * words * sizeof(uint32_t) + 16);
     if (e == cudaSuccess) e = cudaMemcpy(b->dViewStart, start.data(), start.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
     // the batch's own queue: a quarter of the triangles of every view; overflow is rasterized in place
     b->scratch.bigCapacity = (uint32_t)std::min<uint64_t>(std::max<uint64_t>(totalTris, 1u << 18), 1u << 26);
@@ -381,7 +380,7 @@ swr_status swr_batch_destroy(swr_batch b) {
     cudaFree(b->dViews);
     cudaFree(b->dBatch);
     cudaFree(b->dViewStart);
-    cudaFree(b->dBitmaps);
+    cudaFree(b->dGroupMasks);
     cudaFree(b->scratch.control);
     cudaFree(b->scratch.big);
     cudaFree(b->scratch.bigBase);

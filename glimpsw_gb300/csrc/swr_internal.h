@@ -124,7 +124,8 @@ struct ViewParams {
     float bx, by;
     uint32_t meshletOffset, count;
     unsigned long long* keys;
-    const uint16_t* cullBitmap;
+    const uint32_t* groupMasks;  // batched views: bit l of word g is the cull result of draw position
+                                 // 32 g + l (nullptr: every meshlet visible)
     uint32_t* tileMin;      // per 4x4 tile: lower bound of its keys' depth words (nullptr: no tile culling)
     uint32_t orderStride;   // draw order: position p draws meshlet (p * orderStride) mod count (order_stride)
     uint32_t pad;
@@ -185,6 +186,10 @@ constexpr uint32_t kShadedSize = 1472, kShadedIndices = 64, kShadedPositions = 4
 // the group to the share of visible meshlets, and the alpha pass takes kDrawGroup list entries.
 constexpr uint32_t kDrawGroup = 4, kBatchGroup = 32;
 uint32_t order_stride(uint32_t count);
+// Meshlet drawn at position p of a view of count meshlets (order_stride).
+__device__ __forceinline__ uint32_t draw_order(uint32_t p, uint32_t count, uint32_t stride) {
+    return (uint32_t)(((unsigned long long)p * stride) % count);
+}
 
 void launch_draw(const DrawArgs& a, cudaStream_t st, int numSMs);
 void launch_init_keys(const uint32_t* depthLayer, unsigned long long* keys, uint32_t* tileMin, uint32_t n, cudaStream_t st);

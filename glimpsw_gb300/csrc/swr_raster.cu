@@ -725,11 +725,6 @@ __device__ __forceinline__ uint32_t view_of(const uint32_t* viewStart, uint32_t 
     return lo;
 }
 
-// Meshlet drawn at position p of a view of count meshlets (order_stride).
-__device__ __forceinline__ uint32_t draw_order(uint32_t p, uint32_t count, uint32_t stride) {
-    return (uint32_t)(((unsigned long long)p * stride) % count);
-}
-
 enum : int { kPassOpaque = 0, kPassAlpha = 1, kPassOverdraw = 2 };
 // kShaded: the meshlets come shaded by a user mesh shader (a.shaded, swr_shaded_meshlet records):
 // clip positions, indices, PrimCount, CullMode and FragmentShaderId are read from the record
@@ -761,7 +756,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
             for (int k = 0; k < 16; k++) v.m[k] = a.m[k];
             v.halfW = a.halfW, v.halfH = a.halfH, v.width = a.width, v.height = a.height;
             v.bx = a.bx, v.by = a.by, v.meshletOffset = a.meshletOffset, v.count = a.count;
-            v.keys = a.keys, v.cullBitmap = a.cullBitmap, v.tileMin = a.tileMin;
+            v.keys = a.keys, v.tileMin = a.tileMin;
             S.view = v;
         }
         curView = 0;
@@ -808,15 +803,13 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                     const uint32_t G = base / kBatchGroup;
                     fetchView = G % a.numViews;
                     const ViewParams& fv = a.views[fetchView];
-                    const uint32_t q = (G / a.numViews) * kBatchGroup + lane;
-                    bool vis = false;
-                    if (q < fv.count) {
-                        laneMeshlet = draw_order(q, fv.count, fv.orderStride);
-                        const uint16_t* bm = fv.cullBitmap;
-                        vis = bm == nullptr || ((bm[laneMeshlet >> 4] >> (laneMeshlet & 15)) & 1);
-                    }
-                    fetchMask = __ballot_sync(0xFFFFFFFFu, vis);
+                    // the cull wrote the group's 32 results as one word, in draw order
+                    const uint32_t g = G / a.numViews, q = g * kBatchGroup + lane;
+                    const uint32_t n = fv.count - g * kBatchGroup;  // positions of the group in the view (> 0)
+                    const unsigned inView = n >= 32 ? 0xFFFFFFFFu : (1u << n) - 1u;
+                    fetchMask = (fv.groupMasks ? fv.groupMasks[g] : 0xFFFFFFFFu) & inView;
                     if (fetchMask == 0) continue;
+                    laneMeshlet = q < fv.count ? draw_order(q, fv.count, fv.orderStride) : 0u;
                 }
                 view = fetchView;
                 m = __shfl_sync(0xFFFFFFFFu, laneMeshlet, __ffs(fetchMask) - 1);
