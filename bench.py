@@ -4,9 +4,9 @@
 Workload (the headline configuration): 100k meshlets of 64 vertices / 124 triangles (12.4M
 triangles), seeded, scattered in a 200^3 volume with log-uniform scale 0.1-10, 64 materials of two
 2048^2 RGBA8 layers with full mips, an octahedral 1024^2 R11G11B10 sky, 1920x1080. One step is one
-frame of the reference's frame driver (Main.cpp:171-261): clear, per 65536-meshlet batch
-CullMeshlets then DrawMeshlets (unbinned semantics, clipping on), Resolve, and DownsampleDepth for
-the next frame. The headline frame has no previous depth (frustum culling only, every triangle
+frame of the reference's frame driver (Main.cpp:171-261): clear, CullMeshlets then DrawMeshlets
+for the node's meshlets (unbinned semantics, clipping on), Resolve, and DownsampleDepth for the
+next frame. The headline frame has no previous depth (frustum culling only, every triangle
 of the visible meshlets is set up); `hiz_frame` reports the following frame, whose perturbed
 camera is culled against that Hi-Z (in this dense scene the occlusion test removes almost all
 meshlets).
@@ -18,8 +18,10 @@ inside the timed region. Host-to-device copies run at about 210 GB/s on the GB30
 (0.82 ms for the 172.8 MB scene), so the end-to-end frame draws in batches of 12,000, 44,000 and
 44,000 meshlets whose uploads go up on a copy stream while the batches before them draw: only the
 first batch's 20.7 MB upload is not overlapped. The image goes back while the Hi-Z pyramid builds,
-written straight into the pinned host buffer by the de-tiling kernel. The device-timed frame keeps the frame driver's
-65,536-meshlet batches; both give the same image (checked). `--impl reference` times the reference's CPU algorithm (the oracle
+written straight into the pinned host buffer by the de-tiling kernel. The device-timed frame draws
+the node in one call (`--frame-batch`); the reference's frame driver draws it in 65,536-meshlet
+batches because its cull bitmap is a stack array of that size (Main.cpp:221-222), and the same
+frame drawn that way is reported beside it (`frame_driver_batches`). All give the same image (checked). `--impl reference` times the reference's CPU algorithm (the oracle
 restatement; the reference itself cannot be compiled here) on the host cores.
 """
 from __future__ import annotations
@@ -40,7 +42,16 @@ sys.path.insert(0, ROOT)
 
 METRIC = "1080p frame time (100k meshlets, 12.4M triangles: cull, draw, resolve, Hi-Z)"
 UNIT = "ms/frame"
-BATCH = 65536  # Main.cpp:222
+BATCH = 65536  # Main.cpp:222: the reference draws a node in batches of its stack cull bitmap's size
+
+
+def gpu_batches(n: int, batch: int) -> list[tuple[int, int]]:
+    """The GPU frames' draw calls: the whole node in one call (batch 0), or batches of `batch`
+    meshlets. The reference's 65,536-meshlet batches come from its stack-allocated cull bitmap
+    (Main.cpp:221-222); the device bitmap has no such limit, and every extra draw call costs the
+    mesh and chunk stages' tails (keys are order-independent, so the image is the same)."""
+    step = batch or n
+    return [(off, min(step, n - off)) for off in range(0, n, step)]
 
 
 MESHLET_BYTES = 1728  # one Meshlet record (Scene.h:15-30)
@@ -72,6 +83,9 @@ def parse():
     p.add_argument("--neural-height", type=int, default=1440)
     p.add_argument("--no-alpha", action="store_true")
     p.add_argument("--no-cone", action="store_true")
+    p.add_argument("--frame-batch", type=int, default=0,
+                   help="meshlets per draw call of the GPU frames (0: the whole node in one call; the frame is "
+                        "also timed with the reference frame driver's 65,536)")
     p.add_argument("--e2e-batches", default="12000,44000",
                    help="meshlets per draw batch of the end-to-end frame, comma-separated; the last size repeats "
                         "until the scene is covered (each batch's upload overlaps the draws before it)")
@@ -338,10 +352,10 @@ def peaks():
 
 
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of the frame's kernels, from
-# one ncu capture of the default workload (100k meshlets, 1920x1080; the capture used 256^2
-# textures, which changes only the resolve's texel addresses), averaged over the frame's launches:
-# k_draw_meshlets 86.73 MB and 35.01 MB for the two batches, k_raster_big 41.93 MB and 22.11 MB.
-NCU_DRAM_BYTES_PER_LAUNCH = {"k_draw_meshlets": 60.87e6, "k_raster_big": 32.02e6, "k_resolve": 27.26e6}
+# one ncu capture of the default workload drawn in one call (100k meshlets, 1920x1080; the capture
+# used 256^2 textures, which changes only the resolve's texel addresses): k_draw_meshlets 108.83 MB
+# read + 22.18 MB written, k_raster_big 52.39 + 0.42 MB, k_resolve 27.26 MB.
+NCU_DRAM_BYTES_PER_LAUNCH = {"k_draw_meshlets": 131.01e6, "k_raster_big": 52.81e6, "k_resolve": 27.26e6}
 NCU_WORKLOAD = (100_000, 1920, 1080)
 
 
@@ -534,7 +548,7 @@ def alpha_section(args, api, stream, sc, texs, env, lights, flush):
     W, H = v0.width, v0.height
     fb = api.Framebuffer(W, H, 3)
     n = len(sca.meshlets)
-    batches = [(off, min(BATCH, n - off)) for off in range(0, n, BATCH)]
+    batches = gpu_batches(n, args.frame_batch)
     bitmaps = [torch.zeros((cnt + 15) // 16, dtype=torch.int16, device="cuda") for _, cnt in batches]
     hw, hh = api.hiz_texture_size(W, H)
     hiz = api.Texture2D(api.FORMAT_R32F, hw, hh, 16, 1)
@@ -562,7 +576,6 @@ def alpha_section(args, api, stream, sc, texs, env, lights, flush):
     rast.reset_counters()
     frame()
     c = rast.counters()
-    api.profile_enable(True)
     ms = []
     for _ in range(args.steps):
         flush.zero_()
@@ -572,6 +585,11 @@ def alpha_section(args, api, stream, sc, texs, env, lights, flush):
         b.record(stream)
         torch.cuda.synchronize()
         ms.append(a.elapsed_time(b))
+    api.profile_enable(True)  # per-kernel times from a second pass (events around every launch)
+    for _ in range(args.steps):
+        flush.zero_()
+        frame()
+    torch.cuda.synchronize()
     api.profile_enable(False)
     per = {}
     for name, t in api.profile_collect():
@@ -609,7 +627,7 @@ def cone_section(args, api, stream, texs, env, lights, flush):
     W, H = v0.width, v0.height
     fb = api.Framebuffer(W, H, 3)
     n = len(sc.meshlets)
-    batches = [(off, min(BATCH, n - off)) for off in range(0, n, BATCH)]
+    batches = gpu_batches(n, args.frame_batch)
     bitmaps = [torch.zeros((cnt + 15) // 16, dtype=torch.int16, device="cuda") for _, cnt in batches]
     hw, hh = api.hiz_texture_size(W, H)
     hiz = api.Texture2D(api.FORMAT_R32F, hw, hh, 16, 1)
@@ -727,7 +745,7 @@ def neural_section(args, api, stream, sc, texs, env, scene, rast, lights):
     texel = texel_accuracy(api, model, texs)
     W, H = args.neural_width, args.neural_height
     n = len(sc.meshlets)
-    batches = [(off, min(BATCH, n - off)) for off in range(0, n, BATCH)]
+    batches = gpu_batches(n, args.frame_batch)
     bms = [torch.zeros((cnt + 15) // 16, dtype=torch.int16, device="cuda") for _, cnt in batches]
     fbs = [api.Framebuffer(W, H, 3), api.Framebuffer(W, H, 3)]
     eye = sc.views[0].eye
@@ -830,7 +848,7 @@ def run_ours(args):
     rast.EnableBinning = False  # the reference frame driver's setting (Main.cpp:76)
     fb = api.Framebuffer(W, H, 3)
     n = len(sc.meshlets)
-    batches = [(off, min(BATCH, n - off)) for off in range(0, n, BATCH)]
+    batches = gpu_batches(n, args.frame_batch)
     bitmaps = [torch.zeros((cnt + 15) // 16, dtype=torch.int16, device="cuda") for _, cnt in batches]
     hw, hh = api.hiz_texture_size(W, H)
     hiz = [api.Texture2D(api.FORMAT_R32F, hw, hh, 16, 1) for _ in range(2)]
@@ -847,8 +865,8 @@ def run_ours(args):
 
     def frame_fn(view, prev, hiz_in, hiz_out, blist=None):
         """The frame driver's sequence (Main.cpp:203-260) for one camera, drawing the meshlets in
-        the batches blist (default: the frame driver's 65,536). Matrices and shading contexts are
-        parameter blocks, built once per camera as a renderer keeps them."""
+        the batches blist (default: gpu_batches). Matrices and shading contexts are parameter
+        blocks, built once per camera as a renderer keeps them."""
         blist = batches if blist is None else blist
         bms = bitmaps if blist is batches else [torch.zeros((cnt + 15) // 16, dtype=torch.int16, device="cuda")
                                                 for _, cnt in blist]
@@ -905,19 +923,29 @@ def run_ours(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     launches0 = api.launch_count()
-    api.profile_enable(True)
     with ClockSampler(local) as clocks:
         step_ms = timed(headline, args.steps)
-    api.profile_enable(False)
-    prof = api.profile_collect()
     launches = api.launch_count() - launches0
     ms = float(np.mean(step_ms))
+    # per-kernel times: a second pass of the same steps with an event pair around every launch
+    # (the events add a few microseconds per launch, so the frame time comes from the pass without)
     api.profile_enable(True)
+    prof_ms = float(np.mean(timed(headline, args.steps)))
+    api.profile_enable(False)
+    prof = api.profile_collect()
     hiz_ms = float(np.mean(timed(hiz_frame, args.steps)))
+    api.profile_enable(True)
+    timed(hiz_frame, args.steps)
     api.profile_enable(False)
     hiz_per = {}
     for name, t in api.profile_collect():
         hiz_per[name] = hiz_per.get(name, 0.0) + t / args.steps
+    # the same frame drawn as the reference frame driver calls it (Main.cpp:221-242)
+    ref_batches = [(off, min(BATCH, n - off)) for off in range(0, n, BATCH)]
+    ref_batch_frame = frame_fn(v0, v0, None, hiz[0], ref_batches)
+    for _ in range(2):
+        ref_batch_frame()
+    ref_batch_ms = float(np.mean(timed(ref_batch_frame, args.steps)))
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -1023,11 +1051,15 @@ def run_ours(args):
                 "gpix_per_s": W * H / (ms / 1e3) / 1e9,
                 "counters": {"triangles_processed": int(counters[0]), "triangles_rasterized": int(counters[1]),
                              "triangles_clipped": int(counters[2])},
+                "draw_calls": len(batches),
+                "frame_driver_batches": {"meshlets_per_draw": BATCH, "draw_calls": len(ref_batches),
+                                         "ms": ref_batch_ms},
                 "hiz_frame": {"ms": hiz_ms, "note": "next frame culled against this frame's Hi-Z (Main.cpp:229-232)",
                               "triangles_processed": int(hiz_counters[0]),
                               "triangles_rasterized": int(hiz_counters[1]),
                               "kernels_ms_per_step": dict(sorted(hiz_per.items()))},
                 "kernels_ms_per_step": {k: s / args.steps for k, (c, s) in sorted(per.items())},
+                "kernels_pass_ms_per_step": prof_ms,
                 "roofline": roofline,
                 "e2e": {"value": float(np.median(e2e_ms)), "unit": UNIT, "h2d_bytes_per_step": int(sc.meshlets.nbytes),
                         "d2h_bytes_per_step": int(W * H * 4), "draw_batches_meshlets": [c for _, c in eb]},
