@@ -15,9 +15,10 @@ Timing: CUDA events on the library's stream (torch's current stream), L2 flushed
 steps by a 256 MiB write outside the step's events. `e2e` runs the same frame through the public
 API with the scene uploaded from pinned host memory and the colour image read back to host memory
 inside the timed region. Host-to-device copies run at about 210 GB/s on the GB300's host link
-(0.82 ms for the 172.8 MB scene), so the end-to-end frame draws in batches of 12,000, 44,000 and
-44,000 meshlets whose uploads go up on a copy stream while the batches before them draw: only the
-first batch's 20.7 MB upload is not overlapped. The image goes back while the Hi-Z pyramid builds,
+(0.82 ms for the 172.8 MB scene), so the end-to-end frame draws in batches of 16,000, 24,000,
+30,000 and 30,000 meshlets whose uploads go up on a copy stream while the batches before them draw:
+only the first batch's 27.6 MB upload is not overlapped. Two rasterizers on two streams take the
+batches in turn, so one batch's chunk stage overlaps the next batch's mesh stage. The image goes back while the Hi-Z pyramid builds,
 written straight into the pinned host buffer by the de-tiling kernel. The device-timed frame draws
 the node in one call (`--frame-batch`); the reference's frame driver draws it in 65,536-meshlet
 batches because its cull bitmap is a stack array of that size (Main.cpp:221-222), and the same
@@ -86,7 +87,9 @@ def parse():
     p.add_argument("--frame-batch", type=int, default=0,
                    help="meshlets per draw call of the GPU frames (0: the whole node in one call; the frame is "
                         "also timed with the reference frame driver's 65,536)")
-    p.add_argument("--e2e-batches", default="12000,44000",
+    p.add_argument("--e2e-lanes", type=int, default=2,
+                   help="rasterizer/stream pairs that take the end-to-end frame's batches in turn")
+    p.add_argument("--e2e-batches", default="16000,24000,30000",
                    help="meshlets per draw batch of the end-to-end frame, comma-separated; the last size repeats "
                         "until the scene is covered (each batch's upload overlaps the draws before it)")
     p.add_argument("--multiview-cameras", type=int, default=58,
@@ -876,16 +879,31 @@ def run_ours(args):
         rctx = api.ShadingContext(scene, view.world_to_clip, world_to_clip=view.world_to_clip, skybox=env,
                                   view_pos=view.eye, lights=lights)
 
-        def run(uploaded=None, resolved=None):
+        def run(uploaded=None, resolved=None, lanes=None):
             """uploaded: per batch, an event after which its records are on the device, or None
             (their upload then overlaps the culling and drawing of the batches before). resolved:
-            an event recorded once the colour image is complete (before the Hi-Z build)."""
+            an event recorded once the colour image is complete (before the Hi-Z build). lanes:
+            (rasterizer, stream, event) triples that take the batches in turn, so that one batch's
+            chunk stage overlaps the next batch's mesh stage (keys are order-independent); the
+            first is the frame's own (rast, stream)."""
+            lanes = lanes or [(rast, stream, None)]
             fb.clear(0xFF000000, 0.0)
+            for r, s, ev in lanes[1:]:  # the other lanes start after the clear
+                ev.record(stream)
+                s.wait_event(ev)
             for k, ((off, cnt), bm, ctx) in enumerate(zip(blist, bms, ctxs)):
+                r, s, _ = lanes[k % len(lanes)]
+                if s is not stream:
+                    api.set_stream(s)
                 if uploaded is not None and uploaded[k] is not None:
-                    stream.wait_event(uploaded[k])
+                    s.wait_event(uploaded[k])
                 api.cull_meshlets(scene, off, cnt, bm, *mats, W, H, hiz_in)
-                rast.draw_meshlets(fb, cnt, ctx)
+                r.draw_meshlets(fb, cnt, ctx)
+                if s is not stream:
+                    api.set_stream(stream)
+            for r, s, ev in lanes[1:]:  # the resolve waits for every lane's draws
+                ev.record(s)
+                stream.wait_event(ev)
             rctx.resolve(rast, fb)
             if resolved is not None:
                 resolved.record(stream)
@@ -991,6 +1009,11 @@ def run_ours(args):
     e2e_frame = frame_fn(v0, v0, None, hiz[0], eb)
     copy_stream = torch.cuda.Stream()
     first_up, resolved = torch.cuda.Event(), torch.cuda.Event()
+    lanes = [(rast, stream, None)]
+    for _ in range(args.e2e_lanes - 1):
+        r2 = api.Rasterizer()
+        r2.EnableBinning = False
+        lanes.append((r2, torch.cuda.Stream(), torch.cuda.Event()))
     uploaded = [None] + [torch.cuda.Event() for _ in eb[1:]]
     headline()
     expected = fb.get_pixels(0)  # the image the overlapped upload must reproduce
@@ -1009,7 +1032,7 @@ def run_ours(args):
                                                           off, cnt))
             ev.record(copy_stream)
         api.set_stream(stream.cuda_stream)
-        e2e_frame(uploaded, resolved)
+        e2e_frame(uploaded, resolved, lanes)
         copy_stream.wait_event(resolved)
         api.set_stream(copy_stream.cuda_stream)
         api._check(api._lib.swr_framebuffer_get_pixels(fb.h, 0, C.c_void_p(host_img.data_ptr()), W))
@@ -1062,7 +1085,8 @@ def run_ours(args):
                 "kernels_pass_ms_per_step": prof_ms,
                 "roofline": roofline,
                 "e2e": {"value": float(np.median(e2e_ms)), "unit": UNIT, "h2d_bytes_per_step": int(sc.meshlets.nbytes),
-                        "d2h_bytes_per_step": int(W * H * 4), "draw_batches_meshlets": [c for _, c in eb]},
+                        "d2h_bytes_per_step": int(W * H * 4), "draw_batches_meshlets": [c for _, c in eb],
+                        "lanes": args.e2e_lanes},
                 "gpu_launches": int(launches), "clocks": clocks.summary(), "cpu_baseline": cpu,
                 "alpha": alpha, "cone": cone, "multiview": multiview, "neural": neural, "combined": combined}
         print(json.dumps(line), flush=True)

@@ -137,6 +137,43 @@ def test_clear_values_and_layers(grid):
         assert_visbuffer_equal(gfb, ofb)
 
 
+def test_two_rasterizers_on_two_streams(inside):
+    """Batches drawn in turn by two rasterizers on two streams into one framebuffer (one batch's
+    chunk stage overlaps the next batch's mesh stage, as the end-to-end frame does): the keys are
+    order-independent, so the vis-buffer equals one draw's, and the oracle's."""
+    import torch
+
+    from glimpsw_gb300 import api
+    sc, mats, g = inside
+    v = sc.views[0]
+    view = scenes.make_view(v.width, v.height, eye=(0.0, 0.0, 0.0), target=(0.3, 0.1, 1.0))
+    n = len(sc.meshlets)
+    other = api.Rasterizer()
+    other.EnableBinning = False
+    main, side = torch.cuda.Stream(), torch.cuda.Stream()
+    cleared, joined = torch.cuda.Event(), torch.cuda.Event()
+    g.rast.EnableBinning, g.rast.EnableClipping, g.rast.EnableGuardband = False, True, True
+    bounds = [0, 400, 1100, 2000, n]
+    try:
+        api.set_stream(main)
+        fb = api.Framebuffer(v.width, v.height)
+        fb.clear(0xFF000000, 0.0)
+        cleared.record(main)
+        side.wait_event(cleared)
+        for k in range(4):
+            rast, s = (g.rast, main) if k % 2 == 0 else (other, side)
+            api.set_stream(s)
+            ctx = api.ShadingContext(g.scene, view.world_to_clip, meshlet_offset=bounds[k])
+            rast.draw_meshlets(fb, bounds[k + 1] - bounds[k], ctx)
+        api.set_stream(main)
+        joined.record(side)
+        main.wait_event(joined)
+        ofb, _ = render_oracle(sc.meshlets, mats, view.world_to_clip, v.width, v.height, binning=False)
+        assert_visbuffer_equal(fb, ofb)
+    finally:
+        api.set_stream(0)  # the per-thread default stream again
+
+
 def test_get_pixels_into_pinned_memory(grid):
     """GetPixels into page-locked memory (written by the de-tiling kernel over the host link) with a
     row stride wider than the frame: the same words as the staged copy into pageable memory, and
