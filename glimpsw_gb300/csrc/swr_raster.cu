@@ -494,12 +494,18 @@ __device__ __forceinline__ void shade_live_tiles_alpha(Rec&& rec, Ext&& ext, uin
     }
 }
 
+// ceil(2^16 / n) for n = 1..16: t / n == (t * kDiv16[n]) >> 16 for every t < 256 (checked
+// exhaustively), the tile index division of a chunk of at most 16 x 16 tiles.
+__constant__ uint32_t kDiv16[17] = { 0, 65536, 32768, 21846, 16384, 13108, 10923, 9363, 8192,
+                                     7282, 6554, 5958, 5462, 5042, 4682, 4370, 4096 };
+
 // Rasterizes the tiles of [x0, x0 + 4*tilesX) x [y0, y0 + 4*tilesY) that are not provably empty
 // or hidden: 32 tiles are tested at a time (one per lane), then shade(mask, tpx, tpy, tmin) shades
-// the surviving ones.
+// the surviving ones. divMagic: kDiv16[tilesX] for a chunk (tilesX, tilesY <= 16), 0 otherwise.
 template <class Shade>
 __device__ __forceinline__ void raster_region_with(const TriRec& r, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
-                                                   const uint32_t* tileMin, uint32_t width, int lane, Shade&& shade) {
+                                                   const uint32_t* tileMin, uint32_t width, int lane, Shade&& shade,
+                                                   uint32_t divMagic) {
     const int T = tilesX * tilesY;
     const uint32_t tw = width >> 2;
     for (int tb = 0; tb < T; tb += 32) {
@@ -507,7 +513,7 @@ __device__ __forceinline__ void raster_region_with(const TriRec& r, uint32_t x0,
         bool live = false;
         uint32_t tpx = 0, tpy = 0, tmin = 0;
         if (t < T) {
-            int ty = t / tilesX, tx = t - ty * tilesX;
+            int ty = divMagic ? (int)(((uint32_t)t * divMagic) >> 16) : t / tilesX, tx = t - ty * tilesX;
             tpx = x0 + tx * 4, tpy = y0 + ty * 4;
             live = tile_live(r, tpx, tpy, tileMin, tw, &tmin);
         }
@@ -517,24 +523,26 @@ __device__ __forceinline__ void raster_region_with(const TriRec& r, uint32_t x0,
 
 // raster_region_with for an opaque triangle, two tiles per step.
 __device__ __forceinline__ void raster_region(const TriRec& r, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
-                                              unsigned long long* keys, uint32_t* tileMin, uint32_t width, int lane, uint32_t readTiles) {
+                                              unsigned long long* keys, uint32_t* tileMin, uint32_t width, int lane, uint32_t readTiles,
+                                              uint32_t divMagic = 0) {
     raster_region_with(r, x0, y0, tilesX, tilesY, tileMin, width, lane,
                        [&](unsigned mask, uint32_t tpx, uint32_t tpy, uint32_t tmin) {
                            shade_live_tiles([&](uint32_t) -> const TriRec& { return r; }, 0, mask, tpx, tpy, tmin, keys,
                                             tileMin, width, lane, readTiles);
-                       });
+                       }, divMagic);
 }
 
 // The same for the alpha-tested triangle *rp with alpha terms *xp (material texture tex, cutoff << 24).
 __device__ __forceinline__ void raster_region_alpha(const TriRec* rp, const AlphaExt* xp, const DevTexture& tex,
                                                     uint32_t cutoff, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
-                                                    unsigned long long* keys, uint32_t* tileMin, uint32_t width, int lane) {
+                                                    unsigned long long* keys, uint32_t* tileMin, uint32_t width, int lane,
+                                                    uint32_t divMagic = 0) {
     raster_region_with(*rp, x0, y0, tilesX, tilesY, tileMin, width, lane,
                        [&](unsigned mask, uint32_t tpx, uint32_t tpy, uint32_t tmin) {
                            shade_live_tiles_alpha([&](uint32_t) -> const TriRec& { return *rp; },
                                                   [&](uint32_t) -> const AlphaExt& { return *xp; }, 0, tex, cutoff, mask, tpx,
                                                   tpy, tmin, keys, tileMin, width, lane);
-                       });
+                       }, divMagic);
 }
 
 // ------------------------------------------------------------------ overdraw shader
@@ -582,12 +590,12 @@ __device__ __forceinline__ void shade_live_tiles_overdraw(Rec&& rec, uint32_t rs
 
 __device__ __forceinline__ void raster_region_overdraw(const TriRec& r, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
                                                        unsigned long long* keys, unsigned long long* counts,
-                                                       uint32_t width, int lane) {
+                                                       uint32_t width, int lane, uint32_t divMagic = 0) {
     raster_region_with(r, x0, y0, tilesX, tilesY, nullptr, width, lane,
                        [&](unsigned mask, uint32_t tpx, uint32_t tpy, uint32_t) {
                            shade_live_tiles_overdraw([&](uint32_t) -> const TriRec& { return r; }, 0, mask, tpx, tpy, keys,
                                                      counts, width, lane);
-                       });
+                       }, divMagic);
 }
 
 // One lane draws a whole triangle with the overdraw shader (the full-queue fallback of a clipped
@@ -1098,7 +1106,8 @@ __device__ __noinline__ void raster_chunk_alpha(const TriRec* q, const DevMateri
                                                 uint32_t width, int lane) {
     const AlphaExt* xp = (const AlphaExt*)&q[1];
     const DevMaterial& mt = materials[xp->material & ~kTriAlpha];
-    raster_region_alpha(q, xp, mt.tex, mt.alpha_cutoff << 24, x0, y0, tilesX, tilesY, keys, tileMin, width, lane);
+    raster_region_alpha(q, xp, mt.tex, mt.alpha_cutoff << 24, x0, y0, tilesX, tilesY, keys, tileMin, width, lane,
+                        kDiv16[tilesX]);
 }
 
 template <bool kOver>
@@ -1137,12 +1146,24 @@ __global__ void __launch_bounds__(256, 5) k_raster_big(const TriRec* __restrict_
         TriRec r = big[slot];
         unsigned long long base = bigBase[slot];
         unsigned long long next = slot + 1 < n ? bigBase[slot + 1] : total;
+        // the run's chunk of the triangle: one division where the run starts, then stepped
+        auto chunks_x = [&](const TriRec& t) { return ((((t.bbMax & 0xFFFF) - (t.bbMin & 0xFFFF)) >> 2) + cw - 1) / cw; };
+        uint32_t chunksX = chunks_x(r);
+        uint32_t cy = (uint32_t)(w0 - base) / chunksX, cx = (uint32_t)(w0 - base) - cy * chunksX;
         for (unsigned long long w = w0; w < w1; w++) {
-            while (w >= next) {  // the run crossed into the next triangle(s)
-                slot++;
-                base = next;
-                next = slot + 1 < n ? bigBase[slot + 1] : total;
-                if (w < next) r = big[slot];
+            if (w != w0) {
+                if (w >= next) {  // the run crossed into the next triangle(s): its chunk 0
+                    while (w >= next) {
+                        slot++;
+                        base = next;
+                        next = slot + 1 < n ? bigBase[slot + 1] : total;
+                        if (w < next) r = big[slot];
+                    }
+                    chunksX = chunks_x(r);
+                    cx = 0, cy = 0;
+                } else if (++cx == chunksX) {
+                    cx = 0, cy++;
+                }
             }
             unsigned long long* vkeys = keys;
             uint32_t* vtiles = tileMin;
@@ -1151,20 +1172,17 @@ __global__ void __launch_bounds__(256, 5) k_raster_big(const TriRec* __restrict_
                 const ViewParams& v = views[r.pad & ~kTriAlpha];
                 vkeys = v.keys, vtiles = v.tileMin, vwidth = v.width;
             }
-            const uint32_t c = (uint32_t)(w - base);
             const uint32_t minX = r.bbMin & 0xFFFF, minY = r.bbMin >> 16, maxX = r.bbMax & 0xFFFF, maxY = r.bbMax >> 16;
-            const uint32_t chunksX = (((maxX - minX) >> 2) + cw - 1) / cw;
-            const uint32_t cy = c / chunksX, cx = c - cy * chunksX;
             const uint32_t x0 = minX + cx * (cw * 4), y0 = minY + cy * (ch * 4);
             const uint32_t x1 = min(x0 + cw * 4, maxX), y1 = min(y0 + ch * 4, maxY);
             // Empty and hidden tiles of the chunk are rejected inside raster_region.
+            const int tilesX = (int)((x1 - x0) >> 2), tilesY = (int)((y1 - y0) >> 2);
             if constexpr (kOver) {
-                raster_region_overdraw(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys, counts, vwidth, lane);
+                raster_region_overdraw(r, x0, y0, tilesX, tilesY, vkeys, counts, vwidth, lane, kDiv16[tilesX]);
             } else if (r.pad & kTriAlpha) {
-                raster_chunk_alpha(big + slot, materials, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys,
-                                   vtiles, vwidth, lane);
+                raster_chunk_alpha(big + slot, materials, x0, y0, tilesX, tilesY, vkeys, vtiles, vwidth, lane);
             } else {
-                raster_region(r, x0, y0, (int)((x1 - x0) >> 2), (int)((y1 - y0) >> 2), vkeys, vtiles, vwidth, lane, readTiles);
+                raster_region(r, x0, y0, tilesX, tilesY, vkeys, vtiles, vwidth, lane, readTiles, kDiv16[tilesX]);
             }
         }
     }
