@@ -128,6 +128,7 @@ struct swr_neural_t {
     unsigned long long* pixelReq;
     unsigned long long* sorted;
     uint2* decoded;
+    uint4* surf;                             // two words per pixel: the emit pass's surface records
     size_t scratchSlots;
     uint32_t* counters;                      // counts | cursors | reqOffset | tileOffset, numMaterials+1 each,
                                              // then 4 per-level request counts

@@ -48,7 +48,8 @@ cudaError_t dev_alloc(T** p, size_t count) {
 
 void free_model(swr_neural_t* n) {
     void* ptrs[] = { n->tex, n->latent, n->latentM, n->latentV, n->latentGrad, n->latentHalf, n->params, n->paramM,
-                     n->paramV, n->image, n->partial, n->loss, n->status, n->pixelReq, n->sorted, n->decoded, n->counters };
+                     n->paramV, n->image, n->partial, n->loss, n->status, n->pixelReq, n->sorted, n->decoded, n->surf,
+                     n->counters };
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete n;

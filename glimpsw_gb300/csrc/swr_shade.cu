@@ -238,6 +238,16 @@ struct NeuralResolve {
     unsigned long long* pixelReq;      // [pixel * 4 + k] material<<32 | level<<28 | ty<<14 | tx
     uint32_t* counts;                  // [material]
     const uint2* decoded;              // [pixel * 4 + k] layer-0 RGBA8, layer-1 RGBA8
+    uint4* surf;                       // [pixel * 2 + 0..1] the emit pass's surface record (kSurf*)
+};
+// The emit pass's per-pixel surface record, which spares the second pass the reconstruction of a
+// tile whose pixels all have it (kSurfFast): word 0-1 barycentrics b1, b2; 2-4 the vertices'
+// normal/tangent words; 5-6 the decoded quad's filter fractions; 7 flags.
+enum : uint32_t {
+    kSurfFast = 1u,        // sampled from decoded texels, or untextured (albedo and NMR 0)
+    kSurfDecoded = 2u,     // a decoded material sample: fetch it
+    kSurfNearest = 4u, kSurfInX = 8u, kSurfInY = 16u, kSurfTwoLayers = 32u,
+    kSurfHand = 1u << 31,  // the bitangent's sign bit
 };
 
 __device__ __forceinline__ uint32_t sat_u8(int32_t v) { return (uint32_t)min(max(min(max(v, -32768), 32767), 0), 255); }
@@ -348,9 +358,46 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a, NeuralResolve nr
         }
     }
     if (skyBits != 0xFFFF) {
+        uint32_t ntg[3] = {}, hand = 0, albedo = 0, nmr = 0;
+        float b[3];
+        bool fast = false;  // the neural pass found the emit pass's records for the whole tile
+        if constexpr (kMode == kResolveNeural) {
+            uint4 s0 = make_uint4(0u, 0u, 0u, 0u), s1 = make_uint4(0u, 0u, 0u, 0u);
+            if (!isSky) s0 = nr.surf[(size_t)off * 2], s1 = nr.surf[(size_t)off * 2 + 1];
+            fast = (__ballot_sync(hm, isSky || (s1.w & kSurfFast)) & hm) == hm;
+            if (fast) {
+                const float nan = __int_as_float(0x7FFFFFFF);  // what the full path gives sky pixels
+                b[1] = isSky ? nan : __uint_as_float(s0.x);
+                b[2] = isSky ? nan : __uint_as_float(s0.y);
+                b[0] = 1 - b[1] - b[2];
+                ntg[0] = s0.z, ntg[1] = s0.w, ntg[2] = s1.x;
+                hand = s1.w & kSurfHand;
+                if (!isSky && (s1.w & kSurfDecoded)) {
+                    const ulonglong2* rq = (const ulonglong2*)(nr.pixelReq + (size_t)off * 4);
+                    const ulonglong2 r01 = rq[0], r23 = rq[1];
+                    auto at = [&](unsigned long long r, uint32_t k) {
+                        const size_t slot = (r != ~0ull && (r & kReqRedirect)) ? (size_t)(uint32_t)r : (size_t)off * 4 + k;
+                        return nr.decoded[slot];
+                    };
+                    const bool inX = s1.w & kSurfInX, inY = s1.w & kSurfInY;
+                    const uint2 d00 = at(r01.x, 0);
+                    uint2 r0 = d00;
+                    if (!(s1.w & kSurfNearest)) {
+                        const uint2 d10 = inX ? at(r01.y, 1) : d00, d01 = inY ? at(r23.x, 2) : d00;
+                        const uint2 d11 = inY ? (inX ? at(r23.y, 3) : d01) : d10;
+                        r0.x = filter_rgba8(d00.x, d10.x, d01.x, d11.x, s1.y, s1.z);
+                        r0.y = filter_rgba8(d00.y, d10.y, d01.y, d11.y, s1.y, s1.z);
+                    }
+                    albedo = r0.x;
+                    if (s1.w & kSurfTwoLayers) nmr = r0.y;
+                }
+            }
+        }
+        if (!fast) {
         // ---- ResolveSurface (Shading.cpp:471-579): waterfall over the tile's surface ids
         F3 pos[3] = {};
-        uint32_t tc[3] = {}, ntg[3] = {}, hand = 0, matId = 0;
+        uint32_t tc[3] = {}, matId = 0;
+        uint32_t sflags = kSurfFast, sfx = 0, sfy = 0;  // the emit pass's record of this pixel
         unsigned pending = (~skyBits) & 0xFFFF;
         while (pending) {
             const int src = __ffs(pending) - 1;
@@ -390,7 +437,6 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a, NeuralResolve nr
         const float r0x = su - p0x, r0y = sv - p0y;
         const float interpInvW = iw0 + r0x * dxs + r0y * dys;
         const float interpW = 1.0f / interpInvW;
-        float b[3];
         b[1] = interpW * (r0x * dx[1] + r0y * dy[1]);
         b[2] = interpW * (r0x * dx[2] + r0y * dy[2]);
         b[0] = 1 - b[1] - b[2];
@@ -413,7 +459,6 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a, NeuralResolve nr
         const float g2 = t10x * dy[1] + t20x * dy[2], g3 = t10y * dy[1] + t20y * dy[2];
 
         // waterfall over materials: filter chosen over the whole tile per material
-        uint32_t albedo = 0, nmr = 0;
         unsigned pm = (__ballot_sync(hm, !isSky && matId != 0xFFFFFFFFu) >> (16 * half)) & 0xFFFF;
         while (pm) {
             const int src = __ffs(pm) - 1;
@@ -437,6 +482,10 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a, NeuralResolve nr
                                      nr.tex[mid].width == tex.width && nr.tex[mid].height == tex.height;
                     if constexpr (kMode == kResolveEmit) {
                         uint32_t nq = 0;
+                        sflags = dec ? kSurfFast | kSurfDecoded | (nearest ? kSurfNearest : 0u) | (q.inX ? kSurfInX : 0u) |
+                                           (q.inY ? kSurfInY : 0u) | (tex.num_layers >= 2 ? kSurfTwoLayers : 0u)
+                                     : 0u;  // sampled from the plain texture: the second pass reconstructs
+                        sfx = q.fx, sfy = q.fy;
                         if (dec) {
                             const unsigned long long b = ((unsigned long long)mid << 32) | ((uint32_t)q.m << 28);
                             const uint32_t x0 = (uint32_t)q.tx, y0 = (uint32_t)q.ty;
@@ -489,8 +538,11 @@ __global__ void __launch_bounds__(256) k_resolve(ResolveArgs a, NeuralResolve nr
             uint4* dst = (uint4*)(nr.pixelReq + (size_t)off * 4);
             dst[0] = make_uint4((uint32_t)req[0], (uint32_t)(req[0] >> 32), (uint32_t)req[1], (uint32_t)(req[1] >> 32));
             dst[1] = make_uint4((uint32_t)req[2], (uint32_t)(req[2] >> 32), (uint32_t)req[3], (uint32_t)(req[3] >> 32));
+            nr.surf[(size_t)off * 2] = make_uint4(__float_as_uint(b[1]), __float_as_uint(b[2]), ntg[0], ntg[1]);
+            nr.surf[(size_t)off * 2 + 1] = make_uint4(ntg[2], sfx, sfy, sflags | hand);
             return;
         }
+        }  // !fast
         F3 nrm[3], tan[3];
 #pragma unroll
         for (int k = 0; k < 3; k++) {
@@ -821,10 +873,12 @@ swr_status swr_resolve_neural(swr_rasterizer r, swr_framebuffer fb, const swr_sh
         if (n->pixelReq) cudaFree(n->pixelReq);
         if (n->sorted) cudaFree(n->sorted);
         if (n->decoded) cudaFree(n->decoded);
-        n->pixelReq = n->sorted = nullptr, n->decoded = nullptr, n->scratchSlots = 0;
+        if (n->surf) cudaFree(n->surf);
+        n->pixelReq = n->sorted = nullptr, n->decoded = nullptr, n->surf = nullptr, n->scratchSlots = 0;
         e = cudaMalloc(&n->pixelReq, slots * sizeof(unsigned long long));
         if (e == cudaSuccess) e = cudaMalloc(&n->sorted, slots * sizeof(unsigned long long));
         if (e == cudaSuccess) e = cudaMalloc(&n->decoded, slots * sizeof(uint2));
+        if (e == cudaSuccess) e = cudaMalloc(&n->surf, slots / 4 * 2 * sizeof(uint4));
         if (e != cudaSuccess) {
             if (a.lights) cudaFreeAsync((void*)a.lights, st);
             return swr_internal_cuda_fail(e, "swr_resolve_neural: scratch");
@@ -839,7 +893,7 @@ swr_status swr_resolve_neural(swr_rasterizer r, swr_framebuffer fb, const swr_sh
     uint32_t* levelCount = tileOffset + (M + 1);
     NeuralResolve nr = {};
     nr.tex = n->d.tex, nr.numMaterials = M, nr.decodedLevels = n->d.levels + 2;
-    nr.pixelReq = n->pixelReq, nr.counts = counts, nr.decoded = n->decoded;
+    nr.pixelReq = n->pixelReq, nr.counts = counts, nr.decoded = n->decoded, nr.surf = n->surf;
     const uint32_t tiles = (fb->width / 4) * (fb->height / 4), blocks = (tiles * 16 + 255) / 256;
     e = cudaMemsetAsync(counts, 0, 2 * (M + 1) * sizeof(uint32_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(levelCount, 0, kNeuralMaxDecoded * sizeof(uint32_t), st);
