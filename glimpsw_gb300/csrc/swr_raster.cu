@@ -360,6 +360,13 @@ __device__ __forceinline__ bool enqueue_alpha(const TriRec& r, const AlphaExt& x
     return false;
 }
 
+// A small triangle's record (the mesh stage's tile walk): pad = tilesX | row_magic << 8 | kPadReadKey.
+constexpr uint32_t kPadReadKey = 1u << 24;
+// The 4x4 tiles of a triangle's render box.
+__device__ __forceinline__ uint32_t triangle_tiles(const TriRec& r) {
+    return (((r.bbMax & 0xFFFF) - (r.bbMin & 0xFFFF)) >> 2) * (((r.bbMax >> 16) - (r.bbMin >> 16)) >> 2);
+}
+
 // Largest value over the tile [px, px+3] x [py, py+3] of the affine edge function e(px, py) + A*dx + B*dy.
 __device__ __forceinline__ int32_t tile_max_edge(int32_t e, int32_t A, int32_t B) {
     return e + (A > 0 ? 3 * A : 0) + (B > 0 ? 3 * B : 0);
@@ -426,10 +433,10 @@ __device__ __forceinline__ unsigned long long tile_pixel_key(const TriRec& r, ui
 // bounds (each pixel reports a lower bound of its depth word afterwards). Four tiles per step: each
 // half-warp takes two, and a lane's two key loads are issued together (the walk is bound by their
 // latency).
-template <class Rec>
-__device__ __forceinline__ void shade_live_tiles(Rec&& rec, uint32_t rsel, unsigned mask, uint32_t tpx, uint32_t tpy,
-                                                 uint32_t tmin, unsigned long long* keys, uint32_t* tileMin, uint32_t width,
-                                                 int lane, uint32_t readTiles) {
+template <class Rec, class ReadKey>
+__device__ __forceinline__ void shade_live_tiles(Rec&& rec, ReadKey&& readKey, uint32_t rsel, unsigned mask, uint32_t tpx,
+                                                 uint32_t tpy, uint32_t tmin, unsigned long long* keys, uint32_t* tileMin,
+                                                 uint32_t width, int lane) {
     const uint32_t half = lane >> 4, tw = width >> 2, l = lane & 15;
     const uint32_t txy = tpx | (tpy << 16);  // tile origins are below 2896
     while (mask) {
@@ -447,13 +454,11 @@ __device__ __forceinline__ void shade_live_tiles(Rec&& rec, uint32_t rsel, unsig
         unsigned long long* pa = keys + (ax << 2) + ay * width + l;
         unsigned long long* pb = keys + (bx << 2) + by * width + l;
         // The key read filters losing atomics and gives the tile bound each pixel's new depth. For
-        // triangles above readTiles tiles (0: none) it is skipped: the atomic is unconditional and a
-        // pixel's bound is max(new depth, old tile bound), still a lower bound of its final key.
-        auto tiles_of = [](const TriRec& r) {
-            return (((r.bbMax & 0xFFFF) - (r.bbMin & 0xFFFF)) >> 2) * (((r.bbMax >> 16) - (r.bbMin >> 16)) >> 2);
-        };
-        const bool readA = srcA >= 0 && (readTiles == 0 || tiles_of(rec(ar)) <= readTiles);
-        const bool readB = srcB >= 0 && (readTiles == 0 || tiles_of(rec(br)) <= readTiles);
+        // triangles whose readKey(selector) is false (above the draw's keyReadTiles tiles) it is
+        // skipped: the atomic is unconditional and a pixel's bound is max(new depth, old tile
+        // bound), still a lower bound of its final key.
+        const bool readA = srcA >= 0 && readKey(ar);
+        const bool readB = srcB >= 0 && readKey(br);
         const unsigned long long curA = readA ? *(volatile unsigned long long*)pa : 0ull;
         const unsigned long long curB = readB ? *(volatile unsigned long long*)pb : 0ull;
         const unsigned long long keyA = srcA >= 0 ? tile_pixel_key(rec(ar), ax, ay, l) : 0ull;
@@ -525,10 +530,11 @@ __device__ __forceinline__ void raster_region_with(const TriRec& r, uint32_t x0,
 __device__ __forceinline__ void raster_region(const TriRec& r, uint32_t x0, uint32_t y0, int tilesX, int tilesY,
                                               unsigned long long* keys, uint32_t* tileMin, uint32_t width, int lane, uint32_t readTiles,
                                               uint32_t divMagic = 0) {
+    const bool readKey = readTiles == 0 || triangle_tiles(r) <= readTiles;
     raster_region_with(r, x0, y0, tilesX, tilesY, tileMin, width, lane,
                        [&](unsigned mask, uint32_t tpx, uint32_t tpy, uint32_t tmin) {
-                           shade_live_tiles([&](uint32_t) -> const TriRec& { return r; }, 0, mask, tpx, tpy, tmin, keys,
-                                            tileMin, width, lane, readTiles);
+                           shade_live_tiles([&](uint32_t) -> const TriRec& { return r; }, [&](uint32_t) { return readKey; }, 0,
+                                            mask, tpx, tpy, tmin, keys, tileMin, width, lane);
                        }, divMagic);
 }
 
@@ -952,8 +958,10 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                     if (kPass == kPassOpaque && det > 0 && tiny_box(t, vp.halfW, vp.halfH, bbMin, bbMax, tb)) {
                         shade_tiny(r, tb, vp.keys, vp.width);
                     } else if (tilesX * tilesY <= kSmallTiles) {
-                        // tile index -> row by a multiply-shift (exact for tile < 16, tilesX <= 16)
-                        r.pad = (uint32_t)tilesX | (row_magic(tilesX) << 8);
+                        // tile index -> row by a multiply-shift (exact for tile < 16, tilesX <= 16), and
+                        // whether the shading reads the keys before its atomics (keyReadTiles)
+                        r.pad = (uint32_t)tilesX | (row_magic(tilesX) << 8) |
+                                (a.keyReadTiles == 0 || (uint32_t)(tilesX * tilesY) <= a.keyReadTiles ? kPadReadKey : 0u);
                         tris[lane].v = r;
                         if constexpr (kAlpha) S.exts[lane].v = x;
                         myTiles = tilesX * tilesY;
@@ -1039,7 +1047,7 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                 if (t < total) {
                     const TriRec& r = tris[own].v;
                     const int tile = t - ownerExcl;
-                    const int tilesX = r.pad & 0xFF, magic = r.pad >> 8;
+                    const int tilesX = r.pad & 0xFF, magic = (r.pad >> 8) & 0x1FF;
                     const int ty = (tile * magic) >> 8, tx = tile - ty * tilesX;
                     tpx = (r.bbMin & 0xFFFF) + tx * 4, tpy = (r.bbMin >> 16) + ty * 4;
                     live = tile_live(r, tpx, tpy, vp.tileMin, tw, &tmin, S.zmax[own]);
@@ -1055,8 +1063,9 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                     shade_live_tiles_overdraw([&](uint32_t q) -> const TriRec& { return tris[q].v; }, own, liveMask, tpx, tpy,
                                               vp.keys, a.counts, vp.width, lane);
                 } else {
-                    shade_live_tiles([&](uint32_t q) -> const TriRec& { return tris[q].v; }, own, liveMask, tpx, tpy, tmin,
-                                     vp.keys, vp.tileMin, vp.width, lane, a.keyReadTiles);
+                    shade_live_tiles([&](uint32_t q) -> const TriRec& { return tris[q].v; },
+                                     [&](uint32_t q) { return (tris[q].v.pad & kPadReadKey) != 0u; }, own, liveMask, tpx, tpy,
+                                     tmin, vp.keys, vp.tileMin, vp.width, lane);
                 }
             }
             // Triangles the full queue turned away are rasterized here by the whole warp.
