@@ -104,7 +104,8 @@ static_assert(sizeof(AlphaExt) == sizeof(TriRec) && offsetof(AlphaExt, zero0) ==
 // Per-rasterizer device scratch, reused by every draw.
 struct DrawScratch {
     unsigned long long* control;   // [0] meshlet work counter, [1] big-triangle queue (slots<<40 | chunks),
-                                   // [2] status flags, [3..6] perf counters, [8] chunk-stage cursor,
+                                   // [2] status flags, [3..6] perf counters, [7] the second pass's work
+                                   // counter of a single-view draw, [8] chunk-stage cursor,
                                    // [9] alpha list length, [10] alpha-pass cursor,
                                    // [11] / [12] warps done in the opaque / alpha pass
     TriRec* big;                   // queue of triangles rasterized by the chunk kernel

@@ -108,6 +108,9 @@ __device__ __forceinline__ void shade_fragment(const TriRec& r, uint32_t px, uin
 // covered pixels. A triangle degenerate in fixed point (det 0) can pass samples on its whole line
 // and keeps the walk.
 constexpr uint32_t kTinyPixels = 2;
+// A meshlet is drawn in the single-view draw's first pass when its bounding sphere's radius exceeds
+// this share of the clip w of its centre (about 94 pixels at 1920 pixels across and 60 degrees).
+constexpr float kLargeMeshlet = 0.1f;
 struct TinyBox { uint32_t x0, y0, x1, y1; };  // inclusive pixel range
 __device__ __forceinline__ bool tiny_box(const Setup& t, int halfW, int halfH, uint32_t bbMin, uint32_t bbMax,
                                          TinyBox& b) {
@@ -788,6 +791,11 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
     uint32_t fetchView = 0;                // batched draws: the view of the fetched group
     unsigned fetchMask = 0;                // lanes of the fetched group whose meshlet is visible
     uint32_t fetchGroup = kDrawGroup;      // single view: positions per fetch
+    // Single-view draws walk their positions twice: meshlets large on screen first, then the rest
+    // (a second cursor, control[7]), so the costliest work items start early and the last ones
+    // are small: a cheaper tail, and near geometry raises the tile depth bounds before the far.
+    const bool twoPass = !multi && !kAlpha && !kShaded;
+    uint32_t pass = twoPass ? 0u : 1u;
     while (true) {
         uint32_t m, view = 0, item;
         if constexpr (kAlpha) {
@@ -837,14 +845,26 @@ __global__ void __launch_bounds__(512, 2) k_draw_meshlets(DrawArgs a) {
                 // the last work items spread evenly over the warps).
                 if (fetchMask == 0) {
                     uint32_t b = 0;
-                    if (lane == 0) b = (uint32_t)atomicAdd(cursor, (unsigned long long)fetchGroup);
+                    if (lane == 0) b = (uint32_t)atomicAdd(twoPass && pass == 1 ? &a.s.control[7] : cursor,
+                                                           (unsigned long long)fetchGroup);
                     const uint32_t base = __shfl_sync(0xFFFFFFFFu, b, 0);
-                    if (base >= totalItems) break;
+                    if (base >= totalItems) {
+                        if (pass == 0) {  // the large meshlets are all taken: the rest from position 0
+                            pass = 1, fetchGroup = kDrawGroup;
+                            continue;
+                        }
+                        break;
+                    }
                     const uint32_t q = base + lane;
                     bool vis = false;
                     if (lane < fetchGroup && q < totalItems) {
                         laneMeshlet = draw_order(q, a.count, a.orderStride);
                         vis = a.cullBitmap == nullptr || ((a.cullBitmap[laneMeshlet >> 4] >> (laneMeshlet & 15)) & 1);
+                        if (vis && twoPass) {  // bounding sphere radius against the clip w of its centre
+                            const float4 sp = *(const float4*)(a.meshlets + (size_t)(a.meshletOffset + laneMeshlet) * kMeshletSize);
+                            const float w = fmaf(sp.x, a.m[3], fmaf(sp.y, a.m[7], fmaf(sp.z, a.m[11], a.m[15])));
+                            vis = (sp.w > kLargeMeshlet * w) == (pass == 0);
+                        }
                     }
                     fetchMask = __ballot_sync(0xFFFFFFFFu, vis);
                     const int got = __popc(fetchMask);
@@ -1127,8 +1147,8 @@ __global__ void __launch_bounds__(256, 5) k_raster_big(const TriRec* __restrict_
                                                     const DevMaterial* __restrict__ materials, unsigned long long* counts,
                                                     uint32_t readTiles) {
     const unsigned long long q = control[1];
-    if (blockIdx.x == 0 && threadIdx.x == 0)  // the next draw's alpha list and idle-warp counts
-        control[9] = control[10] = control[11] = control[12] = 0;
+    if (blockIdx.x == 0 && threadIdx.x == 0)  // the next draw's second cursor, alpha list and idle-warp counts
+        control[7] = control[9] = control[10] = control[11] = control[12] = 0;
     const uint32_t n = (uint32_t)min((unsigned long long)capacity, q >> 40);
     if (n == 0) return;
     const int lane = threadIdx.x & 31;
